@@ -1,0 +1,216 @@
+"""Seeded scenario generators written as UMANS scenario XML.
+
+Every workload is written in the reference's own scenario format
+(``<Simulation>/<World>/<Policies>/<Agents>``, parsed by
+``CrowdSimulator::FromConfigFile``, src/Engine/core/crowdSimulator.cpp:516-647),
+so the same file drives the reference CPU engine, the CPU oracle and this
+engine.  Coordinates are written with 9 significant digits, which round-trips
+every float32 value exactly through ``strtof``.
+
+Workloads (agent counts can be reduced for tests with ``n=``):
+
+* ``circle_orca``          50 agents on a circle of radius 25 m, antipodal goals,
+                           ORCA (global method, range 8, time horizon 5), dt 0.1.
+* ``socialforces_toric``   100k agents uniform in a 400x400 m toric world,
+                           SocialForcesAvoidance(range 5) + GoalReachingForce,
+                           gradient method, dt 0.1.
+* ``karamouzas_corridor``  two opposing flows on a jittered 1 m lattice,
+                           Karamouzas(range 10), regular sampling 10 speeds x 20
+                           angles + base = 181 samples, dt 0.05.
+* ``batch_mixed``          4096 independent scenarios, agent counts log-uniform in
+                           [8, 2048], circle / random-square layouts, policies
+                           cycling ORCA / PowerLaw-sampling / SocialForces-gradient.
+* ``calibration_set``      512 agents in a 40x40 m square with one parameter set of
+                           SocialForcesAvoidance + PowerLaw + GoalReachingForce.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def _f(x) -> str:
+    return "%.9g" % float(np.float32(x))
+
+
+ORCA_POLICY = (
+    '<Policy id="{pid}" OptimizationMethod="global" RelaxationTime="0">'
+    '<costfunction name="ORCA" range="8" timeHorizon="5"/></Policy>')
+
+SF_POLICY = (
+    '<Policy id="{pid}" OptimizationMethod="gradient" RelaxationTime="0.5">'
+    '<costfunction name="SocialForcesAvoidance" range="5"{sfparams}/>'
+    '<costfunction name="GoalReachingForce"/></Policy>')
+
+POWERLAW_SAMPLING_POLICY = (
+    '<Policy id="{pid}" OptimizationMethod="sampling" SamplingType="regular" '
+    'SamplingBase="zero" SamplingBaseDirection="unit" SamplingAngle="360" '
+    'SpeedSamples="4" AngleSamples="36" SamplingRadius="maximum speed" '
+    'RelaxationTime="0.5">'
+    '<costfunction name="PowerLaw" range="5"/>'
+    '<costfunction name="GoalReachingForce"/></Policy>')
+
+KARAMOUZAS_POLICY = (
+    '<Policy id="{pid}" OptimizationMethod="sampling" SamplingType="regular" '
+    'SamplingBase="zero" SamplingBaseDirection="preferred velocity" '
+    'SamplingAngle="180" SpeedSamples="10" AngleSamples="20" '
+    'IncludeBaseAsSample="true" SamplingRadius="maximum speed" RelaxationTime="0">'
+    '<costfunction name="Karamouzas" range="10"/></Policy>')
+
+CALIBRATION_POLICY = (
+    '<Policy id="{pid}" OptimizationMethod="gradient" RelaxationTime="0.5">'
+    '<costfunction name="SocialForcesAvoidance" range="5" V0="{V0}" sigma="{sigma}"/>'
+    '<costfunction name="PowerLaw" range="5" k="{k}" tau0="{tau0}"/>'
+    '<costfunction name="GoalReachingForce"/></Policy>')
+
+
+@dataclass
+class Scenario:
+    """A scenario in memory: world, policies (XML snippets) and agents."""
+    dt: float
+    world: str                      # "Infinite" or "Toric"
+    width: float = 0.0
+    height: float = 0.0
+    end_time: float | None = None
+    policies: list[str] = field(default_factory=list)
+    pos: np.ndarray = None          # (n, 2) float32
+    goal: np.ndarray = None         # (n, 2) float32
+    radius: np.ndarray = None       # (n,) float32
+    pref_speed: np.ndarray = None   # (n,) float32
+    max_speed: np.ndarray = None    # (n,) float32
+    policy_id: np.ndarray = None    # (n,) int
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    def to_xml(self) -> str:
+        w = (f'<World type="Toric" width="{_f(self.width)}" height="{_f(self.height)}"/>'
+             if self.world == "Toric" else '<World type="Infinite"/>')
+        end = f' end_time="{_f(self.end_time)}"' if self.end_time is not None else ""
+        out = ['<?xml version="1.0" encoding="utf-8"?>',
+               f'<Simulation delta_time="{_f(self.dt)}"{end}>', w,
+               "<Policies>", *self.policies, "</Policies>", "<Agents>"]
+        for i in range(self.n):
+            out.append(
+                f'<Agent rad="{_f(self.radius[i])}" pref_speed="{_f(self.pref_speed[i])}" '
+                f'max_speed="{_f(self.max_speed[i])}">'
+                f'<pos x="{_f(self.pos[i, 0])}" y="{_f(self.pos[i, 1])}"/>'
+                f'<goal x="{_f(self.goal[i, 0])}" y="{_f(self.goal[i, 1])}"/>'
+                f'<Policy id="{int(self.policy_id[i])}"/></Agent>')
+        out += ["</Agents>", "</Simulation>", ""]
+        return "\n".join(out)
+
+    def write(self, path: str) -> str:
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        with open(path, "w") as fh:
+            fh.write(self.to_xml())
+        return path
+
+
+def _agents(n, pos, goal, radius=0.3, pref=1.3, maxs=1.8, pid=0):
+    f32 = np.float32
+    return dict(pos=np.asarray(pos, f32).reshape(n, 2),
+                goal=np.asarray(goal, f32).reshape(n, 2),
+                radius=np.full(n, radius, f32) if np.isscalar(radius) else np.asarray(radius, f32),
+                pref_speed=np.full(n, pref, f32) if np.isscalar(pref) else np.asarray(pref, f32),
+                max_speed=np.full(n, maxs, f32) if np.isscalar(maxs) else np.asarray(maxs, f32),
+                policy_id=np.full(n, pid, np.int64) if np.isscalar(pid) else np.asarray(pid, np.int64))
+
+
+def circle_orca(n: int = 50, radius_m: float = 25.0, steps: int = 300) -> Scenario:
+    """n agents evenly spaced on a circle, goals at the antipodal points, ORCA."""
+    ang = 2.0 * np.pi * np.arange(n) / n
+    pos = np.stack([radius_m * np.cos(ang), radius_m * np.sin(ang)], 1)
+    return Scenario(dt=0.1, world="Infinite", end_time=steps * 0.1,
+                    policies=[ORCA_POLICY.format(pid=0)],
+                    **_agents(n, pos, -pos))
+
+
+def socialforces_toric(n: int = 100_000, side: float = 400.0, seed: int = 2,
+                       density: float | None = None) -> Scenario:
+    """Uniform agents and goals in a toric square; SocialForces + goal force.
+
+    ``density`` (agents per m^2), when given, overrides ``side`` so that a
+    reduced ``n`` keeps the neighbourhood size of the full workload
+    (100k agents in 400x400 m = 0.625 agents/m^2).
+    """
+    if density is not None:
+        side = math.sqrt(n / density)
+    rng = np.random.default_rng(seed)
+    h = side / 2.0
+    pos = rng.uniform(-h, h, (n, 2))
+    goal = rng.uniform(-h, h, (n, 2))
+    pref = np.clip(rng.normal(1.3, 0.1, n), 0.8, 1.8)
+    return Scenario(dt=0.1, world="Toric", width=side, height=side,
+                    policies=[SF_POLICY.format(pid=0, sfparams="")],
+                    **_agents(n, pos, goal, pref=pref))
+
+
+def karamouzas_corridor(n: int = 1_000_000, width: float = 100.0, seed: int = 3) -> Scenario:
+    """Two opposing flows on a jittered 1 m lattice (1 agent/m^2).
+
+    The corridor is ``width`` m high and as long as needed for n agents at one
+    agent per m^2; the left half walks to x=+L/2, the right half to x=-L/2.
+    """
+    rng = np.random.default_rng(seed)
+    rows = int(width)
+    cols = int(math.ceil(n / rows))
+    length = float(cols)
+    xs = -length / 2 + 0.5 + np.arange(cols)
+    ys = -width / 2 + 0.5 + np.arange(rows)
+    gx, gy = np.meshgrid(xs, ys, indexing="ij")
+    pos = np.stack([gx.ravel(), gy.ravel()], 1)[:n]
+    pos = pos + rng.uniform(-0.25, 0.25, pos.shape)
+    left = pos[:, 0] < 0
+    goal = pos.copy()
+    goal[:, 0] = np.where(left, length / 2, -length / 2)
+    return Scenario(dt=0.05, world="Infinite",
+                    policies=[KARAMOUZAS_POLICY.format(pid=0)],
+                    **_agents(n, pos, goal))
+
+
+def batch_counts(num: int = 4096, seed: int = 4, lo: int = 8, hi: int = 2048) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(math.log(lo), math.log(hi), num))).astype(np.int64)
+
+
+def batch_member(k: int, n: int, seed: int = 4) -> Scenario:
+    """Scenario k of the mixed batch: layout alternates circle / random square,
+    policy cycles ORCA / PowerLaw-sampling / SocialForces-gradient."""
+    rng = np.random.default_rng([seed, k])
+    if k % 2 == 0:
+        r = max(n * 1.5 / (2 * math.pi), 2.0)
+        ang = 2.0 * np.pi * np.arange(n) / n
+        pos = np.stack([r * np.cos(ang), r * np.sin(ang)], 1)
+        goal = -pos
+    else:
+        side = math.sqrt(n / 0.5)
+        pos = rng.uniform(-side / 2, side / 2, (n, 2))
+        goal = rng.uniform(-side / 2, side / 2, (n, 2))
+    kind = k % 3
+    pol = [ORCA_POLICY, POWERLAW_SAMPLING_POLICY, SF_POLICY][kind].format(pid=0, sfparams="")
+    return Scenario(dt=0.1, world="Infinite", policies=[pol], **_agents(n, pos, goal))
+
+
+DEFAULT_CALIBRATION = dict(V0=2.1, sigma=0.3, k=1.5, tau0=3.0)
+
+
+def calibration_params(sets: int = 256, seed: int = 5) -> np.ndarray:
+    """(sets, 4) float32 parameters (V0, sigma, k, tau0), each within +-30% of default."""
+    rng = np.random.default_rng(seed)
+    base = np.array([DEFAULT_CALIBRATION[k] for k in ("V0", "sigma", "k", "tau0")], np.float64)
+    return (base * rng.uniform(0.7, 1.3, (sets, 4))).astype(np.float32)
+
+
+def calibration_set(params=None, n: int = 512, side: float = 40.0, seed: int = 5) -> Scenario:
+    """One parameter set of the calibration workload (shared seeded layout)."""
+    p = DEFAULT_CALIBRATION if params is None else dict(zip(("V0", "sigma", "k", "tau0"), map(float, params)))
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-side / 2, side / 2, (n, 2))
+    goal = rng.uniform(-side / 2, side / 2, (n, 2))
+    pol = CALIBRATION_POLICY.format(pid=0, **{k: _f(v) for k, v in p.items()})
+    return Scenario(dt=0.1, world="Infinite", policies=[pol], **_agents(n, pos, goal))
