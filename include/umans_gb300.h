@@ -1,0 +1,132 @@
+/* umans_gb300: GB300 engine for the UMANS per-step agent update.
+ *
+ * C ABI.  Plain pointers and sizes; no CUDA or torch types.
+ *
+ * Part 1 is the reference's own library interface, same names, argument
+ * meaning and error behaviour (src/Library/APIFunctions.h:30-113 of UMANS).
+ * The reference declares its out-parameters as C++ references (float&,
+ * AgentData*&, int&); at the ABI level those are pointers, as declared here,
+ * so a program built against the reference header links against this
+ * library unchanged.
+ *
+ * Part 2 is a re-entrant handle interface: any number of simulations, one
+ * CUDA stream each, integer status codes (0 = success) and a per-handle
+ * error string.
+ */
+#ifndef UMANS_GB300_H
+#define UMANS_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Agent status exchanged with external applications
+ * (src/Library/APIFunctions.h:33-49). */
+struct AgentData {
+	int id;
+	float position_x;
+	float position_y;
+	float velocity_x;
+	float velocity_y;
+	float viewingDirection_x;
+	float viewingDirection_y;
+};
+
+/* ---- Part 1: reference-compatible global simulation ---------------------
+ * One process-wide simulation, like the reference (APIFunctions.cpp:35-45);
+ * callers serialise.  nrThreads is accepted and ignored (the step runs on
+ * the GPU). */
+
+/* replaces StartSimulation, APIFunctions.h:52 / .cpp:47-70 */
+bool StartSimulation(const char* configFileName, int nrThreads);
+/* replaces GetSimulationTimeStep, APIFunctions.h:57 / .cpp:72-79 */
+bool GetSimulationTimeStep(float* result_dt);
+/* replaces DoSimulationSteps, APIFunctions.h:63 / .cpp:81-88 */
+bool DoSimulationSteps(int nrSteps);
+/* replaces GetAgentPositions, APIFunctions.h:71 / .cpp:90-115; the buffer is
+ * owned by the library and stays valid until the next call that resizes it
+ * or CleanUp. */
+bool GetAgentPositions(struct AgentData** result_agentData, int* result_nrAgents);
+/* replaces SetAgentPositions, APIFunctions.h:77 / .cpp:117-137 */
+bool SetAgentPositions(struct AgentData* agentData, int nrAgents);
+/* replaces AddAgent, APIFunctions.h:92 / .cpp:139-171 (desiredID -1 = any) */
+bool AddAgent(float x, float y, float radius, float prefSpeed, float maxSpeed, float maxAcceleration,
+              int policyID, int* result_id, int desiredID);
+/* replaces RemoveAgent, APIFunctions.h:98 / .cpp:173-180 */
+bool RemoveAgent(int id);
+/* replaces SetAgentGoal, APIFunctions.h:106 / .cpp:182-194 */
+bool SetAgentGoal(int id, float x, float y);
+/* replaces CleanUp, APIFunctions.h:111 / .cpp:196-206 */
+bool CleanUp(void);
+
+/* ---- Part 2: handle interface --------------------------------------------
+ * Each entry point replaces the reference path named beside it. */
+typedef struct umans_sim umans_sim;
+
+enum umans_status {
+	UMANS_OK = 0,
+	UMANS_ERR_ARGUMENT = 1,   /* null handle/pointer, bad size */
+	UMANS_ERR_LOAD = 2,       /* scenario rejected (CrowdSimulator::FromConfigFile returned null) */
+	UMANS_ERR_CUDA = 3,       /* CUDA runtime error */
+	UMANS_ERR_DEVICE = 4,     /* device-reported condition, e.g. neighbour capacity exceeded */
+	UMANS_ERR_NOT_FOUND = 5   /* unknown agent or policy id */
+};
+
+/* CrowdSimulator::FromConfigFile (crowdSimulator.cpp:516-647) */
+int umans_create(const char* config_file, umans_sim** out);
+/* as umans_create; max_neighbours <= 0 and cells_per_range <= 0 pick defaults */
+int umans_create_ex(const char* config_file, int max_neighbours, float cells_per_range, int use_graph,
+                    umans_sim** out);
+int umans_destroy(umans_sim* sim);
+/* CrowdSimulator::RunSimulationSteps (crowdSimulator.cpp:77-95): n steps,
+ * waits for them, reports device-side errors */
+int umans_step(umans_sim* sim, int nsteps);
+/* enqueue n steps on the simulation's stream without waiting */
+int umans_step_async(umans_sim* sim, int nsteps);
+int umans_synchronize(umans_sim* sim);
+int umans_num_agents(umans_sim* sim, int* n);
+int umans_time(umans_sim* sim, double* t);          /* WorldBase::GetCurrentTime */
+int umans_dt(umans_sim* sim, float* dt);            /* WorldBase::GetDeltaTime */
+int umans_end_time(umans_sim* sim, float* t);       /* scenario end_time (FLT_MAX if absent) */
+/* state in list order (WorldBase::GetAgents): ids[n], pos/vel/viewdir[2n];
+ * any pointer may be null; cap = capacity in agents */
+int umans_get_state(umans_sim* sim, int* ids, float* pos, float* vel, float* viewdir, int cap);
+/* preferred velocities and goals of the last step, [2n] each (may be null) */
+int umans_get_aux(umans_sim* sim, float* prefvel, float* goal, int cap);
+/* overwrite pos/vel/viewdir of all agents, list order (Agent::setPosition,
+ * Agent::setVelocity_ExternalApplication); null pointers leave a field */
+int umans_set_state(umans_sim* sim, const float* pos, const float* vel, const float* viewdir);
+/* SetAgentPositions (APIFunctions.cpp:117-137): by id, unknown ids skipped */
+int umans_set_agents(umans_sim* sim, const struct AgentData* agents, int n);
+/* GetAgentPositions (APIFunctions.cpp:90-115) into a caller buffer of cap records */
+int umans_get_agents(umans_sim* sim, struct AgentData* out, int cap, int* n);
+int umans_add_agent(umans_sim* sim, float x, float y, float radius, float pref_speed, float max_speed,
+                    float max_acceleration, int policy_id, int desired_id, int* out_id);
+int umans_remove_agent(umans_sim* sim, int id);
+int umans_set_goal(umans_sim* sim, int id, float x, float y);
+/* Neighbour lists the next step uses (Agent::ComputeNeighbors,
+ * agent.cpp:43-50): per agent in list order, up to `cap` neighbour ids and
+ * PhantomAgent distSqr values at [i*cap, i*cap+cap); counts[i] = full length. */
+int umans_neighbours(umans_sim* sim, int cap, int* ids, float* dist2, int* counts);
+/* neighbour-list capacity in use (entries per agent) */
+int umans_max_neighbours(umans_sim* sim, int* cap);
+/* the CUDA stream (cudaStream_t) the steps run on, for event timing */
+int umans_stream(umans_sim* sim, void** stream);
+/* device addresses of the float2 position / velocity arrays (list order) */
+int umans_device_state(umans_sim* sim, void** pos, void** vel);
+/* Profiling: when enabled, each step runs without the CUDA graph and is
+ * bracketed by CUDA events on the simulation's stream (whole step, and the
+ * fused per-agent kernel); totals accumulate until the next umans_profile. */
+int umans_profile(umans_sim* sim, int enable);
+int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_ms, int* steps,
+                         int* kernels_per_step);
+/* the last error of this handle, or of the last failed umans_create when sim is null */
+const char* umans_last_error(umans_sim* sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

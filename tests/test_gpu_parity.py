@@ -1,0 +1,115 @@
+"""Parity of the CUDA engine with the reference, through the C ABI.
+
+* trajectories against the golden fixtures made by the reference engine:
+  max per-agent position deviation <= 1e-4 m over the first 100 steps;
+* neighbour lists against the reference's lists (same ids, same order up to
+  distance ties) and, on arbitrary positions, against the CPU oracle;
+* full-size workloads against the CPU oracle for a few steps, plus
+  size-independent properties (determinism, finiteness, no capacity overflow).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, neighbour_lists
+from oracle.port import PortSim
+from test_oracle_golden import assert_same_list
+from umans_gb300 import Simulation, scenarios as S
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4   # m over the first 100 steps (spec bound)
+THREADS = os.cpu_count() or 4
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_trajectory_matches_reference(name, golden_xml):
+    path, g = golden_xml(name)
+    sim = Simulation(path)
+    assert np.array_equal(sim.state()["ids"], g["ids"])
+    done, worst = 0, 0.0
+    for k, s in enumerate(g["steps"]):
+        sim.step(int(s) - done)
+        done = int(s)
+        pos = sim.positions()
+        dev = float(np.abs(pos - g["pos"][k]).max()) if len(pos) else 0.0
+        assert np.isfinite(pos).all()
+        if s <= 100:
+            worst = max(worst, dev)
+    print(f"{name}: max deviation over {done} steps = {worst:.3g} m")
+    assert worst <= TOL, f"{name}: max deviation {worst} m"
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if n.startswith(("toric60", "orca_circle50",
+                                                                          "socialforces_toric", "karamouzas"))])
+def test_neighbour_lists_match_reference(name, golden_xml):
+    path, g = golden_xml(name)
+    sim = Simulation(path)
+    ref = neighbour_lists(g, 1)
+    ids, d2, cnt = sim.neighbours(cap=512)
+    for i, (rid, rd2) in enumerate(ref):
+        k = int(cnt[i])
+        assert_same_list(ids[i, :k], d2[i, :k], rid, rd2, f"{name} agent {i}")
+
+
+@pytest.mark.parametrize("world", ["toric", "infinite"])
+def test_neighbour_lists_match_oracle_on_random_states(world, tmp_path):
+    rng = np.random.default_rng(7)
+    if world == "toric":
+        sc = S.socialforces_toric(n=4000, density=0.625)
+    else:
+        sc = S.karamouzas_corridor(n=3000, width=30.0)
+    path = sc.write(str(tmp_path / "s.xml"))
+    sim = Simulation(path)
+    port = PortSim(path, threads=THREADS)
+    for trial in range(3):
+        pos = sim.positions() + rng.normal(0, 0.5, (sim.n, 2)).astype(np.float32)
+        if world == "toric":
+            h = sc.width / 2
+            pos = np.clip(pos, -h, h).astype(np.float32)
+        sim.set_state(pos=pos)
+        port.set_state(pos=pos)
+        ids, d2, cnt = sim.neighbours(cap=1024)
+        port.step(1)   # builds the port's lists from `pos`
+        pids = port.state()["ids"]
+        for i in range(sim.n):
+            rid, rd2, _ = port.neighbors(i)
+            k = int(cnt[i])
+            assert_same_list(ids[i, :k], d2[i, :k], rid.astype(np.int32), rd2, f"trial {trial} agent {pids[i]}")
+
+
+def _compare_with_port(path, steps):
+    sim = Simulation(path)
+    port = PortSim(path, threads=THREADS)
+    worst = 0.0
+    for s in range(steps):
+        sim.step(1)
+        port.step(1)
+        worst = max(worst, float(np.abs(sim.positions() - port.state()["pos"]).max()))
+    return worst
+
+
+def test_full_size_socialforces_matches_oracle(tmp_path):
+    path = S.socialforces_toric().write(str(tmp_path / "sf100k.xml"))
+    worst = _compare_with_port(path, 3)
+    print(f"100k SocialForces toric: max deviation over 3 steps = {worst:.3g} m")
+    assert worst <= TOL
+
+
+def test_karamouzas_corridor_matches_oracle(tmp_path):
+    path = S.karamouzas_corridor(n=20000, width=100.0).write(str(tmp_path / "k20k.xml"))
+    worst = _compare_with_port(path, 2)
+    print(f"20k Karamouzas corridor: max deviation over 2 steps = {worst:.3g} m")
+    assert worst <= TOL
+
+
+def test_full_size_properties(tmp_path):
+    """100k agents: deterministic, finite, no neighbour-capacity overflow."""
+    path = S.socialforces_toric().write(str(tmp_path / "sf100k.xml"))
+    a, b = Simulation(path), Simulation(path)
+    a.step(20)
+    b.step(20)
+    pa, pb = a.positions(), b.positions()
+    assert np.array_equal(pa, pb)
+    assert np.isfinite(pa).all()
+    assert np.abs(pa).max() <= 200.0 + 1e-3   # toric wrap keeps agents in the box

@@ -1,0 +1,17 @@
+"""umans_gb300: GB300 engine for the per-step agent update of UMANS
+(WorldBase::DoStep).
+
+Python host mirror of the reference's interfaces:
+
+* ``UMANS``       the reference's Python class (src/Library/PyAPI.h:55-246):
+                  startSimulation / getSimulationTimeStep / doSimulationSteps /
+                  getAgentPositions / setAgentPositions / addAgent /
+                  removeAgent / setAgentGoal / cleanUp / getNumberOfAgents.
+* ``Simulation``  a handle to one simulation with numpy state access.
+
+Both call the CUDA engine through the C ABI (include/umans_gb300.h).
+"""
+from ._lib import AgentData  # noqa: F401
+from .api import UMANS, Simulation, UmansError  # noqa: F401
+
+__all__ = ["UMANS", "Simulation", "UmansError", "AgentData"]

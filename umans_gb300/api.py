@@ -1,0 +1,237 @@
+"""Python-facing classes over the C ABI."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import AgentData
+
+
+class UmansError(RuntimeError):
+    pass
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Simulation:
+    """One simulation on the GPU (the reference's CrowdSimulator + World).
+
+    ``Simulation(path)`` loads a UMANS scenario file with the reference's
+    loader semantics (CrowdSimulator::FromConfigFile).
+    """
+
+    def __init__(self, config_file: str, max_neighbours: int = 0, cells_per_range: float = 0.0,
+                 use_graph: bool = True):
+        lib = _lib.load()
+        h = C.c_void_p()
+        rc = lib.umans_create_ex(os.fsencode(config_file), int(max_neighbours), float(cells_per_range),
+                                 int(bool(use_graph)), C.byref(h))
+        if rc != 0:
+            raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+        self._lib = lib
+        self._h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise UmansError(self._lib.umans_last_error(self._h).decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.umans_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- stepping -------------------------------------------------------
+    def step(self, n: int = 1):
+        self._check(self._lib.umans_step(self._h, int(n)))
+
+    def step_async(self, n: int = 1):
+        self._check(self._lib.umans_step_async(self._h, int(n)))
+
+    def synchronize(self):
+        self._check(self._lib.umans_synchronize(self._h))
+
+    # --- properties -----------------------------------------------------
+    @property
+    def n(self) -> int:
+        v = C.c_int()
+        self._check(self._lib.umans_num_agents(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def time(self) -> float:
+        v = C.c_double()
+        self._check(self._lib.umans_time(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def dt(self) -> float:
+        v = C.c_float()
+        self._check(self._lib.umans_dt(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def end_time(self) -> float:
+        v = C.c_float()
+        self._check(self._lib.umans_end_time(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def max_neighbours(self) -> int:
+        v = C.c_int()
+        self._check(self._lib.umans_max_neighbours(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def stream(self) -> int:
+        v = C.c_void_p()
+        self._check(self._lib.umans_stream(self._h, C.byref(v)))
+        return v.value or 0
+
+    def device_state(self):
+        p, v = C.c_void_p(), C.c_void_p()
+        self._check(self._lib.umans_device_state(self._h, C.byref(p), C.byref(v)))
+        return p.value, v.value
+
+    def profile(self, enable: bool = True):
+        self._check(self._lib.umans_profile(self._h, int(bool(enable))))
+
+    def profile_totals(self) -> dict:
+        a, b = C.c_double(), C.c_double()
+        n, k = C.c_int(), C.c_int()
+        self._check(self._lib.umans_profile_totals(self._h, C.byref(a), C.byref(b), C.byref(n), C.byref(k)))
+        return dict(agent_kernel_ms=a.value, step_ms=b.value, steps=n.value, kernels_per_step=k.value)
+
+    # --- state ----------------------------------------------------------
+    def state(self) -> dict:
+        n = self.n
+        out = dict(ids=np.zeros(n, np.int32), pos=np.zeros((n, 2), np.float32),
+                   vel=np.zeros((n, 2), np.float32), viewdir=np.zeros((n, 2), np.float32))
+        self._check(self._lib.umans_get_state(self._h, _p(out["ids"]), _p(out["pos"]), _p(out["vel"]),
+                                              _p(out["viewdir"]), n))
+        pv = np.zeros((n, 2), np.float32)
+        g = np.zeros((n, 2), np.float32)
+        self._check(self._lib.umans_get_aux(self._h, _p(pv), _p(g), n))
+        out["prefvel"] = pv
+        out["goal"] = g
+        return out
+
+    def positions(self) -> np.ndarray:
+        n = self.n
+        pos = np.zeros((n, 2), np.float32)
+        self._check(self._lib.umans_get_state(self._h, None, _p(pos), None, None, n))
+        return pos
+
+    def set_state(self, pos=None, vel=None, viewdir=None):
+        a = [None if x is None else np.ascontiguousarray(x, np.float32) for x in (pos, vel, viewdir)]
+        for x in a:
+            if x is not None and x.size != 2 * self.n:
+                raise ValueError("state arrays must have shape (n, 2)")
+        self._check(self._lib.umans_set_state(self._h, *(_p(x) for x in a)))
+
+    def get_agents(self, out=None):
+        """GetAgentPositions into a ctypes AgentData array (reused if given)."""
+        n = self.n
+        if out is None or len(out) < n:
+            out = (AgentData * max(n, 1))()
+        cnt = C.c_int()
+        self._check(self._lib.umans_get_agents(self._h, out, len(out), C.byref(cnt)))
+        return out, cnt.value
+
+    def set_agents(self, agents):
+        arr = (AgentData * len(agents))(*agents)
+        self._check(self._lib.umans_set_agents(self._h, arr, len(agents)))
+
+    def add_agent(self, x, y, radius, pref_speed, max_speed, max_acceleration, policy_id, desired_id=-1) -> int:
+        out = C.c_int()
+        self._check(self._lib.umans_add_agent(self._h, x, y, radius, pref_speed, max_speed, max_acceleration,
+                                              int(policy_id), int(desired_id), C.byref(out)))
+        return out.value
+
+    def remove_agent(self, agent_id: int):
+        self._check(self._lib.umans_remove_agent(self._h, int(agent_id)))
+
+    def set_goal(self, agent_id: int, x: float, y: float):
+        self._check(self._lib.umans_set_goal(self._h, int(agent_id), float(x), float(y)))
+
+    def neighbours(self, cap: int = 64):
+        """(ids[n, cap], dist2[n, cap], counts[n]) of the lists the next step uses."""
+        n = self.n
+        ids = np.full((n, cap), -1, np.int32)
+        d2 = np.zeros((n, cap), np.float32)
+        cnt = np.zeros(n, np.int32)
+        self._check(self._lib.umans_neighbours(self._h, int(cap), _p(ids), _p(d2), _p(cnt)))
+        return ids, d2, cnt
+
+
+class UMANS:
+    """The reference's Python interface (src/Library/PyAPI.h:55-246) on the
+    reference-compatible global C functions."""
+
+    def __init__(self):
+        self._lib = _lib.load()
+
+    def startSimulation(self, configFileName: str, numberOfThreads: int = 1) -> bool:
+        return bool(self._lib.StartSimulation(os.fsencode(configFileName), int(numberOfThreads)))
+
+    def getSimulationTimeStep(self) -> float:
+        v = C.c_float(-1)
+        if not self._lib.GetSimulationTimeStep(C.byref(v)):
+            return -1.0
+        return v.value
+
+    def doSimulationSteps(self, nrSteps: int) -> bool:
+        return bool(self._lib.DoSimulationSteps(int(nrSteps)))
+
+    def getAgentPositions(self) -> list:
+        ptr = C.POINTER(AgentData)()
+        n = C.c_int()
+        if not self._lib.GetAgentPositions(C.byref(ptr), C.byref(n)):
+            return []
+        out = []
+        for i in range(n.value):
+            a = ptr[i]
+            out.append(AgentData(a.id, a.position_x, a.position_y, a.velocity_x, a.velocity_y,
+                                 a.viewingDirection_x, a.viewingDirection_y))
+        return out
+
+    def setAgentPositions(self, agentData) -> bool:
+        arr = (AgentData * len(agentData))(*agentData)
+        return bool(self._lib.SetAgentPositions(arr, len(agentData)))
+
+    def addAgent(self, x, y, radius, prefSpeed, maxSpeed, maxAcceleration, policyID, customID=-1) -> int:
+        out = C.c_int(-1)
+        ok = self._lib.AddAgent(x, y, radius, prefSpeed, maxSpeed, maxAcceleration, int(policyID),
+                                C.byref(out), int(customID))
+        return out.value if ok else -1
+
+    def removeAgent(self, id: int) -> bool:
+        return bool(self._lib.RemoveAgent(int(id)))
+
+    def setAgentGoal(self, id: int, x: float, y: float) -> bool:
+        return bool(self._lib.SetAgentGoal(int(id), float(x), float(y)))
+
+    def cleanUp(self) -> bool:
+        return bool(self._lib.CleanUp())
+
+    def getNumberOfAgents(self) -> int:
+        return len(self.getAgentPositions())
+
+    def getNumberOfObstacles(self) -> int:
+        return 0

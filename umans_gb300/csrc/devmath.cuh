@@ -1,0 +1,183 @@
+// Device restatement of the reference's 2-D float math.
+//
+// Vector2D (src/Engine/tools/vector2D.h) computes in float, one rounding per
+// operation, with `v / s` implemented as `(1/s) * v` (vector2D.h:132-135).
+// These helpers keep that operation order.  The translation units that
+// include this header are compiled with -fmad=false so that nvcc never fuses
+// a*b+c into an FMA: the reference's CPU build rounds each product.
+//
+// FP64 islands: the reference promotes to double in angle()/cosAngle()
+// (vector2D.h:172-195), rotateCounterClockwise (:166-170) and pow(x, 2).
+// Double throughput on GB300 is ~1/64 of float, so:
+//   * cosAngle = (float)(dot / (double)len): a single double division of two
+//     float operands rounded to float equals the float division (double
+//     rounding is innocuous for p_double >= 2 p_float + 2), so it is computed
+//     in float;
+//   * comparisons of angle() against a threshold use a float guard band and
+//     fall back to the exact double computation only within 1e-6 of it.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+namespace umans {
+
+#define UD __device__ __forceinline__
+
+constexpr float MAXF = FLT_MAX;
+constexpr double REF_PI = 3.1415926535897;   // vector2D.h:27
+
+UD float2 V(float x, float y) { return make_float2(x, y); }
+UD float2 vadd(float2 a, float2 b) { return V(a.x + b.x, a.y + b.y); }
+UD float2 vsub(float2 a, float2 b) { return V(a.x - b.x, a.y - b.y); }
+UD float2 vmul(float2 a, float s) { return V(a.x * s, a.y * s); }
+UD float2 vdiv(float2 a, float s) { float r = 1.0f / s; return V(a.x * r, a.y * r); }
+UD float2 vneg(float2 a) { return V(-a.x, -a.y); }
+UD float vdot(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+UD float vsq(float2 a) { return a.x * a.x + a.y * a.y; }
+UD float vmag(float2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+UD bool viszero(float2 a) { return a.x == 0 && a.y == 0; }
+UD float2 vnorm(float2 a)
+{
+	float m = vmag(a);
+	if (m > 0) { a.x = a.x / m; a.y = a.y / m; }
+	return a;
+}
+UD float2 vclamp(float2 v, float maxLength)   // clampVector: vector2D.h:241-247
+{
+	float m = vmag(v);
+	if (m <= maxLength) return v;
+	return vmul(vnorm(v), maxLength);
+}
+UD float fminr(float a, float b) { return (b < a) ? b : a; }   // std::min
+UD float fmaxr(float a, float b) { return (a < b) ? b : a; }   // std::max
+
+// rotateCounterClockwise with cosf/sinf already evaluated (a float pair):
+// the products are exact in double, the sum is rounded once in double and
+// then to float, exactly as vector2D.h:166-170.
+UD float2 vrot_cs(float2 v, float c, float s)
+{
+	const double C = (double)c, S = (double)s;
+	const double x = __dsub_rn(__dmul_rn(C, (double)v.x), __dmul_rn(S, (double)v.y));
+	const double y = __dadd_rn(__dmul_rn(S, (double)v.x), __dmul_rn(C, (double)v.y));
+	return V((float)x, (float)y);
+}
+
+// angle(): vector2D.h:172-186, computed exactly in double
+UD float vangle_exact(float2 a, float2 b)
+{
+	const float lf = vmag(a) * vmag(b);
+	const double lengths = (double)lf;
+	if (lengths == 0) return 0.0f;
+	const double frac = __ddiv_rn((double)vdot(a, b), lengths);
+	if (frac < -1 || frac > 1) return 0.0f;
+	return (float)acos(frac);
+}
+
+// cosAngle(): vector2D.h:188-195; float division == (float)(double division)
+UD float vcosangle(float2 a, float2 b)
+{
+	const float lf = vmag(a) * vmag(b);
+	if (lf == 0) return 0.0f;
+	return vdot(a, b) / lf;
+}
+
+// angle(a, b) > thr, with cos_thr = cos(thr) to within 1e-7.  angle() is
+// never negative and returns 0 for zero-length inputs or |frac| > 1.
+UD bool angle_greater(float2 a, float2 b, float thr, float cos_thr)
+{
+	if (thr < 0) return true;
+	const float lf = vmag(a) * vmag(b);
+	if (lf == 0) return false;
+	const float c = vdot(a, b) / lf;
+	if (c > cos_thr + 1e-6f) return false;                   // clearly smaller (or frac > 1)
+	if (c < cos_thr - 1e-6f && c > -0.9999f) return true;    // clearly larger
+	return vangle_exact(a, b) > thr;
+}
+
+// angle(a, b) < thr
+UD bool angle_less(float2 a, float2 b, float thr, float cos_thr)
+{
+	if (thr <= 0) return false;
+	const float lf = vmag(a) * vmag(b);
+	if (lf == 0) return true;
+	const float c = vdot(a, b) / lf;
+	if (c > cos_thr + 1e-6f) return true;
+	if (c < cos_thr - 1e-6f && c > -0.9999f) return false;
+	return vangle_exact(a, b) < thr;
+}
+
+UD bool vclockwise(float2 a, float2 b) { float c = a.x * b.y - a.y * b.x; return c < 0; }
+
+// getLineIntersection: vector2D.h:249-272 (double)
+UD bool line_intersection(float2 a, float2 b, float2 c, float2 d, float2* res)
+{
+	double a1 = b.y - a.y, b1 = a.x - b.x;
+	double c1 = __dadd_rn(__dmul_rn(a1, (double)a.x), __dmul_rn(b1, (double)a.y));
+	double a2 = d.y - c.y, b2 = c.x - d.x;
+	double c2 = __dadd_rn(__dmul_rn(a2, (double)c.x), __dmul_rn(b2, (double)c.y));
+	double det = __dsub_rn(__dmul_rn(a1, b2), __dmul_rn(a2, b1));
+	if (fabs(det) < 0.00001) return false;
+	res->x = (float)__ddiv_rn(__dsub_rn(__dmul_rn(b2, c1), __dmul_rn(b1, c2)), det);
+	res->y = (float)__ddiv_rn(__dsub_rn(__dmul_rn(a1, c2), __dmul_rn(a2, c1)), det);
+	return true;
+}
+
+// (float)((double)x * (double)x - (double)y * (double)y): pow(x,2) - pow(y,2)
+UD float sq_diff_d(float x, float y)
+{
+	return (float)__dsub_rn(__dmul_rn((double)x, (double)x), __dmul_rn((double)y, (double)y));
+}
+
+// ---------------------------------------------------------------------
+// shared cost helpers (src/Engine/core/costFunction.cpp:173-227, 354-380)
+// ---------------------------------------------------------------------
+UD int solve_quadratic(float a, float b, float c, float* x1, float* x2)
+{
+	const float D = b * b - 4 * a * c;
+	if (D < 0) return 0;
+	if (D == 0) { *x1 = -b / 2 * a; return 1; }   // sic: costFunction.cpp:180
+	const float m = -b / (2 * a);
+	const float s = sqrtf(D) / (2 * a);
+	*x1 = m + s;
+	*x2 = m - s;
+	return 2;
+}
+
+UD float ttc_pair(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2)
+{
+	const float2 P = vsub(p1, p2);
+	const float R = r1 + r2, RR = R * R;
+	if (vsq(P) <= RR) return 0;
+	const float2 Vd = vsub(v1, v2);
+	const float a = vdot(Vd, Vd), b = 2 * vdot(P, Vd), c = vdot(P, P) - RR;
+	float t1 = MAXF, t2 = MAXF;
+	solve_quadratic(a, b, c, &t1, &t2);
+	if (t1 < 0) t1 = MAXF;
+	if (t2 < 0) t2 = MAXF;
+	return fminr(t1, t2);
+}
+
+UD void ttca_dca(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2, float* ttca_o, float* dca_o)
+{
+	const float2 dpc = vsub(p2, p1), dvc = vsub(v2, v1);
+	const float dpMag = vmag(dpc);
+	const float2 dp = vmul(vdiv(dpc, dpMag), dpMag - r1 - r2);
+	const float2 nrm = V(-dpc.y, dpc.x);
+	const float2 dv = vadd(dvc, vmul(nrm, vdot(nrm, dvc)));
+	float ttca = (vsq(dv) == 0 ? 0 : -vdot(dp, dv) / vsq(dv));
+	if (ttca < 0) ttca = 0;
+	float dca = vmag(vadd(dp, vmul(dv, ttca)));
+	if (dca < 0) dca = 0;
+	*ttca_o = ttca;
+	*dca_o = dca;
+}
+
+// RotateGradientToEuclideanCoordinates: costFunction.cpp:30-34
+UD float2 rotate_gradient(float gth, float gs, float2 dir, float speed)
+{
+	const float2 w = vadd(vmul(V(sinf(gth), 1 - cosf(gth)), speed), V(0, gs));
+	return V(dir.y * w.x + dir.x * w.y, -dir.x * w.x + dir.y * w.y);
+}
+
+#undef UD
+}  // namespace umans

@@ -1,0 +1,1669 @@
+// GB300 step engine: the per-step agent update of WorldBase::DoStep
+// (src/Engine/core/worldBase.cpp:79-128) as a short kernel sequence.
+//
+//   k_bbox / k_grid     bounding box (infinite world) -> grid parameters
+//   k_count             cell of every agent, per-cell histogram
+//                       (warp-aggregated atomics via __match_any_sync)
+//   k_scan_*            exclusive prefix sum of the histogram (3 passes)
+//   k_scatter           counting-sort scatter into cell-sorted copies of
+//                       position / velocity / preferred velocity / radius,
+//                       computing the preferred velocity (agent.cpp:52-59)
+//   k_agent             one warp per agent, agents in cell order:
+//                         neighbour query (kd-tree radius search semantics,
+//                         AgentKDTree.cpp:35-59, worldToric.cpp:32-79),
+//                         contact forces (policy.cpp:107-141),
+//                         velocity optimisation (policy.cpp:43-105),
+//                         integration + toric wrap (agent.cpp:71-93,
+//                         worldToric.cpp:81-108).
+//
+// Phases 2-6 of DoStep only read state that earlier phases finished and only
+// write per-agent state, so they fuse into k_agent: every neighbour read goes
+// to the cell-sorted copies made by k_scatter, every write to the agent's own
+// slot.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "costs.cuh"
+
+namespace umans {
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err_ = std::string(#x) + ": " + cudaGetErrorString(e_); return false; } } while (0)
+
+static const uint32_t LCG_M = 2147483647u;   // minstd_rand0 modulus
+static const uint32_t LCG_A = 16807u;
+
+struct DevState {
+	int n, world;
+	float width, height, dt;
+	float2 *pos, *vel, *goal, *view, *vwf, *pref;
+	float4* prm;
+	int *pol, *id;
+	uint32_t* rng;
+	float2 *sP, *sV;
+	float4* sB;
+	int *sSlot, *sId;
+	int *cell, *cnt, *start, *fill, *blocksum;
+	GridParams* grid;
+	unsigned* bbox;
+	int* status;
+	const PolicyDesc* pols;
+	const SampleEntry* table;
+	const uint32_t* lcgpow;
+	float4* scratch;
+	int maxnb, total_warps, max_cells;
+	float max_range, cells_per_range;
+	int* slot_of_id;      // id -> list slot, -1 when absent
+	int id_bound;         // size of slot_of_id
+	AgentRecord* io;      // staging for AgentData exchange
+	// neighbour-list dump (tests)
+	int *dump_ids, *dump_cnt;
+	float* dump_d2;
+	int dump_cap;
+};
+
+// ------------------------------------------------------------------------
+// grid build
+// ------------------------------------------------------------------------
+__device__ __forceinline__ unsigned f2o(float f)
+{
+	unsigned u = __float_as_uint(f);
+	return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(unsigned u)
+{
+	return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void k_bbox(DevState S)
+{
+	float mnx = FLT_MAX, mny = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+		const float2 p = S.pos[i];
+		mnx = fminf(mnx, p.x); mxx = fmaxf(mxx, p.x);
+		mny = fminf(mny, p.y); mxy = fmaxf(mxy, p.y);
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+		mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+		mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+		mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicMin(&S.bbox[0], f2o(mnx)); atomicMin(&S.bbox[1], f2o(mny));
+		atomicMax(&S.bbox[2], f2o(mxx)); atomicMax(&S.bbox[3], f2o(mxy));
+	}
+}
+
+__global__ void k_grid(DevState S)
+{
+	float x0, y0, ex, ey;
+	if (S.world == W_TORIC) {
+		x0 = -0.5f * S.width; y0 = -0.5f * S.height; ex = S.width; ey = S.height;
+	} else {
+		x0 = o2f(S.bbox[0]); y0 = o2f(S.bbox[1]);
+		ex = o2f(S.bbox[2]) - x0; ey = o2f(S.bbox[3]) - y0;
+		if (S.n == 0) { x0 = y0 = 0; ex = ey = 1; }
+	}
+	S.bbox[0] = S.bbox[1] = f2o(FLT_MAX);
+	S.bbox[2] = S.bbox[3] = f2o(-FLT_MAX);
+	if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
+		atomicOr(S.status, ST_GRID_OVERFLOW);
+		x0 = y0 = 0; ex = ey = 1;
+	}
+	float cs = S.max_range / S.cells_per_range;
+	if (!(cs >= 1e-3f)) cs = 1e-3f;
+	while (((double)ex / cs + 1.0) * ((double)ey / cs + 1.0) > (double)S.max_cells) cs *= 2.0f;
+	GridParams g;
+	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
+	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
+	g.ncells = g.nx * g.ny; g.pad = 0;
+	*S.grid = g;
+}
+
+__device__ __forceinline__ int cell_coord(float v, float v0, float inv, int nmax)
+{
+	const float f = (v - v0) * inv;
+	int c = (f >= 0.0f) ? (int)fminf(f, 2.0e9f) : 0;   // NaN -> 0
+	return c >= nmax ? nmax - 1 : c;
+}
+
+__global__ void k_count(DevState S)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= S.n) return;
+	const GridParams g = *S.grid;
+	const float2 p = S.pos[i];
+	const int c = cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
+	S.cell[i] = c;
+	const unsigned peers = __match_any_sync(__activemask(), c);
+	if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.cnt[c], __popc(peers));
+}
+
+// exclusive scan of cnt[0..ncells) in 3 passes; 1024 cells per block
+constexpr int SCAN_BLOCK = 256, SCAN_PER_BLOCK = 1024;
+
+__global__ void k_scan_reduce(DevState S)
+{
+	const int nc = S.grid->ncells;
+	const int base = blockIdx.x * SCAN_PER_BLOCK;
+	if (base >= nc) return;
+	int s = 0;
+	for (int k = threadIdx.x; k < SCAN_PER_BLOCK; k += SCAN_BLOCK) {
+		const int c = base + k;
+		if (c < nc) s += S.cnt[c];
+	}
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	__shared__ int ws[SCAN_BLOCK / 32];
+	if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		int t = 0;
+		for (int w = 0; w < SCAN_BLOCK / 32; ++w) t += ws[w];
+		S.blocksum[blockIdx.x] = t;
+	}
+}
+
+__global__ void k_scan_top(DevState S)
+{
+	// one block of 1024 threads; exclusive scan of the block sums in place
+	const int nb = (S.grid->ncells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+	const int per = (nb + 1023) / 1024;
+	const int b0 = threadIdx.x * per;
+	int local = 0;
+	for (int k = 0; k < per; ++k) if (b0 + k < nb) local += S.blocksum[b0 + k];
+	__shared__ int tot[1024];
+	tot[threadIdx.x] = local;
+	__syncthreads();
+	for (int o = 1; o < 1024; o <<= 1) {
+		int v = threadIdx.x >= o ? tot[threadIdx.x - o] : 0;
+		__syncthreads();
+		tot[threadIdx.x] += v;
+		__syncthreads();
+	}
+	int run = tot[threadIdx.x] - local;
+	for (int k = 0; k < per; ++k) {
+		if (b0 + k < nb) {
+			const int v = S.blocksum[b0 + k];
+			S.blocksum[b0 + k] = run;
+			run += v;
+		}
+	}
+}
+
+__global__ void k_scan_down(DevState S)
+{
+	const int nc = S.grid->ncells;
+	const int base = blockIdx.x * SCAN_PER_BLOCK;
+	if (base >= nc) return;
+	// each thread owns 4 consecutive cells
+	const int c0 = base + threadIdx.x * 4;
+	int v[4], s = 0;
+	for (int k = 0; k < 4; ++k) { v[k] = (c0 + k < nc) ? S.cnt[c0 + k] : 0; s += v[k]; }
+	__shared__ int ts[SCAN_BLOCK];
+	ts[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = 1; o < SCAN_BLOCK; o <<= 1) {
+		int x = threadIdx.x >= o ? ts[threadIdx.x - o] : 0;
+		__syncthreads();
+		ts[threadIdx.x] += x;
+		__syncthreads();
+	}
+	int run = S.blocksum[blockIdx.x] + ts[threadIdx.x] - s;
+	for (int k = 0; k < 4; ++k) {
+		const int c = c0 + k;
+		if (c < nc) {
+			S.start[c] = run;
+			S.fill[c] = run;
+			S.cnt[c] = 0;   // histogram is all-zero between steps
+			run += v[k];
+		}
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) S.start[nc] = S.n;
+}
+
+__global__ void k_scatter(DevState S)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= S.n) return;
+	const int c = S.cell[i];
+	const unsigned act = __activemask();
+	const unsigned peers = __match_any_sync(act, c);
+	const int lane = threadIdx.x & 31;
+	const int leader = __ffs(peers) - 1;
+	int base = 0;
+	if (lane == leader) base = atomicAdd(&S.fill[c], __popc(peers));
+	base = __shfl_sync(peers, base, leader);
+	const int t = base + __popc(peers & ((1u << lane) - 1u));
+	const float2 p = S.pos[i];
+	const float2 g = S.goal[i];
+	const float4 prm = S.prm[i];
+	// Agent::ComputePreferredVelocity / hasReachedGoal: agent.cpp:52-59, 99-102
+	const float2 d = vsub(g, p);
+	float2 pv;
+	if (vsq(d) <= prm.x * prm.x) pv = V(0, 0);
+	else pv = vmul(vnorm(d), prm.y);
+	S.pref[i] = pv;
+	S.sP[t] = p;
+	S.sV[t] = S.vel[i];
+	S.sB[t] = make_float4(pv.x, pv.y, prm.x, 0.0f);
+	S.sSlot[t] = i;
+	S.sId[t] = S.id[i];
+}
+
+// ------------------------------------------------------------------------
+// neighbour query (warp-cooperative)
+// ------------------------------------------------------------------------
+struct WarpLists {
+	uint32_t* ref;
+	float* key;
+	int* nid;
+};
+
+__device__ __forceinline__ bool nb_less(const WarpLists& L, int a, int b)
+{
+	const float ka = L.key[a], kb = L.key[b];
+	return ka < kb || (ka == kb && L.nid[a] < L.nid[b]);
+}
+__device__ __forceinline__ void nb_cmpswap(const WarpLists& L, int lo, int hi)
+{
+	if (nb_less(L, hi, lo)) {
+		float k = L.key[lo]; L.key[lo] = L.key[hi]; L.key[hi] = k;
+		int d = L.nid[lo]; L.nid[lo] = L.nid[hi]; L.nid[hi] = d;
+		uint32_t r = L.ref[lo]; L.ref[lo] = L.ref[hi]; L.ref[hi] = r;
+	}
+}
+
+// ascending bitonic sort of [s, s+len) by (key, id); the network compares
+// only i < j pairs with the min going to i, so the missing elements of the
+// power-of-two padding behave as +infinity and are simply skipped.
+__device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
+{
+	if (len <= 1) return;
+	int P = 1;
+	while (P < len) P <<= 1;
+	for (int size = 2; size <= P; size <<= 1) {
+		const int half = size >> 1;
+		for (int k = lane; k < (P >> 1); k += 32) {
+			const int blk = k / half, pos = k % half;
+			const int lo = blk * size + pos, hi = blk * size + size - 1 - pos;
+			if (hi < len) nb_cmpswap(L, s + lo, s + hi);
+		}
+		__syncwarp();
+		for (int j = half >> 1; j > 0; j >>= 1) {
+			for (int k = lane; k < (P >> 1); k += 32) {
+				const int lo = (k / j) * 2 * j + (k % j), hi = lo + j;
+				if (hi < len) nb_cmpswap(L, s + lo, s + hi);
+			}
+			__syncwarp();
+		}
+	}
+}
+
+__device__ __forceinline__ double exact_key(float2 q, float2 c)
+{
+	// nanoflann L2_Simple_Adaptor<double>::evalMetric (nanoflann.hpp:423-446)
+	const double d0 = __dsub_rn((double)q.x, (double)c.x);
+	const double d1 = __dsub_rn((double)q.y, (double)c.y);
+	return __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
+}
+
+// Float keys order the list except within runs of near-equal keys, whose
+// order is settled with the reference's double distance (then id).
+__device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane)
+{
+	bool close = false;
+	for (int k = s + lane; k + 1 < e; k += 32) {
+		const float a = L.key[k], b = L.key[k + 1];
+		if (b - a <= 1e-6f * b) close = true;
+	}
+	if (!__any_sync(0xffffffffu, close)) return;
+	if (lane == 0) {
+		int k = s;
+		while (k + 1 < e) {
+			const float a = L.key[k], b = L.key[k + 1];
+			if (!(b - a <= 1e-6f * b)) { ++k; continue; }
+			int r0 = k;
+			while (k + 1 < e && L.key[k + 1] - L.key[k] <= 1e-6f * L.key[k + 1]) ++k;
+			const int r1 = k;   // inclusive
+			for (int x = r0 + 1; x <= r1; ++x) {
+				const uint32_t rx = L.ref[x];
+				const int ix = L.nid[x];
+				const float kx = L.key[x];
+				const double dx = exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
+				int y = x - 1;
+				while (y >= r0) {
+					const double dy = exact_key(q, S.sP[L.ref[y] & 0x0FFFFFFFu]);
+					if (dy > dx || (dy == dx && L.nid[y] > ix)) {
+						L.ref[y + 1] = L.ref[y]; L.nid[y + 1] = L.nid[y]; L.key[y + 1] = L.key[y];
+						--y;
+					} else break;
+				}
+				L.ref[y + 1] = rx; L.nid[y + 1] = ix; L.key[y + 1] = kx;
+			}
+			++k;
+		}
+	}
+	__syncwarp();
+}
+
+// Gathers the neighbour list of the agent at cell-sorted index t.  Returns
+// the list length (clamped to maxnb; *overflow set when clamped).  Entries
+// are grouped by displacement in the reference's order (worldToric.cpp:61-79)
+// and each group is sorted by the reference's double distance, ties by id.
+// On return key[] holds PhantomAgent::distSqr (worldBase.h:73-77).
+__device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L, int t, float2 p, float r,
+                      int lane, bool* overflow)
+{
+	int K = 0;
+	const int maxnb = S.maxnb;
+	if (!(r > 0)) return 0;   // dist < r*r never holds for r = 0
+	const float r2 = r * r;
+	const double r2d = (double)r2;
+	const float r2lo = r2 * 0.999999f, r2hi = r2 * 1.000001f;
+	const float W = S.width, H = S.height;
+	const unsigned lt = (1u << lane) - 1u;
+	for (int g = 0; g < 5; ++g) {
+		float2 disp = V(0, 0);
+		if (g > 0) {
+			if (S.world != W_TORIC) break;
+			bool active;
+			if (g == 1) { active = (double)(p.x - r) < -0.5 * (double)W; disp = V(W, 0); }
+			else if (g == 2) { active = (double)(p.x + r) > 0.5 * (double)W; disp = V(-W, 0); }
+			else if (g == 3) { active = (double)(p.y - r) < -0.5 * (double)H; disp = V(0, H); }
+			else { active = (double)(p.y + r) > 0.5 * (double)H; disp = V(0, -H); }
+			if (!active) continue;
+		}
+		const float2 q = vadd(p, disp);
+		const int gs = K;
+		const int cx0 = cell_coord((q.x - r - G.x0) * G.inv_cs - 0.01f, 0.0f, 1.0f, G.nx);
+		const int cx1 = cell_coord((q.x + r - G.x0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.nx);
+		const int cy0 = cell_coord((q.y - r - G.y0) * G.inv_cs - 0.01f, 0.0f, 1.0f, G.ny);
+		const int cy1 = cell_coord((q.y + r - G.y0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.ny);
+		for (int cy = cy0; cy <= cy1; ++cy) {
+			const int s0 = S.start[cy * G.nx + cx0];
+			const int e0 = S.start[cy * G.nx + cx1 + 1];
+			for (int base = s0; base < e0; base += 32) {
+				const int tt = base + lane;
+				bool ok = false;
+				float d2f = 0;
+				if (tt < e0 && tt != t) {
+					const float2 c = S.sP[tt];
+					const float dx = q.x - c.x, dy = q.y - c.y;
+					d2f = dx * dx + dy * dy;
+					if (d2f < r2lo) ok = true;
+					else if (d2f <= r2hi) ok = exact_key(q, c) < r2d;
+				}
+				const unsigned m = __ballot_sync(0xffffffffu, ok);
+				if (ok) {
+					const int idx = K + __popc(m & lt);
+					if (idx < maxnb) {
+						L.ref[idx] = ((uint32_t)g << 28) | (uint32_t)tt;
+						L.key[idx] = d2f;
+						L.nid[idx] = S.sId[tt];
+					}
+				}
+				K += __popc(m);
+			}
+		}
+		if (K > maxnb) { *overflow = true; K = maxnb; }
+		__syncwarp();
+		warp_sort(L, gs, K - gs, lane);
+		fix_near_ties(S, L, gs, K, q, lane);
+	}
+	// PhantomAgent position offset = -displacement; distSqr in float
+	const float2 off[5] = { V(0, 0), V(-W, -0.0f), V(W, -0.0f), V(-0.0f, -H), V(-0.0f, H) };
+	for (int k = lane; k < K; k += 32) {
+		const uint32_t rr = L.ref[k];
+		const float2 ph = vadd(S.sP[rr & 0x0FFFFFFFu], off[rr >> 28]);
+		L.key[k] = vsq(vsub(p, ph));
+	}
+	__syncwarp();
+	return K;
+}
+
+// ------------------------------------------------------------------------
+// warp helpers
+// ------------------------------------------------------------------------
+// Adds f (this lane's term, used where `take` is set) to acc in lane order
+// of the ballot, i.e. neighbour order.  All lanes end with the same acc.
+__device__ __forceinline__ float2 ordered_accumulate(float2 acc, float2 f, bool take)
+{
+	unsigned m = __ballot_sync(0xffffffffu, take);
+	while (m) {
+		const int src = __ffs(m) - 1;
+		const float fx = __shfl_sync(0xffffffffu, f.x, src);
+		const float fy = __shfl_sync(0xffffffffu, f.y, src);
+		acc.x += fx;
+		acc.y += fy;
+		m &= m - 1;
+	}
+	return acc;
+}
+
+// ObjectInteractionForces::ComputeForce: ObjectInteractionForces.cpp:26-48
+// (agents only; obstacles add (0,0)); GoalReachingForce.cpp:26-29
+__device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane)
+{
+	if (c.kind == K_GOALREACHING) return vdiv(vsub(A.pref, A.vel), fmaxr(A.relax, A.dt));
+	const float rs = c.range * c.range;
+	float2 F = V(0, 0);
+	for (int base = 0; base < N.K; base += 32) {
+		const int k = base + lane;
+		const bool in = k < N.K && N.d2[k] <= rs;
+		float2 f = V(0, 0);
+		if (in) {
+			const float2 np = nb_pos(N, k), nv = nb_vel(N, k);
+			if (c.kind == K_SOCIALFORCES) f = sf_force(A, c, np, nv, nb_pref(N, k), nb_radius(N, k));
+			else f = pl_force(A, c, np, nv, nb_radius(N, k));
+		}
+		F = ordered_accumulate(F, f, in);
+	}
+	return vadd(F, V(0, 0));
+}
+
+// ForceBasedFunction::ComputeTargetVelocity: ForceBasedFunction.cpp:48-52
+__device__ __forceinline__ float2 target_velocity(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane)
+{
+	return vadd(A.vel, vmul(vdiv(compute_force(A, N, c, lane), c.p[5]), A.dt));
+}
+
+__device__ __forceinline__ bool is_force_based(int kind)
+{
+	return kind == K_SOCIALFORCES || kind == K_POWERLAW || kind == K_GOALREACHING;
+}
+
+// ------------------------------------------------------------------------
+// ORCA (ORCASolver.cpp:61-326, CostFunctions/ORCA.cpp:26-95)
+// lines are float4 (point.x, point.y, direction.x, direction.y)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float det2(float2 a, float2 b) { return a.x * b.y - a.y * b.x; }
+__device__ __forceinline__ float2 lp_point(float4 l) { return V(l.x, l.y); }
+__device__ __forceinline__ float2 lp_dir(float4 l) { return V(l.z, l.w); }
+
+__device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res)
+{
+	const float4 ln = L[lineNo];
+	const float2 P = lp_point(ln), D = lp_dir(ln);
+	const float dp = vdot(P, D);
+	const float disc = dp * dp + radius * radius - vsq(P);
+	if (disc < 0.0f) return false;
+	const float sd = sqrtf(disc);
+	float tl = -dp - sd, tr = -dp + sd;
+	for (int i = 0; i < lineNo; ++i) {
+		const float4 li = L[i];
+		const float den = det2(D, lp_dir(li));
+		const float num = det2(lp_dir(li), vsub(P, lp_point(li)));
+		if (fabsf(den) <= 0.00001f) {
+			if (num < 0.0f) return false;
+			continue;
+		}
+		const float t = num / den;
+		if (den >= 0.0f) tr = fminr(tr, t);
+		else tl = fmaxr(tl, t);
+		if (tl > tr) return false;
+	}
+	if (dirOpt) {
+		if (vdot(opt, D) > 0.0f) *res = vadd(P, vmul(D, tr));
+		else *res = vadd(P, vmul(D, tl));
+	} else {
+		const float t = vdot(D, vsub(opt, P));
+		if (t < tl) *res = vadd(P, vmul(D, tl));
+		else if (t > tr) *res = vadd(P, vmul(D, tr));
+		else *res = vadd(P, vmul(D, t));
+	}
+	return true;
+}
+
+__device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res)
+{
+	if (dirOpt) *res = vmul(opt, radius);
+	else if (vsq(opt) > radius * radius) *res = vmul(vnorm(opt), radius);
+	else *res = opt;
+	for (int i = 0; i < n; ++i) {
+		const float4 li = L[i];
+		if (det2(lp_dir(li), vsub(lp_point(li), *res)) > 0.0f) {
+			const float2 tmp = *res;
+			if (!lp1(L, i, radius, opt, dirOpt, res)) { *res = tmp; return i; }
+		}
+	}
+	return n;
+}
+
+__device__ void lp3(const float4* L, int n, int begin, float radius, float2* res, float4* proj, int lane)
+{
+	float distance = 0.0f;
+	for (int i = begin; i < n; ++i) {
+		const float4 li = L[i];
+		const float2 Pi = lp_point(li), Di = lp_dir(li);
+		if (det2(Di, vsub(Pi, *res)) > distance) {
+			// projected lines, built lane-parallel and compacted in order
+			int np = 0;
+			for (int base = 0; base < i; base += 32) {
+				const int j = base + lane;
+				bool keep = false;
+				float4 out = make_float4(0, 0, 0, 0);
+				if (j < i) {
+					const float4 lj = L[j];
+					const float2 Pj = lp_point(lj), Dj = lp_dir(lj);
+					const float determinant = det2(Di, Dj);
+					float2 pt;
+					keep = true;
+					if (fabsf(determinant) <= 0.00001f) {
+						if (vdot(Di, Dj) > 0.0f) keep = false;
+						else pt = vmul(vadd(Pi, Pj), 0.5f);
+					} else {
+						pt = vadd(Pi, vmul(Di, det2(Dj, vsub(Pi, Pj)) / determinant));
+					}
+					if (keep) {
+						const float2 d = vnorm(vsub(Dj, Di));
+						out = make_float4(pt.x, pt.y, d.x, d.y);
+					}
+				}
+				const unsigned m = __ballot_sync(0xffffffffu, keep);
+				if (keep) proj[np + __popc(m & ((1u << lane) - 1u))] = out;
+				np += __popc(m);
+			}
+			__syncwarp();
+			const float2 tmp = *res;
+			if (lp2(proj, np, radius, V(-Di.y, Di.x), true, res) < np) *res = tmp;
+			distance = det2(Di, vsub(Pi, *res));
+			__syncwarp();
+		}
+	}
+}
+
+// Solver::createAgentOrcaLines + solveOrcaProgram: ORCASolver.cpp:61-171
+__device__ float2 orca_solve(const AgentCtx& A, const NbView& N, const CostDesc& c, float4* lines, float4* proj,
+                             int* nlines_out, int lane)
+{
+	const float tH = c.p[0];
+	const float maxDistSq = c.range * c.range;
+	int nl = 0;
+	for (int base = 0; base < N.K; base += 32) {
+		const int k = base + lane;
+		const bool in = k < N.K && N.d2[k] <= maxDistSq;
+		float4 out = make_float4(0, 0, 0, 0);
+		if (in) {
+			const float2 relPos = vsub(nb_pos(N, k), A.pos);
+			const float2 relVel = vsub(A.vel, nb_vel(N, k));
+			const float distSq = vsq(relPos);
+			const float cR = A.radius + nb_radius(N, k);
+			const float cRSq = cR * cR;
+			float2 dir, u;
+			if (distSq > cRSq) {
+				const float2 w = vsub(relVel, vdiv(relPos, tH));
+				const float wLenSq = vsq(w);
+				const float dp1 = vdot(w, relPos);
+				if (dp1 < 0.0f && dp1 * dp1 > cRSq * wLenSq) {
+					const float wLen = sqrtf(wLenSq);
+					const float2 unitW = vdiv(w, wLen);
+					dir = V(unitW.y, -unitW.x);
+					u = vmul(unitW, cR / tH - wLen);
+				} else {
+					const float leg = sqrtf(distSq - cRSq);
+					if (det2(relPos, w) > 0.0f)
+						dir = vdiv(V(relPos.x * leg - relPos.y * cR, relPos.x * cR + relPos.y * leg), distSq);
+					else
+						dir = vdiv(vmul(V(relPos.x * leg + relPos.y * cR, -relPos.x * cR + relPos.y * leg), -1), distSq);
+					const float dp2 = vdot(relVel, dir);
+					u = vsub(vmul(dir, dp2), relVel);
+				}
+			} else {
+				const float2 w = vsub(relVel, vdiv(relPos, A.dt));
+				const float wLen = vsq(w);   // sic: ORCASolver.cpp:161
+				const float2 unitW = vdiv(w, wLen);
+				dir = V(unitW.y, -unitW.x);
+				u = vmul(unitW, cR / A.dt - wLen);
+			}
+			const float2 pt = vadd(A.vel, vmul(u, 0.5f));
+			out = make_float4(pt.x, pt.y, dir.x, dir.y);
+		}
+		const unsigned m = __ballot_sync(0xffffffffu, in);
+		if (in) lines[nl + __popc(m & ((1u << lane) - 1u))] = out;
+		nl += __popc(m);
+	}
+	__syncwarp();
+	float2 res;
+	const int fail = lp2(lines, nl, A.maxspeed, A.pref, false, &res);
+	if (fail < nl) lp3(lines, nl, fail, A.maxspeed, &res, proj, lane);
+	*nlines_out = nl;
+	return res;
+}
+
+// ------------------------------------------------------------------------
+// gradients (uniform across the warp)
+// ------------------------------------------------------------------------
+// TtcaDca::GetGradient: TtcaDca.cpp:131-262
+__device__ float2 grad_ttcadca(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v)
+{
+	const float sA = c.p[0], sS = c.p[1], sT = c.p[2], sD = c.p[3];
+	const float viewHalf = (float)(REF_PI / 2.0);
+	const float eps = 0.001f;
+	const float rs = c.range * c.range;
+	float GradTh = 0, GradS = 0, total = 0;
+	for (int k = 0; k < N.K; ++k) {
+		if (N.d2[k] > rs) continue;
+		const float2 np = nb_pos(N, k);
+		const float nr = nb_radius(N, k);
+		const float2 dpc = vsub(np, A.pos), dvc = vsub(nb_vel(N, k), v);
+		if (angle_greater(dpc, A.vel, viewHalf, -4.3711388e-08f)) continue;
+		const float dpMag = vmag(dpc);
+		const float2 dp = vmul(vdiv(dpc, dpMag), dpMag - A.radius - nr);
+		const float2 nrm = V(-dpc.y, dpc.x);
+		const float2 dv = vadd(dvc, vmul(nrm, vdot(nrm, dvc)));
+		const float dvSq = vsq(dv);
+		float ttca = (dvSq == 0 ? 0 : -vdot(dp, dv) / dvSq);
+		if (ttca < 0) ttca = 0;
+		const float2 vdca = vadd(dp, vmul(dv, ttca));
+		float dca = vmag(vdca);
+		if (dca < 0) dca = 0;
+		if (dvSq <= eps) continue;
+		const float2 VelRot = V(dv.y, -dv.x);
+		const float VelMag = sqrtf(dvSq);
+		const float2 VelNorm = vdiv(dv, VelMag);
+		float gTA = 0, gTS = 0;
+		if (fabsf(ttca) > eps) {
+			const float2 rel = vadd(dp, vmul(dv, 2 * ttca));
+			gTA = -vdot(rel, VelRot) / dvSq;
+			gTS = vdot(rel, VelNorm) / dvSq;
+		}
+		float gDA = 0, gDS = 0;
+		if (fabsf(dca) > eps) {
+			gDA = vdot(vdca, vadd(vmul(dv, gTA), vmul(VelRot, ttca))) / dca;
+			gDS = vdot(vdca, vsub(vmul(dv, gTS), vmul(VelNorm, ttca))) / dca;
+		}
+		const float cost = ttcadca_pair_cost(ttca, dca, sT, sD);
+		const float tf = ttca / (sT * sT), df = dca / (sD * sD);
+		const float gCS = -cost * (gTS * tf + gDS * df);
+		const float gCA = -cost * (gTA * tf + gDA * df);
+		const float scale = 1 / vsq(dp);
+		total += scale;
+		GradTh += gCA * scale;
+		GradS += gCS * scale;
+	}
+	if (total > 0) { GradTh /= total; GradS /= total; }
+	// getMovementCostGradient: TtcaDca.cpp:54-60 (counterClockwiseAngle)
+	float alpha = vangle_exact(v, A.pref);
+	if (vclockwise(v, A.pref)) alpha = -alpha;
+	const float ds = vmag(v) - A.prefspeed;
+	const double qa = (double)(alpha / sA), qs = (double)(ds / sS);
+	const double DCa = __dmul_rn((double)(alpha / (2 * sA * sA)), exp(-0.5 * __dmul_rn(qa, qa)));
+	const double DCs = __dmul_rn((double)(ds / (2 * sS * sS)), exp(-0.5 * __dmul_rn(qs, qs)));
+	GradTh += (float)DCa;
+	GradS += (float)DCs;
+	if ((double)vsq(v) < 0.01)
+		return rotate_gradient(GradTh, GradS, vnorm(A.pref), vmag(A.pref));
+	return rotate_gradient(GradTh, GradS, vnorm(v), vmag(v));
+}
+
+// FOEAvoidance::GetGradient: FOEAvoidance.cpp:94-143
+__device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v)
+{
+	if (viszero(v)) return V(0, 0);
+	const float2 Vn = vnorm(v);
+	const float rs = c.range * c.range;
+	const double LN10 = 2.302585092994045684;
+	float gt = 0, gv = 0;
+	for (int k = 0; k < N.K; ++k) {
+		if (N.d2[k] > rs) continue;
+		const float2 dv = vsub(nb_vel(N, k), v), dp = vsub(nb_pos(N, k), A.pos);
+		const float2 Vel = V(Vn.y * dv.x + -Vn.x * dv.y, Vn.x * dv.x + Vn.y * dv.y);
+		const float2 Pos = V(Vn.y * dp.x + -Vn.x * dp.y, Vn.x * dp.x + Vn.y * dp.y);
+		if (Pos.y < 0.1f || Vel.y >= -0.01f) continue;
+		const float xf = Vel.x / Vel.y, xg = Pos.x / Pos.y, dx = xg - xf;
+		const float ttc = -Pos.y / Vel.y;
+		const float sigma = (float)__ddiv_rn((double)((A.radius + nb_radius(N, k)) / Pos.y), LN10);
+		const float sg = (float)((0 < dx) - (dx < 0));
+		const float E = foe_importance(ttc) * expf(-fabsf(dx) / sigma);
+		gt += E * sg * (xf * xf - xg * xg - (vmag(v) / (-Vel.y))) / sigma;
+		gv += E * sg * (-xf / (-Vel.y)) / sigma;
+	}
+	if (gt < -0.1f) gt = -0.1f;
+	else if (gt > 0.1f) gt = 0.1f;
+	const float2 w = vadd(vmul(V(sinf(gt), 1 - cosf(gt)), vmag(v)), V(0, gv));
+	return V(-Vn.y * w.x + -Vn.x * w.y, -(-Vn.x) * w.x + -Vn.y * w.y);
+}
+
+// ------------------------------------------------------------------------
+// per-cost evaluation (sampling / finite differences)
+// ------------------------------------------------------------------------
+struct CostPrep {
+	float2 target[MAX_COSTS];    // force-based target velocity
+	float ttcp[MAX_COSTS];       // Karamouzas TTC at the preferred velocity
+	float maxdev[MAX_COSTS], cosdev[MAX_COSTS];
+	const float4* lines;         // ORCA lines
+	int nlines;
+	float2 orca_v;
+};
+
+__device__ float eval_cost(const AgentCtx& A, const NbView& N, const CostDesc& c, const CostPrep& P, int ci, float2 v)
+{
+	switch (c.kind) {
+	case K_SOCIALFORCES: case K_POWERLAW: case K_GOALREACHING:
+		return 0.5f * vsq(vsub(v, P.target[ci])) / A.dt;   // ForceBasedFunction.cpp:26-30
+	case K_KARAMOUZAS: return cost_karamouzas(A, N, c, P.ttcp[ci], P.maxdev[ci], P.cosdev[ci], v);
+	case K_MOUSSAID: return cost_moussaid(A, N, c, v);
+	case K_VANTOLL: return cost_vantoll(A, N, c, v);
+	case K_PLEDESTRIANS: return cost_pledestrians(A, N, c, v);
+	case K_RVO: return cost_rvo(A, N, c, v);
+	case K_ORCA: return cost_orca(A, P.lines, P.nlines, v);
+	case K_PARIS: return cost_paris(A, N, c, v);
+	case K_TTCADCA: return cost_ttcadca(A, N, c, v);
+	case K_FOE: return cost_foe(A, N, c, v);
+	}
+	return 0;
+}
+
+__device__ __forceinline__ uint32_t mulmod(uint32_t a, uint32_t b)
+{
+	return (uint32_t)(((uint64_t)a * b) % LCG_M);
+}
+// generate_canonical<float,24> on minstd_rand0 state x, then a + u*(b-a)
+__device__ __forceinline__ float rng_uniform(uint32_t x, float a, float b)
+{
+	const float sum = (float)(x - 1u);
+	float ret = sum / 2147483648.0f;
+	if (ret >= 1.0f) ret = 0.99999994f;   // nextafter(1, 0)
+	return ret * (b - a) + a;
+}
+
+// CostFunction::ApproximateGlobalMinimumBySampling: costFunction.cpp:66-164.
+// Samples are spread over lanes; the argmin keeps the first strict minimum.
+__device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView& N, const PolicyDesc& pol,
+                             const CostPrep& P, uint32_t rng0, int lane)
+{
+	float2 base = V(0, 0);
+	if (pol.table_base == 1) base = A.vel;
+	float radius;
+	if (pol.table_radius == 0) radius = A.prefspeed;
+	else if (pol.table_radius == 1) radius = A.maxspeed;
+	else radius = fminr(2.0f * A.maxspeed, A.maxacc * A.dt);
+	float2 dir = V(1, 0);
+	if (pol.table_dir == 1) dir = vnorm(A.vel);
+	else if (pol.table_dir == 2) dir = vnorm(A.pref);
+	const float dL = radius / (float)pol.len_divisor;
+	const int ncost = pol.single_cost ? 1 : pol.ncost;
+	float bestC = MAXF;
+	int bestI = 0x7fffffff;
+	for (int i = lane; i < pol.nsamples; i += 32) {
+		float2 v;
+		if (pol.table_random) {
+			const float ma = pol.max_angle;
+			const uint32_t x1 = mulmod(S.lcgpow[2 * i + 1], rng0);
+			const uint32_t x2 = mulmod(S.lcgpow[2 * i + 2], rng0);
+			const float ra = rng_uniform(x1, -ma, ma);
+			const float rl = rng_uniform(x2, 0, radius);
+			v = vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
+		} else {
+			const SampleEntry e = S.table[pol.table_offset + i];
+			v = vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
+		}
+		float tc = 0;
+		for (int ci = 0; ci < ncost; ++ci) {
+			const float coeff = pol.single_cost ? 1.0f : pol.cost[ci].coeff;
+			tc += coeff * eval_cost(A, N, pol.cost[ci], P, ci, v);
+		}
+		if (tc < bestC) { bestC = tc; bestI = i; }
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		const float oc = __shfl_xor_sync(0xffffffffu, bestC, o);
+		const int oi = __shfl_xor_sync(0xffffffffu, bestI, o);
+		if (oc < bestC || (oc == bestC && oi < bestI)) { bestC = oc; bestI = oi; }
+	}
+	if (bestI == 0x7fffffff) return V(0, 0);
+	// every lane rebuilds the winning candidate
+	const int i = bestI;
+	if (pol.table_random) {
+		const float ma = pol.max_angle;
+		const uint32_t x1 = mulmod(S.lcgpow[2 * i + 1], rng0);
+		const uint32_t x2 = mulmod(S.lcgpow[2 * i + 2], rng0);
+		const float ra = rng_uniform(x1, -ma, ma);
+		const float rl = rng_uniform(x2, 0, radius);
+		return vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
+	}
+	const SampleEntry e = S.table[pol.table_offset + i];
+	return vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
+}
+
+// ------------------------------------------------------------------------
+// the fused per-agent step
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
+{
+	extern __shared__ unsigned char smem[];
+	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
+	const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+	const int maxnb = S.maxnb;
+	uint32_t* base = reinterpret_cast<uint32_t*>(smem) + (size_t)wib * 3 * maxnb;
+	WarpLists L{ base, reinterpret_cast<float*>(base + maxnb), reinterpret_cast<int*>(base + 2 * maxnb) };
+	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
+	float4* proj = lines + maxnb;
+	const GridParams G = *S.grid;
+	bool overflow = false;
+
+	for (int t = gw; t < S.n; t += S.total_warps) {
+		const int slot = S.sSlot[t];
+		const float4 sb = S.sB[t];
+		const float4 prm = S.prm[slot];
+		const int pi = S.pol[slot];
+		const PolicyDesc& pol = S.pols[pi];
+		AgentCtx A;
+		A.pos = S.sP[t]; A.vel = S.sV[t]; A.pref = V(sb.x, sb.y); A.goal = S.goal[slot];
+		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
+		A.dt = S.dt; A.relax = pol.relax_time;
+
+		const int K = gather(S, G, L, t, A.pos, pol.range, lane, &overflow);
+		NbView N;
+		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB;
+		N.off[0] = V(0, 0); N.off[1] = V(-S.width, -0.0f); N.off[2] = V(S.width, -0.0f);
+		N.off[3] = V(-0.0f, -S.height); N.off[4] = V(-0.0f, S.height);
+
+		if (dump) {
+			const int cap = S.dump_cap;
+			for (int k = lane; k < K && k < cap; k += 32) {
+				S.dump_ids[(size_t)slot * cap + k] = L.nid[k];
+				S.dump_d2[(size_t)slot * cap + k] = L.key[k];
+			}
+			if (lane == 0) S.dump_cnt[slot] = K;
+			__syncwarp();
+			continue;
+		}
+
+		// phase 5: contact forces (policy.cpp:107-141), independent of phase 4
+		float2 contact = V(0, 0);
+		if (pol.contact_scale > 0) {
+			for (int b0 = 0; b0 < K; b0 += 32) {
+				const int k = b0 + lane;
+				bool take = false;
+				float2 f = V(0, 0);
+				if (k < K) {
+					const float2 diff = vsub(A.pos, nb_pos(N, k));
+					const float inter = A.radius + nb_radius(N, k) - vmag(diff);
+					if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
+				}
+				contact = ordered_accumulate(contact, f, take);
+			}
+		}
+
+		// phase 4: Policy::ComputeNewVelocity (policy.cpp:43-76)
+		float2 nv = V(0, 0);
+		uint32_t rng_next = 0;
+		bool rng_used = false;
+		if (!viszero(A.pref)) {
+			CostPrep P;
+			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
+			for (int ci = 0; ci < pol.ncost; ++ci) {
+				const CostDesc& c = pol.cost[ci];
+				if (is_force_based(c.kind)) P.target[ci] = target_velocity(A, N, c, lane);
+				else if (c.kind == K_KARAMOUZAS) {
+					// TTC at the preferred velocity: a min, so lanes split the neighbours
+					float m = MAXF;
+					const float md2 = c.range * c.range;
+					for (int k = lane; k < K; k += 32) {
+						if (N.d2[k] > md2) continue;
+						const float tt = ttc_pair(A.pos, A.pref, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+						if (tt == 0) continue;
+						if (tt < m) m = tt;
+					}
+					for (int o = 16; o > 0; o >>= 1) {
+						const float x = __shfl_xor_sync(0xffffffffu, m, o);
+						if (x < m) m = x;
+					}
+					P.ttcp[ci] = m;
+					P.maxdev[ci] = karamouzas_maxdev(m);
+					P.cosdev[ci] = cosf(P.maxdev[ci]);
+				} else if (c.kind == K_ORCA) {
+					P.orca_v = orca_solve(A, N, c, lines, proj, &P.nlines, lane);
+				}
+			}
+			float2 acc;
+			if (pol.method == M_GRADIENT) {
+				// Policy::getAccelerationFromGradient: policy.cpp:78-89
+				float2 T = V(0, 0);
+				for (int ci = 0; ci < pol.ncost; ++ci) {
+					const CostDesc& c = pol.cost[ci];
+					float2 g;
+					if (is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
+					else if (c.kind == K_TTCADCA) g = grad_ttcadca(A, N, c, A.vel);
+					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel);
+					else {
+						// CostFunction::GetGradient default: costFunction.cpp:36-54;
+						// lanes 0..3 evaluate the four probes
+						const float d = 0.1f;
+						const int which = lane & 3;
+						float2 probe = A.vel;
+						if (which == 0) probe = vsub(A.vel, V(d, 0));
+						else if (which == 1) probe = vadd(A.vel, V(d, 0));
+						else if (which == 2) probe = vsub(A.vel, V(0, d));
+						else probe = vadd(A.vel, V(0, d));
+						const float cv = eval_cost(A, N, c, P, ci, probe);
+						const float cl = __shfl_sync(0xffffffffu, cv, 0), cr = __shfl_sync(0xffffffffu, cv, 1);
+						const float cb = __shfl_sync(0xffffffffu, cv, 2), ct = __shfl_sync(0xffffffffu, cv, 3);
+						g = V((cr - cl) / (2 * d), (ct - cb) / (2 * d));
+					}
+					T = vadd(T, vmul(g, c.coeff));
+				}
+				acc = vmul(T, -1);
+			} else {
+				float2 best;
+				const CostDesc& c0 = pol.cost[0];
+				if (pol.method == M_GLOBAL && pol.ncost == 1 && c0.kind == K_ORCA) best = P.orca_v;
+				else if (pol.method == M_GLOBAL && pol.ncost == 1 && is_force_based(c0.kind)) best = P.target[0];
+				else {
+					const uint32_t r0 = S.rng[slot];
+					best = sample_min(S, A, N, pol, P, r0, lane);
+					if (pol.table_random) {
+						rng_used = true;
+						rng_next = mulmod(S.lcgpow[2 * pol.nsamples], r0);
+					}
+				}
+				acc = vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt));
+			}
+			acc = vclamp(acc, A.maxacc);
+			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
+		}
+
+		// phase 6: Agent::UpdateVelocityAndPosition (agent.cpp:71-93)
+		if (lane == 0) {
+			const float2 af = vdiv(contact, 80.0f);
+			const float2 vel = vadd(nv, vmul(af, A.dt));
+			const float2 vd = vdiv(vadd(vmul(vel, 2), A.pref), 3);
+			if ((double)vsq(vd) > 0.01) S.view[slot] = vnorm(vd);
+			float2 p = vadd(A.pos, vmul(vel, A.dt));
+			if (S.world == W_TORIC) {   // worldToric.cpp:81-108
+				const float hw = 0.5f * S.width, hh = 0.5f * S.height;
+				float x = p.x, y = p.y;
+				if (x > hw) x -= S.width;
+				else if (x < -hw) x += S.width;
+				if (y > hh) y -= S.height;
+				else if (y < -hh) y += S.height;
+				p = V(x, y);
+			}
+			S.pos[slot] = p;
+			S.vel[slot] = vel;
+			S.vwf[slot] = nv;
+			if (rng_used) S.rng[slot] = rng_next;
+		}
+		__syncwarp();
+	}
+	if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
+}
+
+// GetAgentPositions (APIFunctions.cpp:90-115): one record per agent
+__global__ void k_pack(DevState S)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= S.n) return;
+	const float2 p = S.pos[i], v = S.vel[i], w = S.view[i];
+	AgentRecord r;
+	r.id = S.id[i]; r.px = p.x; r.py = p.y; r.vx = v.x; r.vy = v.y; r.wx = w.x; r.wy = w.y;
+	S.io[i] = r;
+}
+
+// SetAgentPositions (APIFunctions.cpp:117-137): Agent::setPosition and
+// Agent::setVelocity_ExternalApplication for every listed id that exists
+__global__ void k_unpack(DevState S, int m)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= m) return;
+	const AgentRecord r = S.io[k];
+	if (r.id < 0 || r.id >= S.id_bound) return;
+	const int i = S.slot_of_id[r.id];
+	if (i < 0) return;
+	S.pos[i] = V(r.px, r.py);
+	S.vel[i] = V(r.vx, r.vy);
+	S.vwf[i] = V(r.vx, r.vy);
+	S.view[i] = V(r.wx, r.wy);
+}
+
+// ------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------
+template <class T> static bool dalloc(T*& p, size_t n, std::string& err)
+{
+	if (p) cudaFree(p);
+	p = nullptr;
+	cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1));
+	if (e != cudaSuccess) { err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return false; }
+	return true;
+}
+
+Engine* Engine::create(const std::string& xml, std::string& err, const EngineOptions& opt)
+{
+	Engine* e = new Engine();
+	if (!e->init(xml, opt)) {
+		err = e->err_;
+		delete e;
+		return nullptr;
+	}
+	return e;
+}
+
+static uint32_t minstd_seed(uint64_t s)
+{
+	uint32_t x = (uint32_t)(s % LCG_M);
+	return x == 0 ? 1u : x;
+}
+
+bool Engine::init(const std::string& xml, const EngineOptions& opt)
+{
+	opt_ = opt;
+	if (!load_scenario(xml, sc_, err_)) return false;
+	for (const auto& p : sc_.policies) {
+		int norca = 0;
+		for (int c = 0; c < p.ncost; ++c) norca += p.cost[c].kind == K_ORCA;
+		if (norca > 1) { err_ = "a policy with more than one ORCA cost function is not supported"; return false; }
+	}
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+	CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+	CK(cudaEventCreate(&ev0_));
+	CK(cudaEventCreate(&ev1_));
+	CK(cudaEventCreate(&pa0_));
+	CK(cudaEventCreate(&pa1_));
+	CK(cudaEventCreate(&ps0_));
+	CK(cudaEventCreate(&ps1_));
+	d_ = new DevState();
+	std::memset(d_, 0, sizeof(DevState));
+	d_->world = sc_.world; d_->width = sc_.width; d_->height = sc_.height; d_->dt = sc_.dt;
+	d_->cells_per_range = opt_.cells_per_range;
+	float mr = 0;
+	for (const auto& p : sc_.policies) mr = std::max(mr, p.range);
+	d_->max_range = mr;
+	next_unused_id_ = sc_.next_unused_id;
+	// agents present at time 0, in the order the reference adds them
+	for (const auto& a : sc_.agents) {
+		if (a.start_time <= 0) {
+			slot_of_[a.id] = (int)id_.size();
+			id_.push_back(a.id); pol_.push_back(a.policy);
+			pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
+			goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
+			prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
+			rng_.push_back(minstd_seed((unsigned int)a.id));
+			remove_.push_back(a.remove_at_goal ? 1 : 0);
+			// Agent::setGoal: agent.cpp:108-115
+			float2 v0 = make_float2(0, 0);
+			if (a.gx != a.x || a.gy != a.y) {
+				float dx = a.gx - a.x, dy = a.gy - a.y, m = sqrtf(dx * dx + dy * dy);
+				if (m > 0) { dx = dx / m; dy = dy / m; }
+				v0 = make_float2(dx, dy);
+			}
+			view_.push_back(v0);
+			any_remove_at_goal_ |= a.remove_at_goal;
+		} else {
+			pending_.push_back(a);
+		}
+	}
+	std::stable_sort(pending_.begin(), pending_.end(),
+	                 [](const AgentInit& x, const AgentInit& y) { return x.start_time < y.start_time; });
+	for (const auto& a : pending_) any_remove_at_goal_ |= a.remove_at_goal;
+	n_ = (int)id_.size();
+	if (!build_tables()) return false;
+	if (!alloc(std::max(n_, 16))) return false;
+	if (!upload_all()) return false;
+	if (!choose_maxnb()) return false;
+	return true;
+}
+
+bool Engine::build_tables()
+{
+	std::vector<PolicyDesc> pols = sc_.policies;
+	std::vector<SampleEntry> table;
+	int maxrandom = 0;
+	for (auto& p : pols) {
+		p.use_sampling = 0; p.table_random = 0; p.single_cost = 0;
+		p.table_offset = 0; p.nsamples = 0; p.len_divisor = 1;
+		bool sampling = p.method == M_SAMPLING;
+		int type = p.s_type, base = p.s_base, dir = p.s_dir, rad = p.s_radius, ns = p.speed_samples, na = p.angle_samples,
+		    incl = p.include_base;
+		float angle = p.s_angle;
+		if (p.method == M_GLOBAL) {
+			const int k0 = p.cost[0].kind;
+			const bool closed = p.ncost == 1 && (k0 == K_ORCA || k0 == K_SOCIALFORCES || k0 == K_POWERLAW || k0 == K_GOALREACHING);
+			if (!closed) {
+				// SamplingParameters::ApproximateGlobalOptimization: policy.h:74-86
+				sampling = true;
+				type = 0; base = 0; dir = 0; rad = 1; angle = 360; na = 36; ns = 11; incl = 1;
+				p.single_cost = p.ncost == 1 ? 1 : 0;
+			}
+		}
+		if (!sampling) continue;
+		p.use_sampling = 1;
+		p.table_base = base; p.table_dir = dir; p.table_radius = rad;
+		p.max_angle = (float)(angle / 360.0 * 3.1415926535897);
+		if (type == 1) {
+			p.table_random = 1;
+			p.nsamples = std::max(p.random_samples, 0);
+			maxrandom = std::max(maxrandom, p.nsamples);
+			continue;
+		}
+		// regular schedule: costFunction.cpp:122-158 (float angle accumulation)
+		p.table_offset = (int)table.size();
+		const float maxAngle = p.max_angle;
+		const float startAngle = -maxAngle, endAngle = maxAngle;
+		const float deltaAngle = (endAngle - startAngle) / (float)(angle == 360 ? na : (na - 1));
+		p.len_divisor = incl ? (ns - 1) : ns;
+		for (int s = 1; s <= ns; ++s) {
+			float a = startAngle;
+			for (int k = 0; k < na; ++k, a += deltaAngle) {
+				SampleEntry e;
+				e.c = cosf(a); e.s = sinf(a);
+				e.mult = (float)(incl ? s - 1 : s);
+				e.pad = 0;
+				table.push_back(e);
+				if (incl && s == 1) break;
+			}
+		}
+		p.nsamples = (int)table.size() - p.table_offset;
+	}
+	if (table.empty()) table.push_back(SampleEntry{ 0, 0, 0, 0 });
+	std::vector<uint32_t> pw(2 * (size_t)maxrandom + 3);
+	pw[0] = 1;
+	for (size_t k = 1; k < pw.size(); ++k) pw[k] = (uint32_t)(((uint64_t)pw[k - 1] * LCG_A) % LCG_M);
+	PolicyDesc* dp = nullptr;
+	SampleEntry* dt = nullptr;
+	uint32_t* dl = nullptr;
+	if (!dalloc(dp, pols.size(), err_) || !dalloc(dt, table.size(), err_) || !dalloc(dl, pw.size(), err_)) return false;
+	CK(cudaMemcpy(dp, pols.data(), sizeof(PolicyDesc) * pols.size(), cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(dt, table.data(), sizeof(SampleEntry) * table.size(), cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(dl, pw.data(), sizeof(uint32_t) * pw.size(), cudaMemcpyHostToDevice));
+	d_->pols = dp; d_->table = dt; d_->lcgpow = dl;
+	return true;
+}
+
+bool Engine::alloc(int cap)
+{
+	cap_ = cap;
+	DevState& S = *d_;
+	const int mc = std::max(4096, std::min(1 << 24, 4 * cap + 1024));
+	S.max_cells = mc;
+	if (!dalloc(S.pos, cap, err_) || !dalloc(S.vel, cap, err_) || !dalloc(S.goal, cap, err_) ||
+	    !dalloc(S.view, cap, err_) || !dalloc(S.vwf, cap, err_) || !dalloc(S.pref, cap, err_) ||
+	    !dalloc(S.prm, cap, err_) || !dalloc(S.pol, cap, err_) || !dalloc(S.id, cap, err_) ||
+	    !dalloc(S.rng, cap, err_) || !dalloc(S.sP, cap, err_) || !dalloc(S.sV, cap, err_) ||
+	    !dalloc(S.sB, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
+	    !dalloc(S.cell, cap, err_) || !dalloc(S.cnt, mc + 1, err_) || !dalloc(S.start, mc + 1, err_) ||
+	    !dalloc(S.fill, mc + 1, err_) || !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 2, err_))
+		return false;
+	if (!S.grid && !dalloc(S.grid, 1, err_)) return false;
+	if (!S.bbox && !dalloc(S.bbox, 4, err_)) return false;
+	if (!S.status) {
+		if (!dalloc(S.status, 1, err_)) return false;
+		CK(cudaMemset(S.status, 0, sizeof(int)));
+	}
+	CK(cudaMemset(S.cnt, 0, sizeof(int) * (mc + 1)));
+	// bbox sentinels: min = +FLT_MAX, max = -FLT_MAX in ordered encoding
+	auto enc = [](float f) { unsigned u; std::memcpy(&u, &f, 4); return (u & 0x80000000u) ? ~u : (u | 0x80000000u); };
+	unsigned hb[4] = { enc(FLT_MAX), enc(FLT_MAX), enc(-FLT_MAX), enc(-FLT_MAX) };
+	CK(cudaMemcpy(S.bbox, hb, sizeof(hb), cudaMemcpyHostToDevice));
+	invalidate_graph();
+	return true;
+}
+
+bool Engine::upload_all()
+{
+	DevState& S = *d_;
+	S.n = n_;
+	if (n_ > 0) {
+		CK(cudaMemcpy(S.pos, pos_.data(), sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.vel, vel_.data(), sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.goal, goal_.data(), sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.view, view_.data(), sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.vwf, vwf_.data(), sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.prm, prm_.data(), sizeof(float4) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.pol, pol_.data(), sizeof(int) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.id, id_.data(), sizeof(int) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.rng, rng_.data(), sizeof(uint32_t) * n_, cudaMemcpyHostToDevice));
+	}
+	int bound = 1;
+	for (int v : id_) bound = std::max(bound, v + 1);
+	std::vector<int> so(bound, -1);
+	for (int i = 0; i < n_; ++i) so[id_[i]] = i;
+	if (bound > S.id_bound || !S.slot_of_id) {
+		if (!dalloc(S.slot_of_id, (size_t)std::max(bound, 2 * S.id_bound), err_)) return false;
+	}
+	S.id_bound = bound;
+	CK(cudaMemcpy(S.slot_of_id, so.data(), sizeof(int) * bound, cudaMemcpyHostToDevice));
+	if (!dalloc(S.io, (size_t)std::max(cap_, 1), err_)) return false;
+	invalidate_graph();
+	return true;
+}
+
+bool Engine::get_agent_data(void* out)
+{
+	DevState& S = *d_;
+	if (n_ == 0) return true;
+	S.n = n_;
+	k_pack<<<(n_ + 255) / 256, 256, 0, stream_>>>(S);
+	CK(cudaMemcpyAsync(out, S.io, sizeof(AgentRecord) * n_, cudaMemcpyDeviceToHost, stream_));
+	CK(cudaStreamSynchronize(stream_));
+	return true;
+}
+
+bool Engine::set_agent_data(const void* in, int m)
+{
+	DevState& S = *d_;
+	if (m <= 0) return true;
+	if (m > cap_ && !dalloc(S.io, (size_t)m, err_)) return false;
+	CK(cudaMemcpyAsync(S.io, in, sizeof(AgentRecord) * m, cudaMemcpyHostToDevice, stream_));
+	k_unpack<<<(m + 255) / 256, 256, 0, stream_>>>(S, m);
+	CK(cudaGetLastError());
+	CK(cudaStreamSynchronize(stream_));
+	if (m > cap_ && !dalloc(S.io, (size_t)std::max(cap_, 1), err_)) return false;
+	return true;
+}
+
+bool Engine::download_mutable()
+{
+	const DevState& S = *d_;
+	CK(cudaStreamSynchronize(stream_));
+	pos_.resize(n_); vel_.resize(n_); view_.resize(n_); vwf_.resize(n_); rng_.resize(n_);
+	if (n_ > 0) {
+		CK(cudaMemcpy(pos_.data(), S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(vel_.data(), S.vel, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(view_.data(), S.view, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(vwf_.data(), S.vwf, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(rng_.data(), S.rng, sizeof(uint32_t) * n_, cudaMemcpyDeviceToHost));
+	}
+	return true;
+}
+
+// The neighbour-list capacity is sized from the initial state: twice the
+// largest list, rounded up to a power of two (at least 64).  A list that
+// later outgrows it sets ST_NEIGHBOUR_OVERFLOW; sync() then reports the
+// error and the capacity doubles for the following steps.
+bool Engine::choose_maxnb()
+{
+	int want = opt_.max_neighbours;
+	if (want <= 0) {
+		const int probe = 4096;
+		std::vector<int> cnt(std::max(n_, 1));
+		int saved = maxnb_;
+		maxnb_ = probe;
+		if (!neighbours(0, nullptr, nullptr, cnt.data())) { maxnb_ = saved; return false; }
+		int mx = 0;
+		for (int i = 0; i < n_; ++i) mx = std::max(mx, cnt[i]);
+		want = 64;
+		while (want < 2 * mx) want <<= 1;
+	}
+	if (want != maxnb_) {
+		maxnb_ = want;
+		invalidate_graph();
+	}
+	return true;
+}
+
+void Engine::invalidate_graph()
+{
+	if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+	if (graph_) cudaGraphDestroy(graph_);
+	graph_exec_ = nullptr;
+	graph_ = nullptr;
+	graph_valid_ = false;
+}
+
+static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem)
+{
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent, warps_per_block * 32, smem);
+	if (per_sm < 1) per_sm = 1;
+	return num_sms * per_sm;
+}
+
+// Launch shape of k_agent for the current neighbour capacity: as many
+// 4-warp blocks as fit on every SM, and ORCA line scratch for each warp.
+bool Engine::configure()
+{
+	DevState& S = *d_;
+	const int wpb = opt_.warps_per_block;
+	const size_t smem = (size_t)wpb * maxnb_ * 12;
+	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	agent_blocks_ = agent_blocks_for(num_sms_, wpb, smem);
+	S.total_warps = agent_blocks_ * wpb;
+	if (!dalloc(S.scratch, (size_t)S.total_warps * 2 * maxnb_, err_)) return false;
+	configured_maxnb_ = maxnb_;
+	invalidate_graph();
+	return true;
+}
+
+void Engine::enqueue_step()
+{
+	DevState& S = *d_;
+	S.n = n_;
+	S.maxnb = maxnb_;
+	const int wpb = opt_.warps_per_block;
+	const size_t smem = (size_t)wpb * maxnb_ * 12;
+	const int threads = 256;
+	const int nb = std::max(1, (n_ + threads - 1) / threads);
+	if (S.world != W_TORIC) k_bbox<<<std::min(nb, 2 * num_sms_), threads, 0, stream_>>>(S);
+	k_grid<<<1, 1, 0, stream_>>>(S);
+	k_count<<<nb, threads, 0, stream_>>>(S);
+	const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	k_scan_top<<<1, 1024, 0, stream_>>>(S);
+	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	k_scatter<<<nb, threads, 0, stream_>>>(S);
+	if (profile_) cudaEventRecord(pa0_, stream_);
+	k_agent<<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	if (profile_) cudaEventRecord(pa1_, stream_);
+}
+
+int Engine::kernels_per_step() const { return sc_.world == W_TORIC ? 7 : 8; }
+
+bool Engine::capture_graph()
+{
+	invalidate_graph();
+	CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+	enqueue_step();
+	cudaError_t e = cudaStreamEndCapture(stream_, &graph_);
+	if (e != cudaSuccess) { err_ = std::string("graph capture: ") + cudaGetErrorString(e); return false; }
+	CK(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+	graph_valid_ = true;
+	return true;
+}
+
+bool Engine::apply_pending_agents()
+{
+	// WorldBase::DoStep: agents whose start time has come (worldBase.cpp:82-86)
+	if (pending_.empty() || (double)pending_.front().start_time > time_) return true;
+	if (!download_mutable()) return false;
+	size_t k = 0;
+	while (k < pending_.size() && (double)pending_[k].start_time <= time_) {
+		const AgentInit& a = pending_[k];
+		slot_of_[a.id] = (int)id_.size();
+		id_.push_back(a.id); pol_.push_back(a.policy);
+		pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
+		goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
+		prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
+		rng_.push_back(minstd_seed((unsigned int)a.id));
+		remove_.push_back(a.remove_at_goal ? 1 : 0);
+		float2 v0 = make_float2(0, 0);
+		if (a.gx != a.x || a.gy != a.y) {
+			float dx = a.gx - a.x, dy = a.gy - a.y, m = sqrtf(dx * dx + dy * dy);
+			if (m > 0) { dx = dx / m; dy = dy / m; }
+			v0 = make_float2(dx, dy);
+		}
+		view_.push_back(v0);
+		++k;
+	}
+	pending_.erase(pending_.begin(), pending_.begin() + k);
+	n_ = (int)id_.size();
+	if (n_ > cap_ && !alloc(std::max(n_, 2 * cap_))) return false;
+	return upload_all();
+}
+
+bool Engine::remove_at_goal()
+{
+	// WorldBase::DoStep tail: worldBase.cpp:122-127, removeAgentAtListIndex :207-235
+	if (!download_mutable()) return false;
+	bool changed = false;
+	for (int i = n_ - 1; i >= 0; --i) {
+		if (!remove_[i]) continue;
+		const float dx = goal_[i].x - pos_[i].x, dy = goal_[i].y - pos_[i].y;
+		const float r = prm_[i].x;
+		if (dx * dx + dy * dy <= r * r) {
+			const int last = n_ - 1;
+			slot_of_.erase(id_[i]);
+			if (i != last) {
+				id_[i] = id_[last]; pol_[i] = pol_[last]; pos_[i] = pos_[last]; vel_[i] = vel_[last];
+				goal_[i] = goal_[last]; view_[i] = view_[last]; vwf_[i] = vwf_[last]; prm_[i] = prm_[last];
+				rng_[i] = rng_[last]; remove_[i] = remove_[last];
+				slot_of_[id_[i]] = i;
+			}
+			id_.pop_back(); pol_.pop_back(); pos_.pop_back(); vel_.pop_back(); goal_.pop_back();
+			view_.pop_back(); vwf_.pop_back(); prm_.pop_back(); rng_.pop_back(); remove_.pop_back();
+			--n_;
+			changed = true;
+		}
+	}
+	return changed ? upload_all() : true;
+}
+
+bool Engine::step(int nsteps)
+{
+	if (nsteps <= 0) return true;
+	const bool dynamic = !pending_.empty() || any_remove_at_goal_;
+	if (time_kernels) CK(cudaEventRecord(ev0_, stream_));
+	if (configured_maxnb_ != maxnb_ && !configure()) return false;
+	for (int s = 0; s < nsteps; ++s) {
+		if (!pending_.empty() && !apply_pending_agents()) return false;
+		if (opt_.use_graph && !dynamic && !profile_) {
+			if (!graph_valid_ && !capture_graph()) return false;
+			CK(cudaGraphLaunch(graph_exec_, stream_));
+		} else {
+			if (profile_) CK(cudaEventRecord(ps0_, stream_));
+			enqueue_step();
+			CK(cudaGetLastError());
+			if (profile_) {
+				CK(cudaEventRecord(ps1_, stream_));
+				CK(cudaEventSynchronize(ps1_));
+				float a = 0, b = 0;
+				cudaEventElapsedTime(&a, pa0_, pa1_);
+				cudaEventElapsedTime(&b, ps0_, ps1_);
+				prof_agent_ms_ += a;
+				prof_step_ms_ += b;
+				prof_steps_ += 1;
+			}
+		}
+		time_ += sc_.dt;
+		if (any_remove_at_goal_ && !remove_at_goal()) return false;
+	}
+	if (time_kernels) {
+		CK(cudaEventRecord(ev1_, stream_));
+		CK(cudaEventSynchronize(ev1_));
+		float ms = 0;
+		cudaEventElapsedTime(&ms, ev0_, ev1_);
+		agent_ms_ = ms / nsteps;
+	}
+	return true;
+}
+
+bool Engine::sync()
+{
+	CK(cudaStreamSynchronize(stream_));
+	int st = 0;
+	CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
+	if (st) {
+		CK(cudaMemset(d_->status, 0, sizeof(int)));
+		if (st & ST_NEIGHBOUR_OVERFLOW) {
+			err_ = "neighbour list longer than the capacity of " + std::to_string(maxnb_) +
+			       "; the capacity has been doubled for the following steps";
+			maxnb_ *= 2;
+			invalidate_graph();
+			return false;
+		}
+		if (st & ST_GRID_OVERFLOW) { err_ = "non-finite agent positions"; return false; }
+		err_ = "device status " + std::to_string(st);
+		return false;
+	}
+	return true;
+}
+
+bool Engine::get_state(int* ids, float* pos, float* vel, float* view, float* pref, float* goal)
+{
+	const DevState& S = *d_;
+	CK(cudaStreamSynchronize(stream_));
+	if (n_ == 0) return true;
+	if (ids) std::memcpy(ids, id_.data(), sizeof(int) * n_);
+	if (pos) CK(cudaMemcpy(pos, S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+	if (vel) CK(cudaMemcpy(vel, S.vel, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+	if (view) CK(cudaMemcpy(view, S.view, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+	if (pref) CK(cudaMemcpy(pref, S.pref, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+	if (goal) CK(cudaMemcpy(goal, S.goal, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
+	return true;
+}
+
+bool Engine::set_state(const float* pos, const float* vel, const float* view)
+{
+	const DevState& S = *d_;
+	CK(cudaStreamSynchronize(stream_));
+	if (n_ == 0) return true;
+	if (pos) CK(cudaMemcpy(S.pos, pos, sizeof(float2) * n_, cudaMemcpyHostToDevice));
+	if (vel) {
+		CK(cudaMemcpy(S.vel, vel, sizeof(float2) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.vwf, vel, sizeof(float2) * n_, cudaMemcpyHostToDevice));
+	}
+	if (view) CK(cudaMemcpy(S.view, view, sizeof(float2) * n_, cudaMemcpyHostToDevice));
+	return true;
+}
+
+bool Engine::set_agent_by_id(int id, float px, float py, float vx, float vy, float wx, float wy)
+{
+	auto it = slot_of_.find(id);
+	if (it == slot_of_.end()) return true;   // SetAgentPositions skips unknown ids
+	const int i = it->second;
+	const DevState& S = *d_;
+	float2 p = make_float2(px, py), v = make_float2(vx, vy), w = make_float2(wx, wy);
+	CK(cudaMemcpyAsync(S.pos + i, &p, sizeof(float2), cudaMemcpyHostToDevice, stream_));
+	CK(cudaMemcpyAsync(S.vel + i, &v, sizeof(float2), cudaMemcpyHostToDevice, stream_));
+	CK(cudaMemcpyAsync(S.vwf + i, &v, sizeof(float2), cudaMemcpyHostToDevice, stream_));
+	CK(cudaMemcpyAsync(S.view + i, &w, sizeof(float2), cudaMemcpyHostToDevice, stream_));
+	CK(cudaStreamSynchronize(stream_));
+	return true;
+}
+
+bool Engine::set_goal(int id, float x, float y)
+{
+	// Agent::setGoal: agent.cpp:108-115
+	auto it = slot_of_.find(id);
+	if (it == slot_of_.end()) { err_ = "no agent with id " + std::to_string(id); return false; }
+	const int i = it->second;
+	const DevState& S = *d_;
+	float2 p;
+	CK(cudaStreamSynchronize(stream_));
+	CK(cudaMemcpy(&p, S.pos + i, sizeof(float2), cudaMemcpyDeviceToHost));
+	float2 g = make_float2(x, y);
+	goal_[i] = g;
+	CK(cudaMemcpy(S.goal + i, &g, sizeof(float2), cudaMemcpyHostToDevice));
+	if (g.x != p.x || g.y != p.y) {
+		float dx = g.x - p.x, dy = g.y - p.y, m = sqrtf(dx * dx + dy * dy);
+		if (m > 0) { dx = dx / m; dy = dy / m; }
+		float2 w = make_float2(dx, dy);
+		CK(cudaMemcpy(S.view + i, &w, sizeof(float2), cudaMemcpyHostToDevice));
+	}
+	return true;
+}
+
+bool Engine::add_agent(float x, float y, float radius, float pref, float maxs, float maxacc, int policy_id,
+                       int desired_id, int* out_id)
+{
+	// AddAgent (APIFunctions.cpp:139-171) -> WorldBase::AddAgent (worldBase.cpp:161-186)
+	int pidx = -1;
+	for (size_t k = 0; k < sc_.policy_ids.size(); ++k)
+		if (sc_.policy_ids[k] == policy_id) pidx = (int)k;
+	if (pidx < 0) { err_ = "no policy with id " + std::to_string(policy_id); return false; }
+	if (!download_mutable()) return false;
+	int id = (desired_id >= 0 && !slot_of_.count(desired_id)) ? desired_id : next_unused_id_;
+	if (id >= next_unused_id_) next_unused_id_ = id + 1;
+	slot_of_[id] = (int)id_.size();
+	id_.push_back(id); pol_.push_back(pidx);
+	pos_.push_back(make_float2(x, y)); vel_.push_back(make_float2(0, 0));
+	goal_.push_back(make_float2(x, y)); vwf_.push_back(make_float2(0, 0));
+	view_.push_back(make_float2(0, 0));
+	prm_.push_back(make_float4(radius, pref, maxs, maxacc));
+	rng_.push_back(minstd_seed((unsigned int)id));
+	remove_.push_back(0);
+	n_ = (int)id_.size();
+	if (n_ > cap_ && !alloc(std::max(n_, 2 * cap_))) return false;
+	if (!upload_all()) return false;
+	if (out_id) *out_id = id;
+	return true;
+}
+
+bool Engine::remove_agent(int id)
+{
+	// WorldBase::RemoveAgent (worldBase.cpp:198-235): the last agent moves into the gap
+	auto it = slot_of_.find(id);
+	if (it == slot_of_.end()) { err_ = "no agent with id " + std::to_string(id); return false; }
+	if (!download_mutable()) return false;
+	const int i = it->second, last = n_ - 1;
+	slot_of_.erase(id);
+	if (i != last) {
+		id_[i] = id_[last]; pol_[i] = pol_[last]; pos_[i] = pos_[last]; vel_[i] = vel_[last];
+		goal_[i] = goal_[last]; view_[i] = view_[last]; vwf_[i] = vwf_[last]; prm_[i] = prm_[last];
+		rng_[i] = rng_[last]; remove_[i] = remove_[last];
+		slot_of_[id_[i]] = i;
+	}
+	id_.pop_back(); pol_.pop_back(); pos_.pop_back(); vel_.pop_back(); goal_.pop_back();
+	view_.pop_back(); vwf_.pop_back(); prm_.pop_back(); rng_.pop_back(); remove_.pop_back();
+	n_ = last;
+	return upload_all();
+}
+
+bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
+{
+	DevState& S = *d_;
+	CK(cudaStreamSynchronize(stream_));
+	if (n_ == 0) return true;
+	const int dcap = std::max(cap, 1);
+	if (!dalloc(S.dump_ids, (size_t)n_ * dcap, err_) || !dalloc(S.dump_d2, (size_t)n_ * dcap, err_) ||
+	    !dalloc(S.dump_cnt, n_, err_))
+		return false;
+	S.dump_cap = dcap;
+	// same grid build and gather as a step, no state update
+	DevState T = S;
+	T.n = n_;
+	const int dump_nb = std::max(maxnb_, 4096);
+	T.maxnb = dump_nb;
+	const int wpb = opt_.warps_per_block;
+	const size_t smem = (size_t)wpb * dump_nb * 12;
+	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const int blocks = agent_blocks_for(num_sms_, wpb, smem);
+	T.total_warps = blocks * wpb;
+	float4* scr = nullptr;
+	if (!dalloc(scr, (size_t)T.total_warps * 2 * dump_nb, err_)) return false;
+	T.scratch = scr;
+	const int threads = 256, nb = (n_ + threads - 1) / threads;
+	if (T.world != W_TORIC) k_bbox<<<std::min(nb, 2 * num_sms_), threads, 0, stream_>>>(T);
+	k_grid<<<1, 1, 0, stream_>>>(T);
+	k_count<<<nb, threads, 0, stream_>>>(T);
+	const int sb = (T.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
+	k_scan_top<<<1, 1024, 0, stream_>>>(T);
+	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
+	k_scatter<<<nb, threads, 0, stream_>>>(T);
+	k_agent<<<blocks, wpb * 32, smem, stream_>>>(T, 1);
+	CK(cudaGetLastError());
+	CK(cudaStreamSynchronize(stream_));
+	cudaFree(scr);
+	int st = 0;
+	CK(cudaMemcpy(&st, S.status, sizeof(int), cudaMemcpyDeviceToHost));
+	CK(cudaMemset(S.status, 0, sizeof(int)));
+	if (counts) CK(cudaMemcpy(counts, S.dump_cnt, sizeof(int) * n_, cudaMemcpyDeviceToHost));
+	if (ids && cap > 0) CK(cudaMemcpy(ids, S.dump_ids, sizeof(int) * (size_t)n_ * cap, cudaMemcpyDeviceToHost));
+	if (d2 && cap > 0) CK(cudaMemcpy(d2, S.dump_d2, sizeof(float) * (size_t)n_ * cap, cudaMemcpyDeviceToHost));
+	if (st & ST_NEIGHBOUR_OVERFLOW) { err_ = "neighbour list longer than " + std::to_string(dump_nb); return false; }
+	// the dump kernel leaves the step's scratch sizes as they were
+	return true;
+}
+
+void* Engine::device_positions() const { return d_->pos; }
+void* Engine::device_velocities() const { return d_->vel; }
+
+Engine::~Engine()
+{
+	if (stream_) cudaStreamSynchronize(stream_);
+	invalidate_graph();
+	if (d_) {
+		DevState& S = *d_;
+		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB,
+		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.fill, S.blocksum, S.grid, S.bbox, S.status,
+		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io };
+		for (void* p : ptrs)
+			if (p) cudaFree(p);
+		delete d_;
+	}
+	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_ })
+		if (e) cudaEventDestroy(e);
+	if (ev0_) cudaEventDestroy(ev0_);
+	if (ev1_) cudaEventDestroy(ev1_);
+	if (stream_) cudaStreamDestroy(stream_);
+}
+
+}  // namespace umans

@@ -1,0 +1,123 @@
+// One simulation on one GPU: the GB300 replacement of WorldBase::DoStep
+// (src/Engine/core/worldBase.cpp:79-128) behind the reference's simulation
+// interface (CrowdSimulator / WorldBase / Agent, src/Engine/core/).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "model.hpp"
+#include "scenario.hpp"
+
+namespace umans {
+
+struct DevState;   // device pointers (engine.cu)
+
+struct EngineOptions {
+	int max_neighbours = 0;        // 0: chosen from the initial state
+	float cells_per_range = 2.0f;  // grid cell size = range / cells_per_range
+	int warps_per_block = 4;
+	bool use_graph = true;
+};
+
+class Engine {
+public:
+	static Engine* create(const std::string& xml, std::string& err, const EngineOptions& opt = EngineOptions());
+	~Engine();
+
+	// Enqueues n steps on the engine's stream; returns false on a host-side
+	// error.  Device-side errors are reported by sync().
+	bool step(int n);
+	bool sync();
+
+	int num_agents() const { return n_; }
+	double time() const { return time_; }
+	float dt() const { return sc_.dt; }
+	float end_time() const { return sc_.end_time; }
+	const std::string& error() const { return err_; }
+	cudaStream_t stream() const { return stream_; }
+	int max_neighbours() const { return maxnb_; }
+
+	// host <-> device state, list order (the reference's agents_ order)
+	bool get_state(int* ids, float* pos, float* vel, float* view, float* pref = nullptr, float* goal = nullptr);
+	bool set_state(const float* pos, const float* vel, const float* view);   // all agents, list order
+	bool set_agent_by_id(int id, float px, float py, float vx, float vy, float wx, float wy);
+	// AgentData records (include/umans_gb300.h), one bulk copy each way
+	bool get_agent_data(void* out);
+	bool set_agent_data(const void* in, int m);
+	bool set_goal(int id, float x, float y);
+	bool add_agent(float x, float y, float radius, float pref, float maxs, float maxacc, int policy_id,
+	               int desired_id, int* out_id);
+	bool remove_agent(int id);
+
+	// neighbour lists the next step would use: ids and PhantomAgent distSqr,
+	// `cap` entries per agent; counts[i] = full list length.
+	bool neighbours(int cap, int* ids, float* d2, int* counts);
+
+	// device pointers of the raw state for callers that keep data on the GPU
+	void* device_positions() const;
+	void* device_velocities() const;
+
+	// timing of the step kernels (ms, averaged over the last step() call)
+	float last_agent_kernel_ms() const { return agent_ms_; }
+	bool time_kernels = false;
+
+	// Profiling mode: every step is launched without the graph, with CUDA
+	// events on the engine's stream around the step and around k_agent;
+	// the elapsed times accumulate until reset.
+	void set_profile(bool on) { profile_ = on; prof_agent_ms_ = prof_step_ms_ = 0; prof_steps_ = 0; }
+	void profile_totals(double* agent_ms, double* step_ms, int* steps) const
+	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; }
+	int kernels_per_step() const;
+
+private:
+	Engine() = default;
+	bool init(const std::string& xml, const EngineOptions& opt);
+	bool upload_all();
+	bool alloc(int cap);
+	bool build_tables();
+	bool choose_maxnb();
+	bool configure();
+	void enqueue_step();
+	bool capture_graph();
+	void invalidate_graph();
+	bool apply_pending_agents();
+	bool remove_at_goal();
+	bool download_mutable();
+
+	Scenario sc_;
+	EngineOptions opt_;
+	std::string err_;
+	int n_ = 0, cap_ = 0;
+	double time_ = 0;
+	int maxnb_ = 0, configured_maxnb_ = -1;
+	int num_sms_ = 0, agent_blocks_ = 0;
+	int next_unused_id_ = 0;
+	bool any_remove_at_goal_ = false;
+	float agent_ms_ = 0;
+
+	// host mirror, list order
+	std::vector<int> id_, pol_;
+	std::vector<float2> pos_, vel_, goal_, view_, vwf_;
+	std::vector<float4> prm_;   // radius, pref speed, max speed, max acceleration
+	std::vector<uint32_t> rng_;
+	std::vector<unsigned char> remove_;
+	std::unordered_map<int, int> slot_of_;
+	std::vector<AgentInit> pending_;   // start_time > now, sorted by start_time
+
+	DevState* d_ = nullptr;
+	cudaStream_t stream_ = nullptr;
+	cudaGraph_t graph_ = nullptr;
+	cudaGraphExec_t graph_exec_ = nullptr;
+	bool graph_valid_ = false;
+	cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+	cudaEvent_t pa0_ = nullptr, pa1_ = nullptr, ps0_ = nullptr, ps1_ = nullptr;
+	bool profile_ = false;
+	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
+	int prof_steps_ = 0;
+};
+
+}  // namespace umans

@@ -186,6 +186,9 @@ def batch_member(k: int, n: int, seed: int = 4) -> Scenario:
         r = max(n * 1.5 / (2 * math.pi), 2.0)
         ang = 2.0 * np.pi * np.arange(n) / n
         pos = np.stack([r * np.cos(ang), r * np.sin(ang)], 1)
+        # small jitter: exact distance ties on a symmetric circle are ordered
+        # by the reference's kd-tree traversal, which nothing else reproduces
+        pos = pos + rng.uniform(-0.01, 0.01, pos.shape)
         goal = -pos
     else:
         side = math.sqrt(n / 0.5)
@@ -214,3 +217,86 @@ def calibration_set(params=None, n: int = 512, side: float = 40.0, seed: int = 5
     goal = rng.uniform(-side / 2, side / 2, (n, 2))
     pol = CALIBRATION_POLICY.format(pid=0, **{k: _f(v) for k, v in p.items()})
     return Scenario(dt=0.1, world="Infinite", policies=[pol], **_agents(n, pos, goal))
+
+
+# The policy configurations the reference ships, one per navigation model
+# (parameter values as in the reference's examples/policies/*.xml; the same
+# values are needed for trajectories to be comparable).
+MODEL_POLICIES = {
+    "ORCA": '<Policy id="0" OptimizationMethod="global" RelaxationTime="0">'
+            '<costfunction range="5" name="ORCA"/></Policy>',
+    "RVO": '<Policy id="0" OptimizationMethod="sampling" SamplingType="random" SamplingBase="current velocity" '
+           'SamplingBaseDirection="unit" SamplingAngle="360" RandomSamples="250" '
+           'SamplingRadius="maximum acceleration" RelaxationTime="0">'
+           '<costfunction range="5" name="RVO"/></Policy>',
+    "SocialForces": '<Policy id="0" OptimizationMethod="gradient" RelaxationTime="0.5">'
+                    '<costfunction range="5" name="SocialForcesAvoidance"/>'
+                    '<costfunction name="GoalReachingForce"/></Policy>',
+    "PowerLaw": '<Policy id="0" OptimizationMethod="gradient" RelaxationTime="0.5">'
+                '<costfunction range="5" name="PowerLaw"/><costfunction name="GoalReachingForce"/></Policy>',
+    "Karamouzas": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+                  'SamplingBaseDirection="preferred velocity" SamplingAngle="180" SpeedSamples="15" '
+                  'AngleSamples="19" SamplingRadius="maximum speed" RelaxationTime="0" IncludeBaseAsSample="true">'
+                  '<costfunction range="5" name="Karamouzas"/></Policy>',
+    "Moussaid": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+                'SamplingBaseDirection="preferred velocity" SamplingAngle="180" SpeedSamples="5" '
+                'AngleSamples="19" SamplingRadius="preferred speed" RelaxationTime="0.5">'
+                '<costfunction range="5" name="Moussaid"/></Policy>',
+    "VanToll": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+               'SamplingBaseDirection="preferred velocity" SamplingAngle="180" SpeedSamples="2" '
+               'AngleSamples="19" SamplingRadius="preferred speed" RelaxationTime="0.25">'
+               '<costfunction range="5" name="VanToll"/></Policy>',
+    "PLEdestrians": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+                    'SamplingBaseDirection="unit" SamplingAngle="360" SpeedSamples="4" AngleSamples="36" '
+                    'SamplingRadius="maximum speed" RelaxationTime="0.5">'
+                    '<costfunction range="5" name="PLEdestrians" t_min="0.5" t_max="3"/></Policy>',
+    "Paris": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+             'SamplingBaseDirection="unit" SamplingAngle="360" SpeedSamples="4" AngleSamples="36" '
+             'SamplingRadius="maximum speed" RelaxationTime="0">'
+             '<costfunction range="5" name="Paris"/></Policy>',
+    "Dutra": '<Policy id="0" OptimizationMethod="gradient">'
+             '<costfunction coeff="20" range="5" name="TtcaDca" sigmaTtca="1" sigmaDca="0.3" '
+             'sigmaAngle_goal="2" sigmaSpeed_goal="2"/></Policy>',
+    "FOEAvoidance": '<Policy id="0" OptimizationMethod="gradient">'
+                    '<costfunction range="5" name="FOEAvoidance" coeff="3"/>'
+                    '<costfunction name="GoalReachingForce"/></Policy>',
+}
+
+
+def model_circle(model: str, n: int = 24, radius_m: float = 8.0, pref: float = 1.3, maxs: float = 1.6,
+                 jitter: float = 0.01, seed: int = 10) -> Scenario:
+    """n agents on a circle swapping sides, with one of the shipped model policies.
+
+    Positions get a seeded jitter of +-``jitter`` m: on a perfectly symmetric
+    circle many neighbour distances tie exactly, and the reference orders
+    tied neighbours by its kd-tree traversal, which no other implementation
+    reproduces (the summation order then differs in the last bit).
+    """
+    ang = 2.0 * np.pi * np.arange(n) / n
+    pos = np.stack([radius_m * np.cos(ang), radius_m * np.sin(ang)], 1)
+    if jitter:
+        pos = pos + np.random.default_rng(seed).uniform(-jitter, jitter, pos.shape)
+    return Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
+                    **_agents(n, pos, -pos, pref=pref, maxs=maxs))
+
+
+def model_crossing(model: str, n: int = 40, seed: int = 11) -> Scenario:
+    """Two jittered groups crossing at 90 degrees, with one of the model policies."""
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    a = np.stack([rng.uniform(-12, -6, h), rng.uniform(-3, 3, h)], 1)
+    b = np.stack([rng.uniform(-3, 3, n - h), rng.uniform(-12, -6, n - h)], 1)
+    pos = np.concatenate([a, b])
+    goal = np.concatenate([a + [20, 0], b + [0, 20]])
+    return Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
+                    **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+
+
+def model_toric(model: str, n: int = 60, side: float = 12.0, seed: int = 12) -> Scenario:
+    """A small toric world (wrap-around neighbours, including displaced
+    duplicates when the range exceeds half the side)."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-side / 2, side / 2, (n, 2))
+    goal = pos + rng.uniform(-30, 30, (n, 2))
+    return Scenario(dt=0.1, world="Toric", width=side, height=side, policies=[MODEL_POLICIES[model]],
+                    **_agents(n, pos, goal, pref=1.3, maxs=1.6))
