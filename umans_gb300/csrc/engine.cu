@@ -116,7 +116,8 @@ __global__ void k_grid(DevState S)
 	}
 	float cs = S.max_range / S.cells_per_range;
 	if (!(cs >= 1e-3f)) cs = 1e-3f;
-	while (((double)ex / cs + 1.0) * ((double)ey / cs + 1.0) > (double)S.max_cells) cs *= 2.0f;
+	// +2 per axis: nx, ny below come from float divisions that may round up
+	while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)S.max_cells) cs *= 2.0f;
 	GridParams g;
 	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
 	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
