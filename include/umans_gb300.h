@@ -123,6 +123,11 @@ int umans_device_state(umans_sim* sim, void** pos, void** vel);
 int umans_profile(umans_sim* sim, int enable);
 int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_ms, int* steps,
                          int* kernels_per_step);
+/* Test hook: the device's exponential used by the force models, which
+ * returns exactly the host C library's expf for x in [-87, 0]; evaluates n
+ * values and reports the size of the exception table.  Errors are reported
+ * through umans_last_error(NULL). */
+int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions);
 /* the last error of this handle, or of the last failed umans_create when sim is null */
 const char* umans_last_error(umans_sim* sim);
 

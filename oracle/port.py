@@ -283,12 +283,21 @@ def _load():
         lib.up_state.argtypes = [P, P, P, P, P, P, P]
         lib.up_set_state.argtypes = [P, P, P, P]
         lib.up_neighbors.argtypes = [P, C.c_int, P, P, P, P, C.c_int]
+        lib.up_libm_expf.argtypes = [P, P, C.c_long]
         _lib = lib
     return _lib
 
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def libm_expf(x: np.ndarray) -> np.ndarray:
+    """The host C library's expf, elementwise (float32)."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.empty_like(x)
+    _load().up_libm_expf(_p(x), _p(y), x.size)
+    return y
 
 
 class PortSim:

@@ -1176,6 +1176,12 @@ void up_set_state(up_world* w, const float* pos, const float* vel, const float* 
 	}
 }
 
+/* the host C library's expf over an array (checks the device exponential) */
+void up_libm_expf(const float* x, float* y, long n)
+{
+	for (long i = 0; i < n; ++i) y[i] = expf(x[i]);
+}
+
 int up_neighbors(const up_world* w, int i, long long* ids, float* dist2, float* px, float* py, int cap)
 {
 	const nbrlist* L = &w->nb[i];

@@ -81,6 +81,8 @@ void up_set_state(up_world* w, const float* pos, const float* vel, const float* 
 int up_neighbors(const up_world* w, int i, long long* ids, float* dist2,
                  float* px, float* py, int cap);
 
+void up_libm_expf(const float* x, float* y, long n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@ _SIGS = {
     "umans_profile": (C.c_int, [P, C.c_int]),
     "umans_profile_totals": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int)]),
+    "umans_debug_ref_expf": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_size_t)]),
     "umans_last_error": (C.c_char_p, [P]),
 }
 

@@ -219,6 +219,14 @@ int umans_profile_totals(umans_sim* s, double* agent_kernel_ms, double* step_ms,
 	return UMANS_OK;
 }
 
+int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
+{
+	if ((n > 0 && (!x || !y)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	std::string err;
+	if (!umans::debug_ref_expf(x, y, n, exceptions, err)) return fail(nullptr, UMANS_ERR_CUDA, err);
+	return UMANS_OK;
+}
+
 const char* umans_last_error(umans_sim* s)
 {
 	return s ? s->err.c_str() : g_create_error.c_str();

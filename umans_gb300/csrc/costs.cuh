@@ -8,6 +8,7 @@
 #pragma once
 #include "devmath.cuh"
 #include "model.hpp"
+#include "refmath.hpp"
 
 namespace umans {
 
@@ -41,6 +42,7 @@ UD float2 nb_pref(const NbView& N, int k)
 struct AgentCtx {
 	float2 pos, vel, pref, goal;
 	float radius, prefspeed, maxspeed, maxacc, dt, relax;
+	ExpExceptions ex;    // host-expf exceptions (refmath.hpp)
 };
 
 // ComputeTimeToFirstCollision: costFunction.cpp:229-268 (agents only)
@@ -77,7 +79,7 @@ UD float2 sf_force(const AgentCtx& A, const CostDesc& c, float2 np, float2 nv, f
 	const float d_magR2 = 1 / (2 * magR2) * (2 * magR - 2 * magV * vcosangle(R, Vv));
 	const float d_bSquared2 = 2 * (magR + magR2) * (1 + d_magR2);
 	const float d_b = (1 / (8 * b)) * d_bSquared2;
-	const float d_V = -V0 / sigma * expf(-b / sigma) * d_b;
+	const float d_V = -V0 / sigma * ref_expf(A.ex, -b / sigma) * d_b;
 	const float2 F = vmul(vneg(R), d_V);
 	// viewingAngleHalf = (float)(100 deg in rad); cos of it to 1e-8
 	const float viewHalf = (float)(100.0 * REF_PI / 180.0);
@@ -100,7 +102,7 @@ UD float2 pl_force(const AgentCtx& A, const CostDesc& c, float2 np, float2 nv, f
 	const float tau = (b - sqrtD) / a;
 	if (tau < 0.001f) return V(0, 0);
 	if (tau > tau0) return V(0, 0);
-	const float comp1 = -k * expf(-tau / tau0) * (2 / tau + 1 / tau0) / (a * tau * tau);
+	const float comp1 = -k * ref_expf(A.ex, -tau / tau0) * (2 / tau + 1 / tau0) / (a * tau * tau);
 	const float2 comp2 = vsub(v, vdiv(vadd(vmul(x, a), vmul(v, b)), sqrtD));
 	return vmul(comp2, comp1);
 }
@@ -323,7 +325,7 @@ UD float cost_foe(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 
 		const float xf = Vel.x / Vel.y, xg = Pos.x / Pos.y, dx = xg - xf;
 		const float ttc = -Pos.y / Vel.y;
 		const float sigma = (float)__ddiv_rn((double)((A.radius + nb_radius(N, k)) / Pos.y), LN10);
-		cost += foe_importance(ttc) * expf(-fabsf(dx) / sigma);
+		cost += foe_importance(ttc) * ref_expf(A.ex, -fabsf(dx) / sigma);
 	}
 	return cost;
 }

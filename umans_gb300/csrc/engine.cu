@@ -56,6 +56,7 @@ struct DevState {
 	float4* scratch;
 	int maxnb, total_warps, max_cells;
 	float max_range, cells_per_range;
+	ExpExceptions expx;   // host-expf exception table
 	int* slot_of_id;      // id -> list slot, -1 when absent
 	int id_bound;         // size of slot_of_id
 	AgentRecord* io;      // staging for AgentData exchange
@@ -719,7 +720,7 @@ __device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c
 		const float ttc = -Pos.y / Vel.y;
 		const float sigma = (float)__ddiv_rn((double)((A.radius + nb_radius(N, k)) / Pos.y), LN10);
 		const float sg = (float)((0 < dx) - (dx < 0));
-		const float E = foe_importance(ttc) * expf(-fabsf(dx) / sigma);
+		const float E = foe_importance(ttc) * ref_expf(A.ex, -fabsf(dx) / sigma);
 		gt += E * sg * (xf * xf - xg * xg - (vmag(v) / (-Vel.y))) / sigma;
 		gv += E * sg * (-xf / (-Vel.y)) / sigma;
 	}
@@ -856,7 +857,7 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 		AgentCtx A;
 		A.pos = S.sP[t]; A.vel = S.sV[t]; A.pref = V(sb.x, sb.y); A.goal = S.goal[slot];
 		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
-		A.dt = S.dt; A.relax = pol.relax_time;
+		A.dt = S.dt; A.relax = pol.relax_time; A.ex = S.expx;
 
 		const int K = gather(S, G, L, t, A.pos, pol.range, lane, &overflow);
 		NbView N;
@@ -995,6 +996,29 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 	if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 }
 
+__global__ void k_ref_expf(ExpExceptions T, const float* x, float* y, int n)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) y[i] = ref_expf(T, x[i]);
+}
+
+// Evaluates the device's reference-exact expf on n host values (tests).
+bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err)
+{
+	ExpExceptions T;
+	if (!exp_exceptions_for_device(&T, exceptions, err)) return false;
+	float *dx = nullptr, *dy = nullptr;
+	if (cudaMalloc(&dx, sizeof(float) * std::max(n, 1)) != cudaSuccess ||
+	    cudaMalloc(&dy, sizeof(float) * std::max(n, 1)) != cudaSuccess) { err = "cudaMalloc"; return false; }
+	cudaMemcpy(dx, x, sizeof(float) * n, cudaMemcpyHostToDevice);
+	if (n > 0) k_ref_expf<<<(n + 255) / 256, 256>>>(T, dx, dy, n);
+	cudaError_t e = cudaMemcpy(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost);
+	cudaFree(dx);
+	cudaFree(dy);
+	if (e != cudaSuccess) { err = cudaGetErrorString(e); return false; }
+	return true;
+}
+
 // GetAgentPositions (APIFunctions.cpp:90-115): one record per agent
 __global__ void k_pack(DevState S)
 {
@@ -1105,6 +1129,11 @@ bool Engine::init(const std::string& xml, const EngineOptions& opt)
 	                 [](const AgentInit& x, const AgentInit& y) { return x.start_time < y.start_time; });
 	for (const auto& a : pending_) any_remove_at_goal_ |= a.remove_at_goal;
 	n_ = (int)id_.size();
+	bool need_exp = false;
+	for (const auto& p : sc_.policies)
+		for (int c = 0; c < p.ncost; ++c)
+			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE;
+	if (need_exp && !exp_exceptions_for_device(&d_->expx, nullptr, err_)) return false;
 	if (!build_tables()) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;

@@ -16,6 +16,9 @@ namespace umans {
 
 struct DevState;   // device pointers (engine.cu)
 
+// device evaluation of the reference-exact expf (refmath.hpp), for tests
+bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err);
+
 struct EngineOptions {
 	int max_neighbours = 0;        // 0: chosen from the initial state
 	float cells_per_range = 2.0f;  // grid cell size = range / cells_per_range
