@@ -268,8 +268,8 @@ __device__ __forceinline__ float ref_expf(const ExpExceptions& T, float x)
 	uint32_t h = ff_hash(b, T.shift);
 	for (;;) {
 		const uint2 e = __ldg(&T.slots[h]);
+		if (e.x == 0) return y;   // empty slot (keys are never 0: +0.0 is not stored)
 		if (e.x == b) return __uint_as_float(e.y);
-		if (e.x == 0) return y;
 		h = (h + 1) & T.mask;
 	}
 }
