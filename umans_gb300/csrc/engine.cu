@@ -28,6 +28,7 @@
 #include <cstring>
 
 #include "costs.cuh"
+#include "orca.cuh"
 
 namespace umans {
 
@@ -476,106 +477,6 @@ __device__ __forceinline__ float2 target_velocity(const AgentCtx& A, const NbVie
 __device__ __forceinline__ bool is_force_based(int kind)
 {
 	return kind == K_SOCIALFORCES || kind == K_POWERLAW || kind == K_GOALREACHING;
-}
-
-// ------------------------------------------------------------------------
-// ORCA (ORCASolver.cpp:61-326, CostFunctions/ORCA.cpp:26-95)
-// lines are float4 (point.x, point.y, direction.x, direction.y)
-// ------------------------------------------------------------------------
-__device__ __forceinline__ float det2(float2 a, float2 b) { return a.x * b.y - a.y * b.x; }
-__device__ __forceinline__ float2 lp_point(float4 l) { return V(l.x, l.y); }
-__device__ __forceinline__ float2 lp_dir(float4 l) { return V(l.z, l.w); }
-
-__device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res)
-{
-	const float4 ln = L[lineNo];
-	const float2 P = lp_point(ln), D = lp_dir(ln);
-	const float dp = vdot(P, D);
-	const float disc = dp * dp + radius * radius - vsq(P);
-	if (disc < 0.0f) return false;
-	const float sd = sqrtf(disc);
-	float tl = -dp - sd, tr = -dp + sd;
-	for (int i = 0; i < lineNo; ++i) {
-		const float4 li = L[i];
-		const float den = det2(D, lp_dir(li));
-		const float num = det2(lp_dir(li), vsub(P, lp_point(li)));
-		if (fabsf(den) <= 0.00001f) {
-			if (num < 0.0f) return false;
-			continue;
-		}
-		const float t = num / den;
-		if (den >= 0.0f) tr = fminr(tr, t);
-		else tl = fmaxr(tl, t);
-		if (tl > tr) return false;
-	}
-	if (dirOpt) {
-		if (vdot(opt, D) > 0.0f) *res = vadd(P, vmul(D, tr));
-		else *res = vadd(P, vmul(D, tl));
-	} else {
-		const float t = vdot(D, vsub(opt, P));
-		if (t < tl) *res = vadd(P, vmul(D, tl));
-		else if (t > tr) *res = vadd(P, vmul(D, tr));
-		else *res = vadd(P, vmul(D, t));
-	}
-	return true;
-}
-
-__device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res)
-{
-	if (dirOpt) *res = vmul(opt, radius);
-	else if (vsq(opt) > radius * radius) *res = vmul(vnorm(opt), radius);
-	else *res = opt;
-	for (int i = 0; i < n; ++i) {
-		const float4 li = L[i];
-		if (det2(lp_dir(li), vsub(lp_point(li), *res)) > 0.0f) {
-			const float2 tmp = *res;
-			if (!lp1(L, i, radius, opt, dirOpt, res)) { *res = tmp; return i; }
-		}
-	}
-	return n;
-}
-
-__device__ void lp3(const float4* L, int n, int begin, float radius, float2* res, float4* proj, int lane)
-{
-	float distance = 0.0f;
-	for (int i = begin; i < n; ++i) {
-		const float4 li = L[i];
-		const float2 Pi = lp_point(li), Di = lp_dir(li);
-		if (det2(Di, vsub(Pi, *res)) > distance) {
-			// projected lines, built lane-parallel and compacted in order
-			int np = 0;
-			for (int base = 0; base < i; base += 32) {
-				const int j = base + lane;
-				bool keep = false;
-				float4 out = make_float4(0, 0, 0, 0);
-				if (j < i) {
-					const float4 lj = L[j];
-					const float2 Pj = lp_point(lj), Dj = lp_dir(lj);
-					const float determinant = det2(Di, Dj);
-					float2 pt;
-					keep = true;
-					if (fabsf(determinant) <= 0.00001f) {
-						if (vdot(Di, Dj) > 0.0f) keep = false;
-						else pt = vmul(vadd(Pi, Pj), 0.5f);
-					} else {
-						pt = vadd(Pi, vmul(Di, det2(Dj, vsub(Pi, Pj)) / determinant));
-					}
-					if (keep) {
-						const float2 d = vnorm(vsub(Dj, Di));
-						out = make_float4(pt.x, pt.y, d.x, d.y);
-					}
-				}
-				const unsigned m = __ballot_sync(0xffffffffu, keep);
-				if (keep) proj[np + __popc(m & ((1u << lane) - 1u))] = out;
-				np += __popc(m);
-			}
-			__syncwarp();
-			const float2 tmp = *res;
-			if (lp2(proj, np, radius, V(-Di.y, Di.x), true, res) < np) *res = tmp;
-			distance = det2(Di, vsub(Pi, *res));
-			__syncwarp();
-		}
-	}
 }
 
 // Solver::createAgentOrcaLines + solveOrcaProgram: ORCASolver.cpp:61-171
