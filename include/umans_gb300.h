@@ -128,6 +128,32 @@ int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_m
  * values and reports the size of the exception table.  Errors are reported
  * through umans_last_error(NULL). */
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions);
+/* ORCA velocities without allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate GPU memory at the moment they need a
+ * result, for instance an application that hands all device memory out
+ * through its own pool at start-up and forbids cudaMalloc afterwards, or code
+ * running while another component owns the device allocator.  Computes, for n
+ * agents of an infinite world whose data the caller keeps on the device, the
+ * new velocity of the ORCA policy with the global method
+ * (Policy::ComputeNewVelocity with ORCA::GetGlobalMinimum), writing new_vel.
+ * It calls no cudaMalloc/cudaFree and no allocating routine: the ORCA line
+ * buffers are a file-scope device array of 1 MiB.
+ *
+ * Device pointers: pos, vel, pref, new_vel are float2[n]; radius, max_speed,
+ * max_accel are float[n]; nbr_index / nbr_dist2 are [n * nbr_cap] (neighbour
+ * list index into the same arrays, and PhantomAgent distSqr), nbr_count[n].
+ * Limit: nbr_cap <= 128 (lines per agent); larger is rejected with
+ * UMANS_ERR_ARGUMENT, and a count above nbr_cap returns UMANS_ERR_DEVICE.
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised.  Waits for `stream` (a
+ * cudaStream_t, may be null).  Errors: umans_last_error(NULL). */
+int umans_orca_velocities_noalloc(int n, const float* pos, const float* vel, const float* pref,
+                                  const float* radius, const float* max_speed, const float* max_accel,
+                                  const int* nbr_index, const float* nbr_dist2, const int* nbr_count,
+                                  int nbr_cap, float range, float time_horizon, float dt,
+                                  float relaxation_time, float* new_vel, void* stream);
 /* the last error of this handle, or of the last failed umans_create when sim is null */
 const char* umans_last_error(umans_sim* sim);
 

@@ -60,6 +60,8 @@ _SIGS = {
     "umans_profile_totals": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int)]),
     "umans_debug_ref_expf": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_size_t)]),
+    "umans_orca_velocities_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, C.c_float,
+                                                C.c_float, C.c_float, C.c_float, P, P]),
     "umans_last_error": (C.c_char_p, [P]),
 }
 

@@ -18,11 +18,20 @@ struct umans_sim {
 };
 
 static thread_local std::string g_create_error;
+static thread_local bool g_last_error_noalloc = false;
+
+namespace umans {
+int orca_velocities_noalloc(int n, const float* pos, const float* vel, const float* pref, const float* radius,
+                            const float* max_speed, const float* max_accel, const int* nbr_index,
+                            const float* nbr_dist2, const int* nbr_count, int nbr_cap, float range,
+                            float time_horizon, float dt, float relaxation_time, float* new_vel, void* stream);
+const char* noalloc_last_error();
+}
 
 static int fail(umans_sim* s, int code, const std::string& msg)
 {
 	if (s) s->err = msg;
-	else g_create_error = msg;
+	else { g_create_error = msg; g_last_error_noalloc = false; }
 	return code;
 }
 
@@ -227,9 +236,23 @@ int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 	return UMANS_OK;
 }
 
+int umans_orca_velocities_noalloc(int n, const float* pos, const float* vel, const float* pref, const float* radius,
+                                  const float* max_speed, const float* max_accel, const int* nbr_index,
+                                  const float* nbr_dist2, const int* nbr_count, int nbr_cap, float range,
+                                  float time_horizon, float dt, float relaxation_time, float* new_vel, void* stream)
+{
+	// no std::string here: this path must not allocate
+	const int rc = umans::orca_velocities_noalloc(n, pos, vel, pref, radius, max_speed, max_accel, nbr_index,
+	                                              nbr_dist2, nbr_count, nbr_cap, range, time_horizon, dt,
+	                                              relaxation_time, new_vel, stream);
+	if (rc != 0) g_last_error_noalloc = true;
+	return rc;
+}
+
 const char* umans_last_error(umans_sim* s)
 {
-	return s ? s->err.c_str() : g_create_error.c_str();
+	if (s) return s->err.c_str();
+	return g_last_error_noalloc ? umans::noalloc_last_error() : g_create_error.c_str();
 }
 
 // ---------------------------------------------------------------------------

@@ -13,7 +13,7 @@ __device__ __forceinline__ float det2(float2 a, float2 b) { return a.x * b.y - a
 __device__ __forceinline__ float2 lp_point(float4 l) { return V(l.x, l.y); }
 __device__ __forceinline__ float2 lp_dir(float4 l) { return V(l.z, l.w); }
 
-__device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res)
+static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res)
 {
 	const float4 ln = L[lineNo];
 	const float2 P = lp_point(ln), D = lp_dir(ln);
@@ -47,7 +47,7 @@ __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool 
 	return true;
 }
 
-__device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res)
+static __device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res)
 {
 	if (dirOpt) *res = vmul(opt, radius);
 	else if (vsq(opt) > radius * radius) *res = vmul(vnorm(opt), radius);
@@ -62,7 +62,7 @@ __device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt
 	return n;
 }
 
-__device__ void lp3(const float4* L, int n, int begin, float radius, float2* res, float4* proj, int lane)
+static __device__ void lp3(const float4* L, int n, int begin, float radius, float2* res, float4* proj, int lane)
 {
 	float distance = 0.0f;
 	for (int i = begin; i < n; ++i) {
