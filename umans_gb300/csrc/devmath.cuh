@@ -123,8 +123,29 @@ UD bool line_intersection(float2 a, float2 b, float2 c, float2 d, float2* res)
 }
 
 // (float)((double)x * (double)x - (double)y * (double)y): pow(x,2) - pow(y,2)
+// of floats (SocialForcesAvoidance.cpp:86).  x^2 and y^2 are exact in double;
+// the difference D is formed exactly as a float expansion (FMA products and
+// TwoSum) and rounded to float.  That equals the double-then-float rounding
+// unless D lies within 2^-10 half-ulp of a float rounding boundary or the
+// subtraction cancels badly; those rare cases take the FP64 path.
 UD float sq_diff_d(float x, float y)
 {
+	const float sh = x * x, sl = fmaf(x, x, -sh);
+	const float th = y * y, tl = fmaf(y, y, -th);
+	const float ah = sh - th;
+	const float bb = ah - sh;
+	const float al = (sh - (ah - bb)) + (-th - bb);
+	const float lo = (sl - tl) + al;
+	const float aah = fabsf(ah);
+	if (aah > 0.0f && fabsf(lo) <= 0x1p-20f * aah && fmaxf(sh, th) <= 1024.0f * aah) {
+		const float rh = ah + lo;
+		const float rl = lo - (rh - ah);
+		const uint32_t e = __float_as_uint(rh) & 0x7f800000u;
+		if (e > (25u << 23) && e < (254u << 23)) {
+			const float half_ulp = __uint_as_float(e - (24u << 23));
+			if (fabsf(rl) < half_ulp * 0.9990234375f) return rh;
+		}
+	}
 	return (float)__dsub_rn(__dmul_rn((double)x, (double)x), __dmul_rn((double)y, (double)y));
 }
 

@@ -261,9 +261,10 @@ __global__ void k_scatter(DevState S)
 // neighbour query (warp-cooperative)
 // ------------------------------------------------------------------------
 struct WarpLists {
-	uint32_t* ref;
-	float* key;
-	int* nid;
+	uint32_t* ref;   // (displacement group << 28) | cell-sorted index
+	float* key;      // sort key, then PhantomAgent::distSqr
+	int* nid;        // neighbour id (tie-break); reused for per-neighbour x terms
+	float* aux;      // per-neighbour y terms
 };
 
 __device__ __forceinline__ bool nb_less(const WarpLists& L, int a, int b)
@@ -286,19 +287,22 @@ __device__ __forceinline__ void nb_cmpswap(const WarpLists& L, int lo, int hi)
 __device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
 {
 	if (len <= 1) return;
-	int P = 1;
-	while (P < len) P <<= 1;
-	for (int size = 2; size <= P; size <<= 1) {
-		const int half = size >> 1;
-		for (int k = lane; k < (P >> 1); k += 32) {
-			const int blk = k / half, pos = k % half;
-			const int lo = blk * size + pos, hi = blk * size + size - 1 - pos;
+	int lp = 0;
+	while ((1 << lp) < len) ++lp;
+	const int halfP = 1 << (lp - 1);   // pairs per stage
+	for (int ls = 1; ls <= lp; ++ls) {
+		// first step of block size 2^ls: i against its mirror in the block
+		const int lh = ls - 1;
+		for (int k = lane; k < halfP; k += 32) {
+			const int blk = k >> lh, pos = k & ((1 << lh) - 1);
+			const int lo = (blk << ls) + pos, hi = (blk << ls) + (1 << ls) - 1 - pos;
 			if (hi < len) nb_cmpswap(L, s + lo, s + hi);
 		}
 		__syncwarp();
-		for (int j = half >> 1; j > 0; j >>= 1) {
-			for (int k = lane; k < (P >> 1); k += 32) {
-				const int lo = (k / j) * 2 * j + (k % j), hi = lo + j;
+		// half-cleaners with distance 2^lj
+		for (int lj = lh - 1; lj >= 0; --lj) {
+			for (int k = lane; k < halfP; k += 32) {
+				const int lo = ((k >> lj) << (lj + 1)) | (k & ((1 << lj) - 1)), hi = lo + (1 << lj);
 				if (hi < len) nb_cmpswap(L, s + lo, s + hi);
 			}
 			__syncwarp();
@@ -374,10 +378,12 @@ __device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L
 		if (g > 0) {
 			if (S.world != W_TORIC) break;
 			bool active;
-			if (g == 1) { active = (double)(p.x - r) < -0.5 * (double)W; disp = V(W, 0); }
-			else if (g == 2) { active = (double)(p.x + r) > 0.5 * (double)W; disp = V(-W, 0); }
-			else if (g == 3) { active = (double)(p.y - r) < -0.5 * (double)H; disp = V(0, H); }
-			else { active = (double)(p.y + r) > 0.5 * (double)H; disp = V(0, -H); }
+			// worldToric.cpp:64-76 compares the float p.x - r with the double
+			// -0.5*W; -0.5f*W is that value exactly, so the float compare agrees
+			if (g == 1) { active = (p.x - r) < -0.5f * W; disp = V(W, 0); }
+			else if (g == 2) { active = (p.x + r) > 0.5f * W; disp = V(-W, 0); }
+			else if (g == 3) { active = (p.y - r) < -0.5f * H; disp = V(0, H); }
+			else { active = (p.y + r) > 0.5f * H; disp = V(0, -H); }
 			if (!active) continue;
 		}
 		const float2 q = vadd(p, disp);
@@ -386,19 +392,44 @@ __device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L
 		const int cx1 = cell_coord((q.x + r - G.x0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.nx);
 		const int cy0 = cell_coord((q.y - r - G.y0) * G.inv_cs - 0.01f, 0.0f, 1.0f, G.ny);
 		const int cy1 = cell_coord((q.y + r - G.y0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.ny);
-		for (int cy = cy0; cy <= cy1; ++cy) {
-			const int s0 = S.start[cy * G.nx + cx0];
-			const int e0 = S.start[cy * G.nx + cx1 + 1];
-			for (int base = s0; base < e0; base += 32) {
-				const int tt = base + lane;
+		// rows of cells covering the query square, ROWS at a time: lane k loads
+		// the contiguous sorted range of row k, the rows are concatenated and
+		// scanned in full 32-lane chunks
+		constexpr int ROWS = 8;
+		for (int ry = cy0; ry <= cy1; ry += ROWS) {
+			const int nr = min(ROWS, cy1 - ry + 1);
+			int rs = 0, len = 0;
+			if (lane < nr) {
+				const int c0 = (ry + lane) * G.nx;
+				rs = S.start[c0 + cx0];
+				len = S.start[c0 + cx1 + 1] - rs;
+			}
+			int incl = len;
+			for (int o = 1; o < ROWS; o <<= 1) {
+				const int v = __shfl_up_sync(0xffffffffu, incl, o);
+				if (lane >= o) incl += v;
+			}
+			int rbeg[ROWS], rst[ROWS];
+#pragma unroll
+			for (int k = 0; k < ROWS; ++k) {
+				rst[k] = __shfl_sync(0xffffffffu, rs, k);
+				rbeg[k] = __shfl_sync(0xffffffffu, incl - len, k);
+			}
+			const int total = __shfl_sync(0xffffffffu, incl, ROWS - 1);
+			for (int base = 0; base < total; base += 32) {
+				const int c = base + lane;
+				int tt = -1;
+#pragma unroll
+				for (int k = 0; k < ROWS; ++k)
+					if (k < nr && c >= rbeg[k]) tt = rst[k] + (c - rbeg[k]);
 				bool ok = false;
 				float d2f = 0;
-				if (tt < e0 && tt != t) {
-					const float2 c = S.sP[tt];
-					const float dx = q.x - c.x, dy = q.y - c.y;
+				if (c < total && tt != t) {
+					const float2 cp = S.sP[tt];
+					const float dx = q.x - cp.x, dy = q.y - cp.y;
 					d2f = dx * dx + dy * dy;
 					if (d2f < r2lo) ok = true;
-					else if (d2f <= r2hi) ok = exact_key(q, c) < r2d;
+					else if (d2f <= r2hi) ok = exact_key(q, cp) < r2d;
 				}
 				const unsigned m = __ballot_sync(0xffffffffu, ok);
 				if (ok) {
@@ -448,30 +479,42 @@ __device__ __forceinline__ float2 ordered_accumulate(float2 acc, float2 f, bool 
 }
 
 // ObjectInteractionForces::ComputeForce: ObjectInteractionForces.cpp:26-48
-// (agents only; obstacles add (0,0)); GoalReachingForce.cpp:26-29
-__device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane)
+// (agents only; obstacles add (0,0)); GoalReachingForce.cpp:26-29.
+// Lanes evaluate one neighbour each into shared memory; lane 0 then adds the
+// x terms and lane 1 the y terms in neighbour order, as the reference's
+// sequential Vector2D sum does.
+__device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane, float* fx, float* fy)
 {
 	if (c.kind == K_GOALREACHING) return vdiv(vsub(A.pref, A.vel), fmaxr(A.relax, A.dt));
 	const float rs = c.range * c.range;
-	float2 F = V(0, 0);
-	for (int base = 0; base < N.K; base += 32) {
-		const int k = base + lane;
-		const bool in = k < N.K && N.d2[k] <= rs;
+	for (int k = lane; k < N.K; k += 32) {
 		float2 f = V(0, 0);
-		if (in) {
+		if (N.d2[k] <= rs) {
 			const float2 np = nb_pos(N, k), nv = nb_vel(N, k);
 			if (c.kind == K_SOCIALFORCES) f = sf_force(A, c, np, nv, nb_pref(N, k), nb_radius(N, k));
 			else f = pl_force(A, c, np, nv, nb_radius(N, k));
 		}
-		F = ordered_accumulate(F, f, in);
+		fx[k] = f.x;
+		fy[k] = f.y;
 	}
-	return vadd(F, V(0, 0));
+	__syncwarp();
+	float acc = 0.0f;
+	if (lane < 2) {
+		const float* src = lane ? fy : fx;
+		for (int k = 0; k < N.K; ++k)
+			if (N.d2[k] <= rs) acc += src[k];
+	}
+	const float ax = __shfl_sync(0xffffffffu, acc, 0);
+	const float ay = __shfl_sync(0xffffffffu, acc, 1);
+	__syncwarp();
+	return vadd(V(ax, ay), V(0, 0));
 }
 
 // ForceBasedFunction::ComputeTargetVelocity: ForceBasedFunction.cpp:48-52
-__device__ __forceinline__ float2 target_velocity(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane)
+__device__ __forceinline__ float2 target_velocity(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane,
+                                                  float* fx, float* fy)
 {
-	return vadd(A.vel, vmul(vdiv(compute_force(A, N, c, lane), c.p[5]), A.dt));
+	return vadd(A.vel, vmul(vdiv(compute_force(A, N, c, lane, fx, fy), c.p[5]), A.dt));
 }
 
 __device__ __forceinline__ bool is_force_based(int kind)
@@ -735,15 +778,23 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 // ------------------------------------------------------------------------
 // the fused per-agent step
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
+// MODE 0: any policy.  MODE 1: every policy uses the gradient method with
+// force-based costs only (SocialForcesAvoidance, PowerLaw,
+// GoalReachingForce); the sampling, ORCA and finite-difference code is
+// compiled out, which lowers register use and raises occupancy.
+template <int MODE>
+__global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
 {
 	extern __shared__ unsigned char smem[];
 	const int lane = threadIdx.x & 31;
 	const int wib = threadIdx.x >> 5;
 	const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
 	const int maxnb = S.maxnb;
-	uint32_t* base = reinterpret_cast<uint32_t*>(smem) + (size_t)wib * 3 * maxnb;
-	WarpLists L{ base, reinterpret_cast<float*>(base + maxnb), reinterpret_cast<int*>(base + 2 * maxnb) };
+	uint32_t* base = reinterpret_cast<uint32_t*>(smem) + (size_t)wib * 4 * maxnb;
+	WarpLists L{ base, reinterpret_cast<float*>(base + maxnb), reinterpret_cast<int*>(base + 2 * maxnb),
+	             reinterpret_cast<float*>(base + 3 * maxnb) };
+	float* fx = reinterpret_cast<float*>(L.nid);   // per-neighbour terms (ids no longer needed)
+	float* fy = L.aux;
 	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
 	float4* proj = lines + maxnb;
 	const GridParams G = *S.grid;
@@ -797,13 +848,24 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 		float2 nv = V(0, 0);
 		uint32_t rng_next = 0;
 		bool rng_used = false;
-		if (!viszero(A.pref)) {
+		if (MODE == 1 && !viszero(A.pref)) {
+			// Policy::getAccelerationFromGradient (policy.cpp:78-89) with
+			// ForceBasedFunction::GetGradient (ForceBasedFunction.cpp:32-36)
+			float2 T = V(0, 0);
+			for (int ci = 0; ci < pol.ncost; ++ci) {
+				const CostDesc& c = pol.cost[ci];
+				const float2 target = target_velocity(A, N, c, lane, fx, fy);
+				T = vadd(T, vmul(vdiv(vsub(A.vel, target), A.dt), c.coeff));
+			}
+			const float2 acc = vclamp(vmul(T, -1), A.maxacc);
+			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
+		} else if (MODE == 0 && !viszero(A.pref)) {
 			CostPrep P;
 			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
 			for (int ci = 0; ci < pol.ncost; ++ci) {
 				const CostDesc& c = pol.cost[ci];
-				if (is_force_based(c.kind)) P.target[ci] = target_velocity(A, N, c, lane);
-				else if (c.kind == K_KARAMOUZAS) {
+				if (is_force_based(c.kind)) P.target[ci] = target_velocity(A, N, c, lane, fx, fy);
+				else if (MODE == 0 && c.kind == K_KARAMOUZAS) {
 					// TTC at the preferred velocity: a min, so lanes split the neighbours
 					float m = MAXF;
 					const float md2 = c.range * c.range;
@@ -820,7 +882,7 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 					P.ttcp[ci] = m;
 					P.maxdev[ci] = karamouzas_maxdev(m);
 					P.cosdev[ci] = cosf(P.maxdev[ci]);
-				} else if (c.kind == K_ORCA) {
+				} else if (MODE == 0 && c.kind == K_ORCA) {
 					P.orca_v = orca_solve(A, N, c, lines, proj, &P.nlines, lane);
 				}
 			}
@@ -831,7 +893,7 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 				for (int ci = 0; ci < pol.ncost; ++ci) {
 					const CostDesc& c = pol.cost[ci];
 					float2 g;
-					if (is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
+					if (MODE == 1 || is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
 					else if (c.kind == K_TTCADCA) g = grad_ttcadca(A, N, c, A.vel);
 					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel);
 					else {
@@ -852,7 +914,7 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 					T = vadd(T, vmul(g, c.coeff));
 				}
 				acc = vmul(T, -1);
-			} else {
+			} else if (MODE == 0) {
 				float2 best;
 				const CostDesc& c0 = pol.cost[0];
 				if (pol.method == M_GLOBAL && pol.ncost == 1 && c0.kind == K_ORCA) best = P.orca_v;
@@ -866,6 +928,8 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 					}
 				}
 				acc = vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt));
+			} else {
+				acc = V(0, 0);
 			}
 			acc = vclamp(acc, A.maxacc);
 			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
@@ -876,7 +940,8 @@ __global__ void __launch_bounds__(128) k_agent(DevState S, int dump)
 			const float2 af = vdiv(contact, 80.0f);
 			const float2 vel = vadd(nv, vmul(af, A.dt));
 			const float2 vd = vdiv(vadd(vmul(vel, 2), A.pref), 3);
-			if ((double)vsq(vd) > 0.01) S.view[slot] = vnorm(vd);
+			// (double)|vd|^2 > 0.01 <=> |vd|^2 > 0.01f (0.01f is the float just below 0.01)
+			if (vsq(vd) > 0.01f) S.view[slot] = vnorm(vd);
 			float2 p = vadd(A.pos, vmul(vel, A.dt));
 			if (S.world == W_TORIC) {   // worldToric.cpp:81-108
 				const float hw = 0.5f * S.width, hh = 0.5f * S.height;
@@ -1213,7 +1278,7 @@ bool Engine::choose_maxnb()
 {
 	int want = opt_.max_neighbours;
 	if (want <= 0) {
-		const int probe = 4096;
+		const int probe = 3072;
 		std::vector<int> cnt(std::max(n_, 1));
 		int saved = maxnb_;
 		maxnb_ = probe;
@@ -1239,10 +1304,11 @@ void Engine::invalidate_graph()
 	graph_valid_ = false;
 }
 
-static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem)
+static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int mode = 0)
 {
 	int per_sm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent, warps_per_block * 32, smem);
+	if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1>, warps_per_block * 32, smem);
+	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<0>, warps_per_block * 32, smem);
 	if (per_sm < 1) per_sm = 1;
 	return num_sms * per_sm;
 }
@@ -1253,9 +1319,19 @@ bool Engine::configure()
 {
 	DevState& S = *d_;
 	const int wpb = opt_.warps_per_block;
-	const size_t smem = (size_t)wpb * maxnb_ * 12;
-	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	agent_blocks_ = agent_blocks_for(num_sms_, wpb, smem);
+	const size_t smem = (size_t)wpb * maxnb_ * 16;
+	if (smem > 48 * 1024) {
+		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	}
+	mode_ = 1;
+	for (const auto& p : sc_.policies) {
+		if (p.method != M_GRADIENT) mode_ = 0;
+		for (int c = 0; c < p.ncost; ++c)
+			if (!(p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_GOALREACHING))
+				mode_ = 0;
+	}
+	agent_blocks_ = agent_blocks_for(num_sms_, wpb, smem, mode_);
 	S.total_warps = agent_blocks_ * wpb;
 	if (!dalloc(S.scratch, (size_t)S.total_warps * 2 * maxnb_, err_)) return false;
 	configured_maxnb_ = maxnb_;
@@ -1269,7 +1345,7 @@ void Engine::enqueue_step()
 	S.n = n_;
 	S.maxnb = maxnb_;
 	const int wpb = opt_.warps_per_block;
-	const size_t smem = (size_t)wpb * maxnb_ * 12;
+	const size_t smem = (size_t)wpb * maxnb_ * 16;
 	const int threads = 256;
 	const int nb = std::max(1, (n_ + threads - 1) / threads);
 	if (S.world != W_TORIC) k_bbox<<<std::min(nb, 2 * num_sms_), threads, 0, stream_>>>(S);
@@ -1281,7 +1357,8 @@ void Engine::enqueue_step()
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
-	k_agent<<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	if (mode_ == 1) k_agent<1><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	else k_agent<0><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
 
@@ -1540,11 +1617,11 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	// same grid build and gather as a step, no state update
 	DevState T = S;
 	T.n = n_;
-	const int dump_nb = std::max(maxnb_, 4096);
+	const int dump_nb = std::max(maxnb_, 3072);   // 4 warps x 3072 x 16 B = 192 KB shared
 	T.maxnb = dump_nb;
 	const int wpb = opt_.warps_per_block;
-	const size_t smem = (size_t)wpb * dump_nb * 12;
-	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const size_t smem = (size_t)wpb * dump_nb * 16;
+	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int blocks = agent_blocks_for(num_sms_, wpb, smem);
 	T.total_warps = blocks * wpb;
 	float4* scr = nullptr;
@@ -1559,7 +1636,7 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	k_scan_top<<<1, 1024, 0, stream_>>>(T);
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
 	k_scatter<<<nb, threads, 0, stream_>>>(T);
-	k_agent<<<blocks, wpb * 32, smem, stream_>>>(T, 1);
+	k_agent<0><<<blocks, wpb * 32, smem, stream_>>>(T, 1);
 	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(stream_));
 	cudaFree(scr);

@@ -97,7 +97,7 @@ private:
 	int n_ = 0, cap_ = 0;
 	double time_ = 0;
 	int maxnb_ = 0, configured_maxnb_ = -1;
-	int num_sms_ = 0, agent_blocks_ = 0;
+	int num_sms_ = 0, agent_blocks_ = 0, mode_ = 0;
 	int next_unused_id_ = 0;
 	bool any_remove_at_goal_ = false;
 	float agent_ms_ = 0;

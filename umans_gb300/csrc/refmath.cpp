@@ -30,6 +30,7 @@ struct HostTable {
 	uint32_t mask = 0;
 	int shift = 32;
 	size_t count = 0;
+	int fast = 0;
 };
 
 std::mutex g_mutex;
@@ -139,6 +140,15 @@ HostTable* build_host_table()
 		T->slots[h] = e;
 	}
 	T->count = exc.size();
+	// the device may skip the table lookup away from rounding midpoints only
+	// if every exception is a near-midpoint argument
+	bool all_near = true;
+	for (const uint2& e : exc) {
+		bool near = false;
+		ff_expf_core(bitsf(e.x), &near);
+		all_near = all_near && near;
+	}
+	T->fast = all_near ? 1 : 0;
 	return T;
 }
 
@@ -172,6 +182,7 @@ bool exp_exceptions_for_device(ExpExceptions* out, size_t* count, std::string& e
 	out->slots = it->second;
 	out->mask = g_host->mask;
 	out->shift = g_host->shift;
+	out->fast = g_host->fast;
 	if (count) *count = g_host->count;
 	return true;
 }

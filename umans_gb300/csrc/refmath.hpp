@@ -56,14 +56,37 @@ RM_HD void ff_split(float a, float* hi, float* lo)   // Veltkamp, 12 + 12 bits
 	*hi = h;
 	*lo = a - h;
 }
-RM_HD FF ff_two_prod(float a, float b)   // Dekker: exact product without FMA
+// exact product a*b = p + e (no overflow or underflow in the uses below):
+// an FMA on the GPU, Dekker's product on the host; both give the same exact e
+RM_HD FF ff_two_prod(float a, float b)
 {
 	const float p = a * b;
+#if defined(__CUDA_ARCH__)
+	return FF{ p, fmaf(a, b, -p) };
+#else
 	float ah, al, bh, bl;
 	ff_split(a, &ah, &al);
 	ff_split(b, &bh, &bl);
 	const float e = ((ah * bh - p) + ah * bl + al * bh) + al * bl;
 	return FF{ p, e };
+#endif
+}
+
+RM_HD uint32_t rm_bits(float f)
+{
+#if defined(__CUDA_ARCH__)
+	return __float_as_uint(f);
+#else
+	union { float f; uint32_t u; } c; c.f = f; return c.u;
+#endif
+}
+RM_HD float rm_float(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+	return __uint_as_float(u);
+#else
+	union { uint32_t u; float f; } c; c.u = u; return c.f;
+#endif
 }
 
 // 2^(j/64) = hi + lo (hi + lo within 2^-48 of the exact value); one copy
@@ -214,8 +237,11 @@ RM_HD float ff_exp2_tab(int j, int w)
 
 constexpr float FF_EXP_LO = -87.0f;
 
-// e^x for x in [FF_EXP_LO, 0]; the caller checks the range.
-RM_HD float ff_expf_core(float x)
+// e^x for x in [FF_EXP_LO, 0]; the caller checks the range.  *near is set
+// when the unrounded value lies within 1/256 ulp of a rounding midpoint (the
+// only place where the host library's expf, accurate to 0.502 ulp, and this
+// function can disagree; the host verifies that against its full table).
+RM_HD float ff_expf_core(float x, bool* near = nullptr)
 {
 	const float INV = 92.33248138427734f;      // 64 / ln 2
 	const float L1 = 0x1.62cp-7f;              // ln2/64 = L1 + L2 + L3, L1 with 11 bits
@@ -243,10 +269,13 @@ RM_HD float ff_expf_core(float x)
 	const FF m = ff_two_prod(Th, s.h);
 	const float ml = m.l + (Th * sl + Tl * s.h);
 	const float f = m.h + ml;
+	if (near) {
+		const float rl = ml - (f - m.h);
+		const float half_ulp = rm_float((rm_bits(f) & 0x7f800000u) - (24u << 23));
+		*near = !(fabsf(rl) < half_ulp * 0.99609375f);
+	}
 	// 2^kq, kq in [-126, 0]: normal, so the scaling is exact
-	union { uint32_t u; float f; } sc;
-	sc.u = (uint32_t)(kq + 127) << 23;
-	return f * sc.f;
+	return f * rm_float((uint32_t)(kq + 127) << 23);
 }
 
 // open-addressing table of (argument bits, host expf bits); key 0 = empty
@@ -254,6 +283,7 @@ struct ExpExceptions {
 	const uint2* slots;
 	uint32_t mask;    // size - 1 (size a power of two)
 	int shift;        // 32 - log2(size)
+	int fast;         // 1 when every table entry is a near-midpoint argument
 };
 
 RM_HD uint32_t ff_hash(uint32_t bits, int shift) { return (bits * 0x9E3779B1u) >> shift; }
@@ -263,7 +293,9 @@ RM_HD uint32_t ff_hash(uint32_t bits, int shift) { return (bits * 0x9E3779B1u) >
 __device__ __forceinline__ float ref_expf(const ExpExceptions& T, float x)
 {
 	if (!(x >= FF_EXP_LO && x <= 0.0f)) return (float)exp((double)x);
-	const float y = ff_expf_core(x);
+	bool near;
+	const float y = ff_expf_core(x, &near);
+	if (T.fast && !near) return y;
 	const uint32_t b = __float_as_uint(x);
 	uint32_t h = ff_hash(b, T.shift);
 	for (;;) {
