@@ -125,3 +125,16 @@ def test_full_size_properties(tmp_path):
     assert np.array_equal(pa, pb)
     assert np.isfinite(pa).all()
     assert np.abs(pa).max() <= 200.0 + 1e-3   # toric wrap keeps agents in the box
+
+
+def test_capacity_overflow_reruns_batch_exactly(tmp_path):
+    """A neighbour capacity far below the list lengths: every overflowing
+    batch is restored from its snapshot and re-run with a doubled capacity,
+    so the trajectory still equals the oracle's."""
+    path = S.socialforces_toric(n=3000, density=0.625).write(str(tmp_path / "dense.xml"))
+    sim = Simulation(path, max_neighbours=8)
+    port = PortSim(path, threads=THREADS)
+    sim.step(15)
+    port.step(15)
+    assert sim.max_neighbours > 8
+    assert np.array_equal(sim.positions(), port.state()["pos"])

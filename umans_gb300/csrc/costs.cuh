@@ -22,6 +22,7 @@ struct NbView {
 	const float2* sP;        // cell-sorted positions
 	const float2* sV;        // cell-sorted velocities
 	const float4* sB;        // cell-sorted (pref.x, pref.y, radius, -)
+	const float4* sE;        // cell-sorted (normalised pref.x, pref.y, speed, -)
 	float2 off[5];           // PhantomAgent offsets per displacement group
 };
 
@@ -32,6 +33,7 @@ UD float2 nb_pos(const NbView& N, int k)
 }
 UD float2 nb_vel(const NbView& N, int k) { return N.sV[N.ref[k] & 0x0FFFFFFFu]; }
 UD float nb_radius(const NbView& N, int k) { return N.sB[N.ref[k] & 0x0FFFFFFFu].z; }
+UD float4 nb_E(const NbView& N, int k) { return N.sE[N.ref[k] & 0x0FFFFFFFu]; }
 UD float2 nb_pref(const NbView& N, int k)
 {
 	const float4 b = N.sB[N.ref[k] & 0x0FFFFFFFu];
@@ -60,14 +62,16 @@ UD float ttc_first(const AgentCtx& A, const NbView& N, float2 vel, float maxDist
 }
 
 // SocialForcesAvoidance::ComputeAgentInteractionForce: SocialForcesAvoidance.cpp:26-110
-UD float2 sf_force(const AgentCtx& A, const CostDesc& c, float2 np, float2 nv, float2 npref, float nr)
+// E = (Eb.x, Eb.y, vb): the neighbour's normalised preferred velocity and
+// its speed (SocialForcesAvoidance.cpp:58-59), precomputed once per agent
+UD float2 sf_force(const AgentCtx& A, const CostDesc& c, float2 np, float4 E, float nr)
 {
 	const float dtp = c.p[0], V0 = c.p[1], sigma = c.p[2];
 	const float2 R = vsub(A.pos, np);
 	const float magR = vmag(R);
 	if (magR <= A.radius + nr) return V(0, 0);
-	const float vb = vmag(nv);
-	const float2 Eb = vnorm(npref);
+	const float vb = E.z;
+	const float2 Eb = V(E.x, E.y);
 	const float2 Vv = vmul(Eb, vb * dtp);
 	const float magV = vmag(Vv);
 	const float2 R2 = vsub(R, Vv);

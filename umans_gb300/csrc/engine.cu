@@ -46,6 +46,7 @@ struct DevState {
 	uint32_t* rng;
 	float2 *sP, *sV;
 	float4* sB;
+	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces)
 	int *sSlot, *sId;
 	int *cell, *cnt, *start, *fill, *blocksum;
 	GridParams* grid;
@@ -253,6 +254,12 @@ __global__ void k_scatter(DevState S)
 	S.sP[t] = p;
 	S.sV[t] = S.vel[i];
 	S.sB[t] = make_float4(pv.x, pv.y, prm.x, 0.0f);
+	// per-agent terms of SocialForcesAvoidance.cpp:58-59 (vb, Eb), computed once
+	// here instead of once per neighbour pair; the same operations, so the
+	// same values
+	const float2 v = S.vel[i];
+	const float2 eb = vnorm(pv);
+	S.sE[t] = make_float4(eb.x, eb.y, vmag(v), 0.0f);
 	S.sSlot[t] = i;
 	S.sId[t] = S.id[i];
 }
@@ -310,6 +317,71 @@ __device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
 	}
 }
 
+// Sort of [s, s+len), len <= 128, in registers: each lane holds up to 4
+// packed keys (float key bits with the low PB bits replaced by the position
+// in the segment; positive floats order like their bit patterns) and a
+// shuffle bitonic network sorts them; the entries are then permuted.  Keys
+// that agree above the low PB bits may come out in either order: the
+// near-tie pass that follows (relative window 2^-16, wider than the 2^-17
+// truncation)
+// re-orders them with the exact double distance and the id.
+template <int M>
+__device__ __forceinline__ void warp_sort_regs(const WarpLists& L, int s, int len, int lane)
+{
+	constexpr int PB = (M == 1) ? 5 : (M == 2) ? 6 : 7;
+	constexpr uint32_t PMASK = (1u << PB) - 1u;
+	uint32_t u[M];
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * 32 + lane;
+		u[m] = (i < len) ? ((__float_as_uint(L.key[s + i]) & ~PMASK) | (uint32_t)i) : 0xffffffffu;
+	}
+	constexpr int P = 32 * M;
+#pragma unroll
+	for (int size = 2; size <= P; size <<= 1) {
+#pragma unroll
+		for (int j = size >> 1; j > 0; j >>= 1) {
+#pragma unroll
+			for (int m = 0; m < M; ++m) {
+				const int i = m * 32 + lane;
+				const bool up = (i & size) == 0;
+				if (j >= 32) {
+					const int mm = m ^ (j >> 5);
+					if (mm > m) {
+						const uint32_t a = u[m], b = u[mm];
+						const bool swap = up ? (a > b) : (a < b);
+						if (swap) { u[m] = b; u[mm] = a; }
+					}
+				} else {
+					const uint32_t o = __shfl_xor_sync(0xffffffffu, u[m], j);
+					const bool lower = (lane & j) == 0;
+					// keep the min in the lower position of an ascending pair
+					const bool take_min = (lower == up);
+					u[m] = take_min ? min(u[m], o) : max(u[m], o);
+				}
+			}
+		}
+	}
+	uint32_t r[M];
+	float k[M];
+	int d[M];
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * 32 + lane;
+		if (i < len) {
+			const int src = s + (int)(u[m] & PMASK);
+			r[m] = L.ref[src]; k[m] = L.key[src]; d[m] = L.nid[src];
+		}
+	}
+	__syncwarp();
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * 32 + lane;
+		if (i < len) { L.ref[s + i] = r[m]; L.key[s + i] = k[m]; L.nid[s + i] = d[m]; }
+	}
+	__syncwarp();
+}
+
 __device__ __forceinline__ double exact_key(float2 q, float2 c)
 {
 	// nanoflann L2_Simple_Adaptor<double>::evalMetric (nanoflann.hpp:423-446)
@@ -318,38 +390,50 @@ __device__ __forceinline__ double exact_key(float2 q, float2 c)
 	return __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
 }
 
-// Float keys order the list except within runs of near-equal keys, whose
-// order is settled with the reference's double distance (then id).
-__device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane)
+// Float keys order the list except within runs of near-equal keys (relative
+// gap <= win: 1e-6 after the exact-key sort, 2^-16 after the packed-key
+// register sort), whose order is settled with the reference's double
+// distance (then id).  Runs are rare; lane 0 handles them.
+__device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane, float win)
 {
 	bool close = false;
 	for (int k = s + lane; k + 1 < e; k += 32) {
 		const float a = L.key[k], b = L.key[k + 1];
-		if (b - a <= 1e-6f * b) close = true;
+		if (b - a <= win * b) close = true;
 	}
 	if (!__any_sync(0xffffffffu, close)) return;
 	if (lane == 0) {
 		int k = s;
 		while (k + 1 < e) {
 			const float a = L.key[k], b = L.key[k + 1];
-			if (!(b - a <= 1e-6f * b)) { ++k; continue; }
-			int r0 = k;
-			while (k + 1 < e && L.key[k + 1] - L.key[k] <= 1e-6f * L.key[k + 1]) ++k;
+			if (!(b - a <= win * b)) { ++k; continue; }
+			const int r0 = k;
+			while (k + 1 < e && L.key[k + 1] - L.key[k] <= win * L.key[k + 1]) ++k;
 			const int r1 = k;   // inclusive
+			// insertion sort of the run on (exact double key, id); the exact keys
+			// are kept in place of the float keys meanwhile
+			double dk[16];
+			const bool small = r1 - r0 < 16;
+			for (int x = r0; x <= r1; ++x) {
+				const double d = exact_key(q, S.sP[L.ref[x] & 0x0FFFFFFFu]);
+				if (small) dk[x - r0] = d;
+			}
 			for (int x = r0 + 1; x <= r1; ++x) {
 				const uint32_t rx = L.ref[x];
 				const int ix = L.nid[x];
 				const float kx = L.key[x];
-				const double dx = exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
+				const double dx = small ? dk[x - r0] : exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
 				int y = x - 1;
 				while (y >= r0) {
-					const double dy = exact_key(q, S.sP[L.ref[y] & 0x0FFFFFFFu]);
+					const double dy = small ? dk[y - r0] : exact_key(q, S.sP[L.ref[y] & 0x0FFFFFFFu]);
 					if (dy > dx || (dy == dx && L.nid[y] > ix)) {
 						L.ref[y + 1] = L.ref[y]; L.nid[y + 1] = L.nid[y]; L.key[y + 1] = L.key[y];
+						if (small) dk[y + 1 - r0] = dy;
 						--y;
 					} else break;
 				}
 				L.ref[y + 1] = rx; L.nid[y + 1] = ix; L.key[y + 1] = kx;
+				if (small) dk[y + 1 - r0] = dx;
 			}
 			++k;
 		}
@@ -445,8 +529,11 @@ __device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L
 		}
 		if (K > maxnb) { *overflow = true; K = maxnb; }
 		__syncwarp();
-		warp_sort(L, gs, K - gs, lane);
-		fix_near_ties(S, L, gs, K, q, lane);
+		const int len = K - gs;
+		if (len <= 32) warp_sort_regs<1>(L, gs, len, lane);
+		else if (len <= 64) warp_sort_regs<2>(L, gs, len, lane);
+		else warp_sort(L, gs, len, lane);
+		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : 1e-6f);
 	}
 	// PhantomAgent position offset = -displacement; distSqr in float
 	const float2 off[5] = { V(0, 0), V(-W, -0.0f), V(W, -0.0f), V(-0.0f, -H), V(-0.0f, H) };
@@ -491,7 +578,7 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 		float2 f = V(0, 0);
 		if (N.d2[k] <= rs) {
 			const float2 np = nb_pos(N, k), nv = nb_vel(N, k);
-			if (c.kind == K_SOCIALFORCES) f = sf_force(A, c, np, nv, nb_pref(N, k), nb_radius(N, k));
+			if (c.kind == K_SOCIALFORCES) f = sf_force(A, c, np, nb_E(N, k), nb_radius(N, k));
 			else f = pl_force(A, c, np, nv, nb_radius(N, k));
 		}
 		fx[k] = f.x;
@@ -813,7 +900,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 
 		const int K = gather(S, G, L, t, A.pos, pol.range, lane, &overflow);
 		NbView N;
-		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB;
+		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB; N.sE = S.sE;
 		N.off[0] = V(0, 0); N.off[1] = V(-S.width, -0.0f); N.off[2] = V(S.width, -0.0f);
 		N.off[3] = V(-0.0f, -S.height); N.off[4] = V(-0.0f, S.height);
 
@@ -836,9 +923,15 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				bool take = false;
 				float2 f = V(0, 0);
 				if (k < K) {
-					const float2 diff = vsub(A.pos, nb_pos(N, k));
-					const float inter = A.radius + nb_radius(N, k) - vmag(diff);
-					if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
+					// d2[k] is |pos - neighbour|^2 computed exactly as vsq(diff); if it
+					// exceeds (r + r_j)^2 by 1e-5 relative, sqrt(d2) >= r + r_j and the
+					// overlap test below is false
+					const float rsum = A.radius + nb_radius(N, k);
+					if (!(N.d2[k] > rsum * rsum * 1.00001f)) {
+						const float2 diff = vsub(A.pos, nb_pos(N, k));
+						const float inter = rsum - vmag(diff);
+						if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
+					}
 				}
 				contact = ordered_accumulate(contact, f, take);
 			}
@@ -1183,7 +1276,7 @@ bool Engine::alloc(int cap)
 	    !dalloc(S.view, cap, err_) || !dalloc(S.vwf, cap, err_) || !dalloc(S.pref, cap, err_) ||
 	    !dalloc(S.prm, cap, err_) || !dalloc(S.pol, cap, err_) || !dalloc(S.id, cap, err_) ||
 	    !dalloc(S.rng, cap, err_) || !dalloc(S.sP, cap, err_) || !dalloc(S.sV, cap, err_) ||
-	    !dalloc(S.sB, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
+	    !dalloc(S.sB, cap, err_) || !dalloc(S.sE, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
 	    !dalloc(S.cell, cap, err_) || !dalloc(S.cnt, mc + 1, err_) || !dalloc(S.start, mc + 1, err_) ||
 	    !dalloc(S.fill, mc + 1, err_) || !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 2, err_))
 		return false;
@@ -1234,6 +1327,7 @@ bool Engine::upload_all()
 bool Engine::get_agent_data(void* out)
 {
 	DevState& S = *d_;
+	if (!sync()) return false;
 	if (n_ == 0) return true;
 	S.n = n_;
 	k_pack<<<(n_ + 255) / 256, 256, 0, stream_>>>(S);
@@ -1245,6 +1339,7 @@ bool Engine::get_agent_data(void* out)
 bool Engine::set_agent_data(const void* in, int m)
 {
 	DevState& S = *d_;
+	if (!sync()) return false;
 	if (m <= 0) return true;
 	if (m > cap_ && !dalloc(S.io, (size_t)m, err_)) return false;
 	CK(cudaMemcpyAsync(S.io, in, sizeof(AgentRecord) * m, cudaMemcpyHostToDevice, stream_));
@@ -1258,7 +1353,7 @@ bool Engine::set_agent_data(const void* in, int m)
 bool Engine::download_mutable()
 {
 	const DevState& S = *d_;
-	CK(cudaStreamSynchronize(stream_));
+	if (!sync()) return false;
 	pos_.resize(n_); vel_.resize(n_); view_.resize(n_); vwf_.resize(n_); rng_.resize(n_);
 	if (n_ > 0) {
 		CK(cudaMemcpy(pos_.data(), S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
@@ -1271,9 +1366,9 @@ bool Engine::download_mutable()
 }
 
 // The neighbour-list capacity is sized from the initial state: twice the
-// largest list, rounded up to a power of two (at least 64).  A list that
-// later outgrows it sets ST_NEIGHBOUR_OVERFLOW; sync() then reports the
-// error and the capacity doubles for the following steps.
+// largest list, rounded up to a power of two (at least 128).  A list that
+// later outgrows it sets ST_NEIGHBOUR_OVERFLOW; sync() then re-runs the batch
+// from its snapshot with the capacity doubled (up to 3072 entries).
 bool Engine::choose_maxnb()
 {
 	int want = opt_.max_neighbours;
@@ -1285,7 +1380,7 @@ bool Engine::choose_maxnb()
 		if (!neighbours(0, nullptr, nullptr, cnt.data())) { maxnb_ = saved; return false; }
 		int mx = 0;
 		for (int i = 0; i < n_; ++i) mx = std::max(mx, cnt[i]);
-		want = 64;
+		want = 128;
 		while (want < 2 * mx) want <<= 1;
 	}
 	if (want != maxnb_) {
@@ -1433,15 +1528,12 @@ bool Engine::remove_at_goal()
 	return changed ? upload_all() : true;
 }
 
-bool Engine::step(int nsteps)
+// Enqueues n steps (no host work in between).
+bool Engine::run_steps(int nsteps)
 {
-	if (nsteps <= 0) return true;
-	const bool dynamic = !pending_.empty() || any_remove_at_goal_;
-	if (time_kernels) CK(cudaEventRecord(ev0_, stream_));
 	if (configured_maxnb_ != maxnb_ && !configure()) return false;
 	for (int s = 0; s < nsteps; ++s) {
-		if (!pending_.empty() && !apply_pending_agents()) return false;
-		if (opt_.use_graph && !dynamic && !profile_) {
+		if (opt_.use_graph && !profile_) {
 			if (!graph_valid_ && !capture_graph()) return false;
 			CK(cudaGraphLaunch(graph_exec_, stream_));
 		} else {
@@ -1460,7 +1552,70 @@ bool Engine::step(int nsteps)
 			}
 		}
 		time_ += sc_.dt;
-		if (any_remove_at_goal_ && !remove_at_goal()) return false;
+	}
+	return true;
+}
+
+// The mutable per-agent state at the start of a batch of steps, kept so that
+// a batch in which some neighbour list outgrew the capacity can be re-run
+// with a larger capacity (every step is then computed with complete lists).
+bool Engine::take_snapshot()
+{
+	DevState& S = *d_;
+	if (snap_cap_ < n_) {
+		snap_cap_ = std::max(n_, 16);
+		if (!dalloc(snap_pos_, snap_cap_, err_) || !dalloc(snap_vel_, snap_cap_, err_) ||
+		    !dalloc(snap_view_, snap_cap_, err_) || !dalloc(snap_vwf_, snap_cap_, err_) ||
+		    !dalloc(snap_rng_, snap_cap_, err_))
+			return false;
+	}
+	if (n_ > 0) {
+		CK(cudaMemcpyAsync(snap_pos_, S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(snap_vel_, S.vel, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(snap_view_, S.view, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(snap_vwf_, S.vwf, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(snap_rng_, S.rng, sizeof(uint32_t) * n_, cudaMemcpyDeviceToDevice, stream_));
+	}
+	snap_valid_ = true;
+	snap_time_ = time_;
+	snap_steps_ = 0;
+	return true;
+}
+
+bool Engine::restore_snapshot()
+{
+	DevState& S = *d_;
+	if (n_ > 0) {
+		CK(cudaMemcpyAsync(S.pos, snap_pos_, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.vel, snap_vel_, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.view, snap_view_, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.vwf, snap_vwf_, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.rng, snap_rng_, sizeof(uint32_t) * n_, cudaMemcpyDeviceToDevice, stream_));
+	}
+	time_ = snap_time_;
+	return true;
+}
+
+bool Engine::step(int nsteps)
+{
+	if (nsteps <= 0) return true;
+	const bool dynamic = !pending_.empty() || any_remove_at_goal_;
+	if (time_kernels) CK(cudaEventRecord(ev0_, stream_));
+	if (!dynamic) {
+		if (!snap_valid_ && !take_snapshot()) return false;
+		if (!run_steps(nsteps)) return false;
+		snap_steps_ += nsteps;
+	} else {
+		// insertions and removals change the agent list between steps: settle
+		// every step before the host-side changes
+		for (int s = 0; s < nsteps; ++s) {
+			if (!pending_.empty() && !apply_pending_agents()) return false;
+			if (!take_snapshot()) return false;
+			if (!run_steps(1)) return false;
+			snap_steps_ = 1;
+			if (!sync()) return false;
+			if (any_remove_at_goal_ && !remove_at_goal()) return false;
+		}
 	}
 	if (time_kernels) {
 		CK(cudaEventRecord(ev1_, stream_));
@@ -1472,31 +1627,43 @@ bool Engine::step(int nsteps)
 	return true;
 }
 
+// Waits for the enqueued steps.  A neighbour-capacity overflow restores the
+// snapshot taken at the start of the batch, doubles the capacity and re-runs
+// the batch; other device conditions are reported.
 bool Engine::sync()
 {
-	CK(cudaStreamSynchronize(stream_));
-	int st = 0;
-	CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
-	if (st) {
+	for (;;) {
+		CK(cudaStreamSynchronize(stream_));
+		int st = 0;
+		CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
+		if (st == 0) {
+			snap_valid_ = false;
+			return true;
+		}
 		CK(cudaMemset(d_->status, 0, sizeof(int)));
-		if (st & ST_NEIGHBOUR_OVERFLOW) {
-			err_ = "neighbour list longer than the capacity of " + std::to_string(maxnb_) +
-			       "; the capacity has been doubled for the following steps";
-			maxnb_ *= 2;
+		if ((st & ST_NEIGHBOUR_OVERFLOW) && snap_valid_ && maxnb_ < 3072) {
+			const int steps = snap_steps_;
+			if (!restore_snapshot()) return false;
+			maxnb_ = std::min(3072, maxnb_ * 2);
 			invalidate_graph();
+			if (!run_steps(steps)) return false;
+			continue;
+		}
+		snap_valid_ = false;
+		if (st & ST_NEIGHBOUR_OVERFLOW) {
+			err_ = "a neighbour list is longer than " + std::to_string(maxnb_) + " entries";
 			return false;
 		}
 		if (st & ST_GRID_OVERFLOW) { err_ = "non-finite agent positions"; return false; }
 		err_ = "device status " + std::to_string(st);
 		return false;
 	}
-	return true;
 }
 
 bool Engine::get_state(int* ids, float* pos, float* vel, float* view, float* pref, float* goal)
 {
 	const DevState& S = *d_;
-	CK(cudaStreamSynchronize(stream_));
+	if (!sync()) return false;
 	if (n_ == 0) return true;
 	if (ids) std::memcpy(ids, id_.data(), sizeof(int) * n_);
 	if (pos) CK(cudaMemcpy(pos, S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToHost));
@@ -1510,7 +1677,7 @@ bool Engine::get_state(int* ids, float* pos, float* vel, float* view, float* pre
 bool Engine::set_state(const float* pos, const float* vel, const float* view)
 {
 	const DevState& S = *d_;
-	CK(cudaStreamSynchronize(stream_));
+	if (!sync()) return false;
 	if (n_ == 0) return true;
 	if (pos) CK(cudaMemcpy(S.pos, pos, sizeof(float2) * n_, cudaMemcpyHostToDevice));
 	if (vel) {
@@ -1544,7 +1711,7 @@ bool Engine::set_goal(int id, float x, float y)
 	const int i = it->second;
 	const DevState& S = *d_;
 	float2 p;
-	CK(cudaStreamSynchronize(stream_));
+	if (!sync()) return false;
 	CK(cudaMemcpy(&p, S.pos + i, sizeof(float2), cudaMemcpyDeviceToHost));
 	float2 g = make_float2(x, y);
 	goal_[i] = g;
@@ -1607,7 +1774,7 @@ bool Engine::remove_agent(int id)
 bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 {
 	DevState& S = *d_;
-	CK(cudaStreamSynchronize(stream_));
+	if (!sync()) return false;
 	if (n_ == 0) return true;
 	const int dcap = std::max(cap, 1);
 	if (!dalloc(S.dump_ids, (size_t)n_ * dcap, err_) || !dalloc(S.dump_d2, (size_t)n_ * dcap, err_) ||
@@ -1660,9 +1827,10 @@ Engine::~Engine()
 	invalidate_graph();
 	if (d_) {
 		DevState& S = *d_;
-		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB,
+		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,
 		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.fill, S.blocksum, S.grid, S.bbox, S.status,
-		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io };
+		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io,
+		                 snap_pos_, snap_vel_, snap_view_, snap_vwf_, snap_rng_ };
 		for (void* p : ptrs)
 			if (p) cudaFree(p);
 		delete d_;

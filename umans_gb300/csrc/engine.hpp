@@ -84,6 +84,9 @@ private:
 	bool build_tables();
 	bool choose_maxnb();
 	bool configure();
+	bool run_steps(int n);
+	bool take_snapshot();
+	bool restore_snapshot();
 	void enqueue_step();
 	bool capture_graph();
 	void invalidate_graph();
@@ -119,6 +122,12 @@ private:
 	cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
 	cudaEvent_t pa0_ = nullptr, pa1_ = nullptr, ps0_ = nullptr, ps1_ = nullptr;
 	bool profile_ = false;
+	// batch snapshot for re-running a batch after a capacity overflow
+	float2 *snap_pos_ = nullptr, *snap_vel_ = nullptr, *snap_view_ = nullptr, *snap_vwf_ = nullptr;
+	uint32_t* snap_rng_ = nullptr;
+	int snap_cap_ = 0, snap_steps_ = 0;
+	bool snap_valid_ = false;
+	double snap_time_ = 0;
 	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
 	int prof_steps_ = 0;
 };
