@@ -81,6 +81,21 @@ int umans_create(const char* config_file, umans_sim** out);
 int umans_create_ex(const char* config_file, int max_neighbours, float cells_per_range, int use_graph,
                     umans_sim** out);
 int umans_destroy(umans_sim* sim);
+
+/* Batched form (no counterpart in the reference, which runs one scenario per
+ * process): n independent scenarios stepped together, their agents
+ * concatenated in list order, scenario k at slots [offsets[k], offsets[k+1]).
+ * Each scenario is simulated exactly as by umans_create on its own file.
+ * Timed insertion and removal at the goal are not supported in a batch. */
+int umans_batch_create(const char* const* config_files, int n, umans_sim** out);
+/* offsets[0..nscenarios] (cap >= nscenarios + 1), either pointer may be null */
+int umans_batch_offsets(umans_sim* sim, int* offsets, int cap, int* nscenarios);
+/* Times the step's launch-shape candidates (cell size per interaction range,
+ * warps per block, occupancy, agent-to-warp schedule) for trial_steps each
+ * from the current state, which is restored, and keeps the fastest; reports
+ * the choice (any pointer may be null). */
+int umans_autotune(umans_sim* sim, int trial_steps, float* cells_per_range, int* warps_per_block,
+                   float* occupancy, int* schedule);
 /* CrowdSimulator::RunSimulationSteps (crowdSimulator.cpp:77-95): n steps,
  * waits for them, reports device-side errors */
 int umans_step(umans_sim* sim, int nsteps);

@@ -1,0 +1,58 @@
+"""The batched form: many independent scenarios stepped together must give
+each scenario exactly the trajectory it has on its own (and, through the
+golden fixtures, the reference's)."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from umans_gb300 import Batch, Simulation, scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed(tmp_path, count=24, cap=300):
+    counts = np.minimum(S.batch_counts(num=count, seed=4), cap)
+    return [S.batch_member(k, int(n)).write(str(tmp_path / f"m{k}.xml")) for k, n in enumerate(counts)]
+
+
+def test_batch_equals_individual_simulations(tmp_path):
+    paths = _mixed(tmp_path)
+    b = Batch(paths)
+    off = b.offsets
+    assert off[0] == 0 and len(off) == len(paths) + 1
+    b.step(25)
+    pos = b.positions()
+    for k, p in enumerate(paths):
+        s = Simulation(p)
+        s.step(25)
+        assert np.array_equal(pos[off[k]:off[k + 1]], s.positions()), f"scenario {k}"
+
+
+def test_autotune_keeps_results(tmp_path):
+    paths = _mixed(tmp_path, count=12)
+    a, b = Batch(paths), Batch(paths)
+    a.step(3)
+    b.step(3)
+    choice = b.autotune(trial_steps=2)
+    assert choice["cells_per_range"] > 0 and choice["warps_per_block"] in (2, 4)
+    a.step(10)
+    b.step(10)
+    assert np.array_equal(a.positions(), b.positions())
+
+
+def test_batch_of_golden_scenarios_matches_reference(golden_xml):
+    names = [n for n in golden_names() if not n.endswith("_Dutra")]
+    items = [golden_xml(n) for n in names]
+    b = Batch([p for p, _ in items])
+    off = b.offsets
+    snaps = sorted({int(s) for _, g in items for s in g["steps"] if s <= 60})
+    done = 0
+    for s in snaps:
+        b.step(s - done)
+        done = s
+        pos = b.positions()
+        for k, (name, (_, g)) in enumerate(zip(names, items)):
+            idx = np.nonzero(g["steps"] == s)[0]
+            if len(idx):
+                dev = float(np.abs(pos[off[k]:off[k + 1]] - g["pos"][idx[0]]).max()) if off[k + 1] > off[k] else 0.0
+                assert dev <= 1e-4, f"{name} step {s}: {dev}"

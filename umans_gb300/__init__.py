@@ -8,10 +8,11 @@ Python host mirror of the reference's interfaces:
                   getAgentPositions / setAgentPositions / addAgent /
                   removeAgent / setAgentGoal / cleanUp / getNumberOfAgents.
 * ``Simulation``  a handle to one simulation with numpy state access.
+* ``Batch``       many independent scenarios stepped together.
 
 Both call the CUDA engine through the C ABI (include/umans_gb300.h).
 """
 from ._lib import AgentData  # noqa: F401
-from .api import UMANS, Simulation, UmansError  # noqa: F401
+from .api import UMANS, Batch, Simulation, UmansError  # noqa: F401
 
-__all__ = ["UMANS", "Simulation", "UmansError", "AgentData"]
+__all__ = ["UMANS", "Simulation", "Batch", "UmansError", "AgentData"]

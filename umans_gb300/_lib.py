@@ -36,6 +36,10 @@ _SIGS = {
     "umans_create": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "umans_create_ex": (C.c_int, [C.c_char_p, C.c_int, C.c_float, C.c_int, C.POINTER(P)]),
     "umans_destroy": (C.c_int, [P]),
+    "umans_batch_create": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.POINTER(P)]),
+    "umans_batch_offsets": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
+    "umans_autotune": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                 C.POINTER(C.c_int)]),
     "umans_step": (C.c_int, [P, C.c_int]),
     "umans_step_async": (C.c_int, [P, C.c_int]),
     "umans_synchronize": (C.c_int, [P]),

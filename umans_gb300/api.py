@@ -109,6 +109,13 @@ class Simulation:
         self._check(self._lib.umans_device_state(self._h, C.byref(p), C.byref(v)))
         return p.value, v.value
 
+    def autotune(self, trial_steps: int = 3) -> dict:
+        cpr, occ = C.c_float(), C.c_float()
+        wpb, sched = C.c_int(), C.c_int()
+        self._check(self._lib.umans_autotune(self._h, int(trial_steps), C.byref(cpr), C.byref(wpb), C.byref(occ),
+                                             C.byref(sched)))
+        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value)
+
     def profile(self, enable: bool = True):
         self._check(self._lib.umans_profile(self._h, int(bool(enable))))
 
@@ -178,6 +185,40 @@ class Simulation:
         cnt = np.zeros(n, np.int32)
         self._check(self._lib.umans_neighbours(self._h, int(cap), _p(ids), _p(d2), _p(cnt)))
         return ids, d2, cnt
+
+
+class Batch(Simulation):
+    """Several independent scenarios stepped together on the GPU.
+
+    ``Batch(paths)``: agents of scenario k are at list slots
+    ``offsets[k]:offsets[k+1]`` of every state array.  Each scenario evolves
+    exactly as a ``Simulation`` of its own file.
+    """
+
+    def __init__(self, config_files):
+        lib = _lib.load()
+        arr = (C.c_char_p * len(config_files))(*[os.fsencode(f) for f in config_files])
+        h = C.c_void_p()
+        rc = lib.umans_batch_create(arr, len(config_files), C.byref(h))
+        if rc != 0:
+            raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+        self._lib = lib
+        self._h = h
+
+    @property
+    def offsets(self) -> np.ndarray:
+        ns = C.c_int()
+        self._check(self._lib.umans_batch_offsets(self._h, None, 0, C.byref(ns)))
+        off = np.zeros(ns.value + 1, np.int32)
+        self._check(self._lib.umans_batch_offsets(self._h, _p(off), off.size, None))
+        return off
+
+    def autotune(self, trial_steps: int = 3) -> dict:
+        cpr, occ = C.c_float(), C.c_float()
+        wpb, sched = C.c_int(), C.c_int()
+        self._check(self._lib.umans_autotune(self._h, int(trial_steps), C.byref(cpr), C.byref(wpb), C.byref(occ),
+                                             C.byref(sched)))
+        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value)
 
 
 class UMANS:

@@ -54,6 +54,49 @@ int umans_create_ex(const char* config_file, int max_neighbours, float cells_per
 	return UMANS_OK;
 }
 
+int umans_batch_create(const char* const* config_files, int n, umans_sim** out)
+{
+	if (!config_files || n <= 0 || !out) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	*out = nullptr;
+	std::vector<std::string> files;
+	for (int k = 0; k < n; ++k) {
+		if (!config_files[k]) return fail(nullptr, UMANS_ERR_ARGUMENT, "null file name");
+		files.emplace_back(config_files[k]);
+	}
+	std::string err;
+	Engine* e = Engine::create_batch(files, err);
+	if (!e) return fail(nullptr, UMANS_ERR_LOAD, err);
+	umans_sim* s = new umans_sim();
+	s->eng = e;
+	*out = s;
+	return UMANS_OK;
+}
+
+int umans_batch_offsets(umans_sim* s, int* offsets, int cap, int* nscenarios)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	const int ns = s->eng->num_scenarios();
+	if (nscenarios) *nscenarios = ns;
+	if (offsets) {
+		if (cap < ns + 1) return fail(s, UMANS_ERR_ARGUMENT, "offsets buffer needs nscenarios + 1 entries");
+		for (int k = 0; k <= ns; ++k) offsets[k] = s->eng->scenario_offset(k);
+	}
+	return UMANS_OK;
+}
+
+int umans_autotune(umans_sim* s, int trial_steps, float* cells_per_range, int* warps_per_block, float* occupancy,
+                   int* schedule)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	umans::EngineOptions o;
+	if (!s->eng->autotune(trial_steps, &o)) return fail(s, UMANS_ERR_CUDA, s->eng->error());
+	if (cells_per_range) *cells_per_range = o.cells_per_range;
+	if (warps_per_block) *warps_per_block = o.warps_per_block;
+	if (occupancy) *occupancy = o.occupancy;
+	if (schedule) *schedule = o.schedule;
+	return UMANS_OK;
+}
+
 int umans_create(const char* config_file, umans_sim** out)
 {
 	return umans_create_ex(config_file, 0, 0, 1, out);

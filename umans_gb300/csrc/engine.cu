@@ -38,8 +38,10 @@ static const uint32_t LCG_M = 2147483647u;   // minstd_rand0 modulus
 static const uint32_t LCG_A = 16807u;
 
 struct DevState {
-	int n, world;
-	float width, height, dt;
+	int n, nscen;
+	const ScenDesc* scen;   // [nscen]
+	int* agent_scen;        // [n] scenario of each agent, list order
+	int* cell_base;         // [nscen + 1]: first cell of each scenario's grid, then the total
 	float2 *pos, *vel, *goal, *view, *vwf, *pref;
 	float4* prm;
 	int *pol, *id;
@@ -49,15 +51,16 @@ struct DevState {
 	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces)
 	int *sSlot, *sId;
 	int *cell, *cnt, *start, *fill, *blocksum;
-	GridParams* grid;
-	unsigned* bbox;
+	GridParams* grid;       // [nscen]
+	unsigned* bbox;         // [4 * nscen]
 	int* status;
 	const PolicyDesc* pols;
 	const SampleEntry* table;
 	const uint32_t* lcgpow;
 	float4* scratch;
-	int maxnb, total_warps, max_cells;
-	float max_range, cells_per_range;
+	int maxnb, total_warps, max_cells;   // max_cells: capacity of the cell arrays (all scenarios)
+	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks
+	float cells_per_range;
 	ExpExceptions expx;   // host-expf exception table
 	int* slot_of_id;      // id -> list slot, -1 when absent
 	int id_bound;         // size of slot_of_id
@@ -81,51 +84,78 @@ __device__ __forceinline__ float o2f(unsigned u)
 	return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
+// bounding box of the agents of each infinite-world scenario
 __global__ void k_bbox(DevState S)
 {
-	float mnx = FLT_MAX, mny = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX;
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
-		const float2 p = S.pos[i];
-		mnx = fminf(mnx, p.x); mxx = fmaxf(mxx, p.x);
-		mny = fminf(mny, p.y); mxy = fmaxf(mxy, p.y);
-	}
-	for (int o = 16; o > 0; o >>= 1) {
-		mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-		mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-		mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-		mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-	}
-	if ((threadIdx.x & 31) == 0) {
-		atomicMin(&S.bbox[0], f2o(mnx)); atomicMin(&S.bbox[1], f2o(mny));
-		atomicMax(&S.bbox[2], f2o(mxx)); atomicMax(&S.bbox[3], f2o(mxy));
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= S.n) return;
+	const int s = S.agent_scen[i];
+	if (S.scen[s].world == W_TORIC) return;
+	const float2 p = S.pos[i];
+	const unsigned peers = __match_any_sync(__activemask(), s);
+	const unsigned a = __reduce_min_sync(peers, f2o(p.x)), b = __reduce_min_sync(peers, f2o(p.y));
+	const unsigned c = __reduce_max_sync(peers, f2o(p.x)), d = __reduce_max_sync(peers, f2o(p.y));
+	if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+		unsigned* B = S.bbox + 4 * s;
+		atomicMin(&B[0], a); atomicMin(&B[1], b);
+		atomicMax(&B[2], c); atomicMax(&B[3], d);
 	}
 }
 
-__global__ void k_grid(DevState S)
+// One block: grid parameters of every scenario, then the exclusive scan of
+// their cell counts into cell_base (scenario grids are concatenated).
+__global__ void __launch_bounds__(1024) k_grid(DevState S)
 {
-	float x0, y0, ex, ey;
-	if (S.world == W_TORIC) {
-		x0 = -0.5f * S.width; y0 = -0.5f * S.height; ex = S.width; ey = S.height;
-	} else {
-		x0 = o2f(S.bbox[0]); y0 = o2f(S.bbox[1]);
-		ex = o2f(S.bbox[2]) - x0; ey = o2f(S.bbox[3]) - y0;
-		if (S.n == 0) { x0 = y0 = 0; ex = ey = 1; }
+	const int ns = S.nscen;
+	const int per = (ns + blockDim.x - 1) / blockDim.x;
+	const int s0 = threadIdx.x * per;
+	int local = 0;
+	for (int k = 0; k < per && s0 + k < ns; ++k) {
+		const int s = s0 + k;
+		const ScenDesc sd = S.scen[s];
+		unsigned* B = S.bbox + 4 * s;
+		float x0, y0, ex, ey;
+		if (sd.world == W_TORIC) {
+			x0 = -0.5f * sd.width; y0 = -0.5f * sd.height; ex = sd.width; ey = sd.height;
+		} else {
+			x0 = o2f(B[0]); y0 = o2f(B[1]);
+			ex = o2f(B[2]) - x0; ey = o2f(B[3]) - y0;
+			if (sd.n == 0) { x0 = y0 = 0; ex = ey = 1; }
+		}
+		B[0] = B[1] = f2o(FLT_MAX);
+		B[2] = B[3] = f2o(-FLT_MAX);
+		if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
+			atomicOr(S.status, ST_GRID_OVERFLOW);
+			x0 = y0 = 0; ex = ey = 1;
+		}
+		float cs = sd.max_range / S.cells_per_range;
+		if (!(cs >= 1e-3f)) cs = 1e-3f;
+		// +2 per axis: nx, ny below come from float divisions that may round up
+		while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)sd.max_cells) cs *= 2.0f;
+		GridParams g;
+		g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
+		g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
+		g.ncells = g.nx * g.ny; g.pad = 0;
+		S.grid[s] = g;
+		S.cell_base[s] = g.ncells;
+		local += g.ncells;
 	}
-	S.bbox[0] = S.bbox[1] = f2o(FLT_MAX);
-	S.bbox[2] = S.bbox[3] = f2o(-FLT_MAX);
-	if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
-		atomicOr(S.status, ST_GRID_OVERFLOW);
-		x0 = y0 = 0; ex = ey = 1;
+	__shared__ int tot[1024];
+	tot[threadIdx.x] = local;
+	__syncthreads();
+	for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+		const int v = threadIdx.x >= o ? tot[threadIdx.x - o] : 0;
+		__syncthreads();
+		tot[threadIdx.x] += v;
+		__syncthreads();
 	}
-	float cs = S.max_range / S.cells_per_range;
-	if (!(cs >= 1e-3f)) cs = 1e-3f;
-	// +2 per axis: nx, ny below come from float divisions that may round up
-	while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)S.max_cells) cs *= 2.0f;
-	GridParams g;
-	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
-	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
-	g.ncells = g.nx * g.ny; g.pad = 0;
-	*S.grid = g;
+	int run = tot[threadIdx.x] - local;
+	for (int k = 0; k < per && s0 + k < ns; ++k) {
+		const int c = S.cell_base[s0 + k];
+		S.cell_base[s0 + k] = run;
+		run += c;
+	}
+	if (threadIdx.x == blockDim.x - 1) S.cell_base[ns] = tot[threadIdx.x];
 }
 
 __device__ __forceinline__ int cell_coord(float v, float v0, float inv, int nmax)
@@ -139,9 +169,10 @@ __global__ void k_count(DevState S)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= S.n) return;
-	const GridParams g = *S.grid;
+	const int sc = S.agent_scen[i];
+	const GridParams g = S.grid[sc];
 	const float2 p = S.pos[i];
-	const int c = cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
+	const int c = S.cell_base[sc] + cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
 	S.cell[i] = c;
 	const unsigned peers = __match_any_sync(__activemask(), c);
 	if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.cnt[c], __popc(peers));
@@ -152,7 +183,7 @@ constexpr int SCAN_BLOCK = 256, SCAN_PER_BLOCK = 1024;
 
 __global__ void k_scan_reduce(DevState S)
 {
-	const int nc = S.grid->ncells;
+	const int nc = S.cell_base[S.nscen];
 	const int base = blockIdx.x * SCAN_PER_BLOCK;
 	if (base >= nc) return;
 	int s = 0;
@@ -174,7 +205,7 @@ __global__ void k_scan_reduce(DevState S)
 __global__ void k_scan_top(DevState S)
 {
 	// one block of 1024 threads; exclusive scan of the block sums in place
-	const int nb = (S.grid->ncells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+	const int nb = (S.cell_base[S.nscen] + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
 	const int per = (nb + 1023) / 1024;
 	const int b0 = threadIdx.x * per;
 	int local = 0;
@@ -200,7 +231,7 @@ __global__ void k_scan_top(DevState S)
 
 __global__ void k_scan_down(DevState S)
 {
-	const int nc = S.grid->ncells;
+	const int nc = S.cell_base[S.nscen];
 	const int base = blockIdx.x * SCAN_PER_BLOCK;
 	if (base >= nc) return;
 	// each thread owns 4 consecutive cells
@@ -446,8 +477,8 @@ __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int 
 // are grouped by displacement in the reference's order (worldToric.cpp:61-79)
 // and each group is sorted by the reference's double distance, ties by id.
 // On return key[] holds PhantomAgent::distSqr (worldBase.h:73-77).
-__device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L, int t, float2 p, float r,
-                      int lane, bool* overflow)
+__device__ int gather(const DevState& S, const GridParams& G, int cb, int world, float W, float H, const WarpLists& L,
+                      int t, float2 p, float r, int lane, bool* overflow)
 {
 	int K = 0;
 	const int maxnb = S.maxnb;
@@ -455,12 +486,11 @@ __device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L
 	const float r2 = r * r;
 	const double r2d = (double)r2;
 	const float r2lo = r2 * 0.999999f, r2hi = r2 * 1.000001f;
-	const float W = S.width, H = S.height;
 	const unsigned lt = (1u << lane) - 1u;
 	for (int g = 0; g < 5; ++g) {
 		float2 disp = V(0, 0);
 		if (g > 0) {
-			if (S.world != W_TORIC) break;
+			if (world != W_TORIC) break;
 			bool active;
 			// worldToric.cpp:64-76 compares the float p.x - r with the double
 			// -0.5*W; -0.5f*W is that value exactly, so the float compare agrees
@@ -484,7 +514,7 @@ __device__ int gather(const DevState& S, const GridParams& G, const WarpLists& L
 			const int nr = min(ROWS, cy1 - ry + 1);
 			int rs = 0, len = 0;
 			if (lane < nr) {
-				const int c0 = (ry + lane) * G.nx;
+				const int c0 = cb + (ry + lane) * G.nx;
 				rs = S.start[c0 + cx0];
 				len = S.start[c0 + cx1 + 1] - rs;
 			}
@@ -884,10 +914,12 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	float* fy = L.aux;
 	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
 	float4* proj = lines + maxnb;
-	const GridParams G = *S.grid;
 	bool overflow = false;
 
-	for (int t = gw; t < S.n; t += S.total_warps) {
+	const int per = (S.n + S.total_warps - 1) / S.total_warps;
+	const int t0 = S.sched ? gw * per : gw, stride = S.sched ? 1 : S.total_warps;
+	const int tend = S.sched ? min(S.n, t0 + per) : S.n;
+	for (int t = t0; t < tend; t += stride) {
 		const int slot = S.sSlot[t];
 		const float4 sb = S.sB[t];
 		const float4 prm = S.prm[slot];
@@ -896,13 +928,16 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		AgentCtx A;
 		A.pos = S.sP[t]; A.vel = S.sV[t]; A.pref = V(sb.x, sb.y); A.goal = S.goal[slot];
 		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
-		A.dt = S.dt; A.relax = pol.relax_time; A.ex = S.expx;
+		const int sc = S.agent_scen[slot];
+		const ScenDesc sd = S.scen[sc];
+		const GridParams G = S.grid[sc];
+		A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
 
-		const int K = gather(S, G, L, t, A.pos, pol.range, lane, &overflow);
+		const int K = gather(S, G, S.cell_base[sc], sd.world, sd.width, sd.height, L, t, A.pos, pol.range, lane, &overflow);
 		NbView N;
 		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB; N.sE = S.sE;
-		N.off[0] = V(0, 0); N.off[1] = V(-S.width, -0.0f); N.off[2] = V(S.width, -0.0f);
-		N.off[3] = V(-0.0f, -S.height); N.off[4] = V(-0.0f, S.height);
+		N.off[0] = V(0, 0); N.off[1] = V(-sd.width, -0.0f); N.off[2] = V(sd.width, -0.0f);
+		N.off[3] = V(-0.0f, -sd.height); N.off[4] = V(-0.0f, sd.height);
 
 		if (dump) {
 			const int cap = S.dump_cap;
@@ -1036,13 +1071,13 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 			// (double)|vd|^2 > 0.01 <=> |vd|^2 > 0.01f (0.01f is the float just below 0.01)
 			if (vsq(vd) > 0.01f) S.view[slot] = vnorm(vd);
 			float2 p = vadd(A.pos, vmul(vel, A.dt));
-			if (S.world == W_TORIC) {   // worldToric.cpp:81-108
-				const float hw = 0.5f * S.width, hh = 0.5f * S.height;
+			if (sd.world == W_TORIC) {   // worldToric.cpp:81-108
+				const float hw = 0.5f * sd.width, hh = 0.5f * sd.height;
 				float x = p.x, y = p.y;
-				if (x > hw) x -= S.width;
-				else if (x < -hw) x += S.width;
-				if (y > hh) y -= S.height;
-				else if (y < -hh) y += S.height;
+				if (x > hw) x -= sd.width;
+				else if (x < -hw) x += sd.width;
+				if (y > hh) y -= sd.height;
+				else if (y < -hh) y += sd.height;
 				p = V(x, y);
 			}
 			S.pos[slot] = p;
@@ -1119,8 +1154,13 @@ template <class T> static bool dalloc(T*& p, size_t n, std::string& err)
 
 Engine* Engine::create(const std::string& xml, std::string& err, const EngineOptions& opt)
 {
+	return create_batch(std::vector<std::string>{ xml }, err, opt);
+}
+
+Engine* Engine::create_batch(const std::vector<std::string>& xmls, std::string& err, const EngineOptions& opt)
+{
 	Engine* e = new Engine();
-	if (!e->init(xml, opt)) {
+	if (!e->init(xmls, opt)) {
 		err = e->err_;
 		delete e;
 		return nullptr;
@@ -1134,38 +1174,58 @@ static uint32_t minstd_seed(uint64_t s)
 	return x == 0 ? 1u : x;
 }
 
-bool Engine::init(const std::string& xml, const EngineOptions& opt)
+bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt)
 {
 	opt_ = opt;
-	if (!load_scenario(xml, sc_, err_)) return false;
-	for (const auto& p : sc_.policies) {
-		int norca = 0;
-		for (int c = 0; c < p.ncost; ++c) norca += p.cost[c].kind == K_ORCA;
-		if (norca > 1) { err_ = "a policy with more than one ORCA cost function is not supported"; return false; }
+	if (xmls.empty()) { err_ = "no scenario"; return false; }
+	scs_.resize(xmls.size());
+	for (size_t k = 0; k < xmls.size(); ++k) {
+		if (!load_scenario(xmls[k], scs_[k], err_)) {
+			if (xmls.size() > 1) err_ = xmls[k] + ": " + err_;
+			return false;
+		}
+		for (const auto& p : scs_[k].policies) {
+			int norca = 0;
+			for (int c = 0; c < p.ncost; ++c) norca += p.cost[c].kind == K_ORCA;
+			if (norca > 1) { err_ = "a policy with more than one ORCA cost function is not supported"; return false; }
+		}
+		if (xmls.size() > 1) {
+			for (const auto& a : scs_[k].agents)
+				if (a.start_time > 0 || a.remove_at_goal) {
+					err_ = xmls[k] + ": timed insertion and removal at the goal are not supported in a batch";
+					return false;
+				}
+		}
 	}
+	sc_ = scs_[0];
 	int dev = 0;
 	CK(cudaGetDevice(&dev));
 	CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
 	CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-	CK(cudaEventCreate(&ev0_));
-	CK(cudaEventCreate(&ev1_));
-	CK(cudaEventCreate(&pa0_));
-	CK(cudaEventCreate(&pa1_));
-	CK(cudaEventCreate(&ps0_));
-	CK(cudaEventCreate(&ps1_));
+	for (cudaEvent_t* e : { &ev0_, &ev1_, &pa0_, &pa1_, &ps0_, &ps1_ }) CK(cudaEventCreate(e));
 	d_ = new DevState();
 	std::memset(d_, 0, sizeof(DevState));
-	d_->world = sc_.world; d_->width = sc_.width; d_->height = sc_.height; d_->dt = sc_.dt;
 	d_->cells_per_range = opt_.cells_per_range;
-	float mr = 0;
-	for (const auto& p : sc_.policies) mr = std::max(mr, p.range);
-	d_->max_range = mr;
+	d_->nscen = (int)scs_.size();
 	next_unused_id_ = sc_.next_unused_id;
-	// agents present at time 0, in the order the reference adds them
-	for (const auto& a : sc_.agents) {
-		if (a.start_time <= 0) {
-			slot_of_[a.id] = (int)id_.size();
-			id_.push_back(a.id); pol_.push_back(a.policy);
+	// agents present at time 0, scenario by scenario, each in the order the
+	// reference adds them; policies concatenated with a base per scenario
+	scen_.resize(scs_.size());
+	for (size_t k = 0; k < scs_.size(); ++k) {
+		const Scenario& sc = scs_[k];
+		const int pbase = (int)pols_.size();
+		for (const auto& p : sc.policies) pols_.push_back(p);
+		ScenDesc& D = scen_[k];
+		D.world = sc.world; D.width = sc.width; D.height = sc.height; D.dt = sc.dt;
+		float mr = 0;
+		for (const auto& p : sc.policies) mr = std::max(mr, p.range);
+		D.max_range = mr;
+		D.agent_off = (int)id_.size();
+		for (const auto& a : sc.agents) {
+			if (a.start_time > 0) { pending_.push_back(a); continue; }
+			if (k == 0) slot_of_[a.id] = (int)id_.size();
+			id_.push_back(a.id); pol_.push_back(pbase + a.policy);
+			agent_scen_.push_back((int)k);
 			pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
 			goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
 			prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
@@ -1180,16 +1240,17 @@ bool Engine::init(const std::string& xml, const EngineOptions& opt)
 			}
 			view_.push_back(v0);
 			any_remove_at_goal_ |= a.remove_at_goal;
-		} else {
-			pending_.push_back(a);
 		}
+		D.n = (int)id_.size() - D.agent_off;
+		D.max_cells = scs_.size() == 1 ? std::max(4096, std::min(1 << 24, 4 * D.n + 1024)) : 4 * D.n + 256;
 	}
 	std::stable_sort(pending_.begin(), pending_.end(),
 	                 [](const AgentInit& x, const AgentInit& y) { return x.start_time < y.start_time; });
 	for (const auto& a : pending_) any_remove_at_goal_ |= a.remove_at_goal;
 	n_ = (int)id_.size();
+	times_.assign(scs_.size(), 0.0);
 	bool need_exp = false;
-	for (const auto& p : sc_.policies)
+	for (const auto& p : pols_)
 		for (int c = 0; c < p.ncost; ++c)
 			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE;
 	if (need_exp && !exp_exceptions_for_device(&d_->expx, nullptr, err_)) return false;
@@ -1202,7 +1263,7 @@ bool Engine::init(const std::string& xml, const EngineOptions& opt)
 
 bool Engine::build_tables()
 {
-	std::vector<PolicyDesc> pols = sc_.policies;
+	std::vector<PolicyDesc> pols = pols_;
 	std::vector<SampleEntry> table;
 	int maxrandom = 0;
 	for (auto& p : pols) {
@@ -1270,18 +1331,24 @@ bool Engine::alloc(int cap)
 {
 	cap_ = cap;
 	DevState& S = *d_;
-	const int mc = std::max(4096, std::min(1 << 24, 4 * cap + 1024));
-	S.max_cells = mc;
+	if (scen_.size() == 1) scen_[0].max_cells = std::max(4096, std::min(1 << 24, 4 * cap + 1024));
+	int64_t mc = 0;
+	for (const auto& D : scen_) mc += D.max_cells;
+	if (mc > (1 << 28)) { err_ = "too many grid cells"; return false; }
+	S.max_cells = (int)mc;
+	const int ns = (int)scen_.size();
 	if (!dalloc(S.pos, cap, err_) || !dalloc(S.vel, cap, err_) || !dalloc(S.goal, cap, err_) ||
 	    !dalloc(S.view, cap, err_) || !dalloc(S.vwf, cap, err_) || !dalloc(S.pref, cap, err_) ||
 	    !dalloc(S.prm, cap, err_) || !dalloc(S.pol, cap, err_) || !dalloc(S.id, cap, err_) ||
 	    !dalloc(S.rng, cap, err_) || !dalloc(S.sP, cap, err_) || !dalloc(S.sV, cap, err_) ||
 	    !dalloc(S.sB, cap, err_) || !dalloc(S.sE, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
-	    !dalloc(S.cell, cap, err_) || !dalloc(S.cnt, mc + 1, err_) || !dalloc(S.start, mc + 1, err_) ||
-	    !dalloc(S.fill, mc + 1, err_) || !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 2, err_))
+	    !dalloc(S.cell, cap, err_) || !dalloc(S.agent_scen, cap, err_) || !dalloc(S.cnt, mc + 1, err_) ||
+	    !dalloc(S.start, mc + 1, err_) || !dalloc(S.fill, mc + 1, err_) ||
+	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 2, err_))
 		return false;
-	if (!S.grid && !dalloc(S.grid, 1, err_)) return false;
-	if (!S.bbox && !dalloc(S.bbox, 4, err_)) return false;
+	if (!S.grid && !dalloc(S.grid, ns, err_)) return false;
+	if (!S.bbox && !dalloc(S.bbox, 4 * ns, err_)) return false;
+	if (!S.cell_base && !dalloc(S.cell_base, ns + 1, err_)) return false;
 	if (!S.status) {
 		if (!dalloc(S.status, 1, err_)) return false;
 		CK(cudaMemset(S.status, 0, sizeof(int)));
@@ -1289,8 +1356,9 @@ bool Engine::alloc(int cap)
 	CK(cudaMemset(S.cnt, 0, sizeof(int) * (mc + 1)));
 	// bbox sentinels: min = +FLT_MAX, max = -FLT_MAX in ordered encoding
 	auto enc = [](float f) { unsigned u; std::memcpy(&u, &f, 4); return (u & 0x80000000u) ? ~u : (u | 0x80000000u); };
-	unsigned hb[4] = { enc(FLT_MAX), enc(FLT_MAX), enc(-FLT_MAX), enc(-FLT_MAX) };
-	CK(cudaMemcpy(S.bbox, hb, sizeof(hb), cudaMemcpyHostToDevice));
+	std::vector<unsigned> hb(4 * ns);
+	for (int k = 0; k < ns; ++k) { hb[4 * k] = hb[4 * k + 1] = enc(FLT_MAX); hb[4 * k + 2] = hb[4 * k + 3] = enc(-FLT_MAX); }
+	CK(cudaMemcpy(S.bbox, hb.data(), sizeof(unsigned) * hb.size(), cudaMemcpyHostToDevice));
 	invalidate_graph();
 	return true;
 }
@@ -1309,7 +1377,14 @@ bool Engine::upload_all()
 		CK(cudaMemcpy(S.pol, pol_.data(), sizeof(int) * n_, cudaMemcpyHostToDevice));
 		CK(cudaMemcpy(S.id, id_.data(), sizeof(int) * n_, cudaMemcpyHostToDevice));
 		CK(cudaMemcpy(S.rng, rng_.data(), sizeof(uint32_t) * n_, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(S.agent_scen, agent_scen_.data(), sizeof(int) * n_, cudaMemcpyHostToDevice));
 	}
+	// scenario 0 owns every agent of a single simulation (including agents
+	// added or removed later)
+	if (scen_.size() == 1) { scen_[0].agent_off = 0; scen_[0].n = n_; }
+	if (!scen_dev_ && !dalloc(scen_dev_, scen_.size(), err_)) return false;
+	CK(cudaMemcpy(scen_dev_, scen_.data(), sizeof(ScenDesc) * scen_.size(), cudaMemcpyHostToDevice));
+	S.scen = scen_dev_;
 	int bound = 1;
 	for (int v : id_) bound = std::max(bound, v + 1);
 	std::vector<int> so(bound, -1);
@@ -1420,14 +1495,17 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	}
 	mode_ = 1;
-	for (const auto& p : sc_.policies) {
+	for (const auto& p : pols_) {
 		if (p.method != M_GRADIENT) mode_ = 0;
 		for (int c = 0; c < p.ncost; ++c)
 			if (!(p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_GOALREACHING))
 				mode_ = 0;
 	}
 	agent_blocks_ = agent_blocks_for(num_sms_, wpb, smem, mode_);
+	if (opt_.occupancy < 1.0f) agent_blocks_ = std::max(num_sms_, (int)(agent_blocks_ * opt_.occupancy));
 	S.total_warps = agent_blocks_ * wpb;
+	S.sched = opt_.schedule;
+	S.cells_per_range = opt_.cells_per_range;
 	if (!dalloc(S.scratch, (size_t)S.total_warps * 2 * maxnb_, err_)) return false;
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
@@ -1443,8 +1521,8 @@ void Engine::enqueue_step()
 	const size_t smem = (size_t)wpb * maxnb_ * 16;
 	const int threads = 256;
 	const int nb = std::max(1, (n_ + threads - 1) / threads);
-	if (S.world != W_TORIC) k_bbox<<<std::min(nb, 2 * num_sms_), threads, 0, stream_>>>(S);
-	k_grid<<<1, 1, 0, stream_>>>(S);
+	k_bbox<<<nb, threads, 0, stream_>>>(S);
+	k_grid<<<1, 1024, 0, stream_>>>(S);
 	k_count<<<nb, threads, 0, stream_>>>(S);
 	const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
 	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
@@ -1457,7 +1535,7 @@ void Engine::enqueue_step()
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
 
-int Engine::kernels_per_step() const { return sc_.world == W_TORIC ? 7 : 8; }
+int Engine::kernels_per_step() const { return 8; }
 
 bool Engine::capture_graph()
 {
@@ -1481,6 +1559,7 @@ bool Engine::apply_pending_agents()
 		const AgentInit& a = pending_[k];
 		slot_of_[a.id] = (int)id_.size();
 		id_.push_back(a.id); pol_.push_back(a.policy);
+		agent_scen_.push_back(0);
 		pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
 		goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
 		prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
@@ -1521,6 +1600,7 @@ bool Engine::remove_at_goal()
 			}
 			id_.pop_back(); pol_.pop_back(); pos_.pop_back(); vel_.pop_back(); goal_.pop_back();
 			view_.pop_back(); vwf_.pop_back(); prm_.pop_back(); rng_.pop_back(); remove_.pop_back();
+			agent_scen_.pop_back();
 			--n_;
 			changed = true;
 		}
@@ -1552,6 +1632,7 @@ bool Engine::run_steps(int nsteps)
 			}
 		}
 		time_ += sc_.dt;
+		for (size_t k = 0; k < times_.size(); ++k) times_[k] += scen_[k].dt;
 	}
 	return true;
 }
@@ -1578,6 +1659,7 @@ bool Engine::take_snapshot()
 	}
 	snap_valid_ = true;
 	snap_time_ = time_;
+	snap_times_ = times_;
 	snap_steps_ = 0;
 	return true;
 }
@@ -1593,6 +1675,7 @@ bool Engine::restore_snapshot()
 		CK(cudaMemcpyAsync(S.rng, snap_rng_, sizeof(uint32_t) * n_, cudaMemcpyDeviceToDevice, stream_));
 	}
 	time_ = snap_time_;
+	times_ = snap_times_;
 	return true;
 }
 
@@ -1738,6 +1821,7 @@ bool Engine::add_agent(float x, float y, float radius, float pref, float maxs, f
 	if (id >= next_unused_id_) next_unused_id_ = id + 1;
 	slot_of_[id] = (int)id_.size();
 	id_.push_back(id); pol_.push_back(pidx);
+	agent_scen_.push_back(0);
 	pos_.push_back(make_float2(x, y)); vel_.push_back(make_float2(0, 0));
 	goal_.push_back(make_float2(x, y)); vwf_.push_back(make_float2(0, 0));
 	view_.push_back(make_float2(0, 0));
@@ -1767,6 +1851,7 @@ bool Engine::remove_agent(int id)
 	}
 	id_.pop_back(); pol_.pop_back(); pos_.pop_back(); vel_.pop_back(); goal_.pop_back();
 	view_.pop_back(); vwf_.pop_back(); prm_.pop_back(); rng_.pop_back(); remove_.pop_back();
+	agent_scen_.pop_back();
 	n_ = last;
 	return upload_all();
 }
@@ -1795,8 +1880,8 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	if (!dalloc(scr, (size_t)T.total_warps * 2 * dump_nb, err_)) return false;
 	T.scratch = scr;
 	const int threads = 256, nb = (n_ + threads - 1) / threads;
-	if (T.world != W_TORIC) k_bbox<<<std::min(nb, 2 * num_sms_), threads, 0, stream_>>>(T);
-	k_grid<<<1, 1, 0, stream_>>>(T);
+	k_bbox<<<nb, threads, 0, stream_>>>(T);
+	k_grid<<<1, 1024, 0, stream_>>>(T);
 	k_count<<<nb, threads, 0, stream_>>>(T);
 	const int sb = (T.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
 	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
@@ -1818,6 +1903,55 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	return true;
 }
 
+// Chooses the launch shape of the step by timing a few steps of each
+// candidate from the current state, which is restored afterwards.  Every
+// candidate computes bit-identical results: the cell size changes which
+// cells are scanned, not which neighbours are found or their order.
+bool Engine::autotune(int trial_steps, EngineOptions* chosen)
+{
+	if (!sync()) return false;
+	if (trial_steps < 1) trial_steps = 1;
+	const EngineOptions base = opt_;
+	EngineOptions best = opt_;
+	float best_ms = 1e30f;
+	const bool prof = profile_;
+	profile_ = false;
+	if (!take_snapshot()) return false;
+	for (float cpr : { 1.0f, 2.0f, 3.0f })
+		for (int wpb : { 2, 4 })
+			for (float occ : { 1.0f, 0.5f })
+				for (int sched : { 0, 1 }) {
+					opt_ = base;
+					opt_.cells_per_range = cpr; opt_.warps_per_block = wpb; opt_.occupancy = occ; opt_.schedule = sched;
+					if (!configure()) return false;
+					if (!restore_snapshot()) return false;
+					if (!run_steps(1)) return false;   // graph capture, warm-up
+					CK(cudaEventRecord(ev0_, stream_));
+					if (!run_steps(trial_steps)) return false;
+					CK(cudaEventRecord(ev1_, stream_));
+					CK(cudaEventSynchronize(ev1_));
+					float ms = 0;
+					cudaEventElapsedTime(&ms, ev0_, ev1_);
+					int st = 0;
+					CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
+					if (st) {   // a trial overflowed the neighbour capacity: grow it, discard the trial
+						CK(cudaMemset(d_->status, 0, sizeof(int)));
+						if (st & ST_NEIGHBOUR_OVERFLOW) maxnb_ = std::min(3072, maxnb_ * 2);
+						continue;
+					}
+					if (ms < best_ms) { best_ms = ms; best = opt_; }
+				}
+	opt_ = best;
+	if (!configure()) return false;
+	if (!restore_snapshot()) return false;
+	snap_steps_ = 0;
+	CK(cudaStreamSynchronize(stream_));
+	snap_valid_ = false;
+	profile_ = prof;
+	if (chosen) *chosen = best;
+	return true;
+}
+
 void* Engine::device_positions() const { return d_->pos; }
 void* Engine::device_velocities() const { return d_->vel; }
 
@@ -1830,6 +1964,7 @@ Engine::~Engine()
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,
 		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.fill, S.blocksum, S.grid, S.bbox, S.status,
 		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io,
+		                 S.agent_scen, S.cell_base, scen_dev_,
 		                 snap_pos_, snap_vel_, snap_view_, snap_vwf_, snap_rng_ };
 		for (void* p : ptrs)
 			if (p) cudaFree(p);

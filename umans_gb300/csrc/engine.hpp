@@ -23,12 +23,20 @@ struct EngineOptions {
 	int max_neighbours = 0;        // 0: chosen from the initial state
 	float cells_per_range = 2.0f;  // grid cell size = range / cells_per_range
 	int warps_per_block = 4;
+	float occupancy = 1.0f;   // fraction of the resident blocks per SM that the agent kernel launches
+	int schedule = 0;         // agents to warps: 0 interleaved, 1 contiguous blocks
 	bool use_graph = true;
 };
 
 class Engine {
 public:
 	static Engine* create(const std::string& xml, std::string& err, const EngineOptions& opt = EngineOptions());
+	// several independent scenarios stepped together (agents concatenated,
+	// scenario k at list slots [offset(k), offset(k+1)))
+	static Engine* create_batch(const std::vector<std::string>& xmls, std::string& err,
+	                            const EngineOptions& opt = EngineOptions());
+	int num_scenarios() const { return (int)scen_.size(); }
+	int scenario_offset(int k) const { return k < (int)scen_.size() ? scen_[k].agent_off : n_; }
 	~Engine();
 
 	// Enqueues n steps on the engine's stream; returns false on a host-side
@@ -60,6 +68,11 @@ public:
 	// `cap` entries per agent; counts[i] = full list length.
 	bool neighbours(int cap, int* ids, float* d2, int* counts);
 
+	// times the launch-shape candidates from the current state (restored
+	// afterwards) and keeps the fastest
+	bool autotune(int trial_steps, EngineOptions* chosen);
+	const EngineOptions& options() const { return opt_; }
+
 	// device pointers of the raw state for callers that keep data on the GPU
 	void* device_positions() const;
 	void* device_velocities() const;
@@ -78,7 +91,7 @@ public:
 
 private:
 	Engine() = default;
-	bool init(const std::string& xml, const EngineOptions& opt);
+	bool init(const std::vector<std::string>& xmls, const EngineOptions& opt);
 	bool upload_all();
 	bool alloc(int cap);
 	bool build_tables();
@@ -94,7 +107,13 @@ private:
 	bool remove_at_goal();
 	bool download_mutable();
 
-	Scenario sc_;
+	Scenario sc_;                    // scenario 0 (single-simulation API)
+	std::vector<Scenario> scs_;
+	std::vector<ScenDesc> scen_;
+	ScenDesc* scen_dev_ = nullptr;
+	std::vector<PolicyDesc> pols_;   // all scenarios' policies, concatenated
+	std::vector<int> agent_scen_;
+	std::vector<double> times_, snap_times_;
 	EngineOptions opt_;
 	std::string err_;
 	int n_ = 0, cap_ = 0;

@@ -72,6 +72,15 @@ struct AgentRecord {
 	float px, py, vx, vy, wx, wy;
 };
 
+// One scenario of a simulation (a batch holds several, agents concatenated).
+struct ScenDesc {
+	int world;
+	float width, height, dt;
+	float max_range;      // largest interaction range of its policies
+	int agent_off, n;     // its agents occupy list slots [agent_off, agent_off + n)
+	int max_cells;        // cap on its grid's cell count
+};
+
 // Grid parameters written by the device each step.
 struct GridParams {
 	float x0, y0, cs, inv_cs;
