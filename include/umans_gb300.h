@@ -138,6 +138,35 @@ int umans_device_state(umans_sim* sim, void** pos, void** vel);
 int umans_profile(umans_sim* sim, int enable);
 int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_ms, int* steps,
                          int* kernels_per_step);
+/* Differentiable form (no counterpart in the reference), for calibrating
+ * force-model parameters against observed trajectories.  Supported policies:
+ * method "gradient" with SocialForcesAvoidance, PowerLaw and
+ * GoalReachingForce costs (ForceBasedFunction::GetGradient,
+ * src/Engine/CostFunctions/ForceBasedFunction.cpp:32-36), contact forces
+ * included; a fixed agent set.
+ *
+ * umans_diff_begin records the current state as the episode's start and the
+ * targets (steps x n x 2 floats, list order); the loss of an episode is
+ *   L = weight * sum_{t=1..steps} sum_i |p_i(t) - target_i(t)|^2
+ * (weight <= 0: 1 / (steps * n)).  umans_diff_forward runs the episode from
+ * its start, keeping a checkpoint every checkpoint_every steps, and returns
+ * L.  umans_diff_backward recomputes each segment from its checkpoint with
+ * the neighbour lists recorded, reverses it (hand-written adjoint), writes
+ * dL/d(V0, sigma, k, tau0) per scenario into dparams[4 * nscenarios] and,
+ * where non-null, dL/d(initial positions) and dL/d(initial velocities)
+ * (n x 2 floats each), and puts the simulation back in the start state.
+ * Neighbour lists and branches (cut-offs, clamps, the view-angle factor) are
+ * those of the forward pass: the gradient is that of the piecewise-smooth
+ * step map on the piece the episode lies in. */
+int umans_diff_begin(umans_sim* sim, int steps, int checkpoint_every, const float* targets, float weight);
+int umans_diff_forward(umans_sim* sim, double* loss);
+int umans_diff_backward(umans_sim* sim, float* dparams, float* dpos0, float* dvel0);
+int umans_diff_end(umans_sim* sim);
+/* (V0, sigma) of every SocialForcesAvoidance cost and (k, tau0) of every
+ * PowerLaw cost of scenario `scenario` (all scenarios when < 0); NaN entries
+ * are left unchanged.  get: NaN where the scenario has no such cost. */
+int umans_set_force_params(umans_sim* sim, int scenario, const float* params4);
+int umans_get_force_params(umans_sim* sim, int scenario, float* params4);
 /* Test hook: the device's exponential used by the force models, which
  * returns exactly the host C library's expf for x in [-87, 0]; evaluates n
  * values and reports the size of the exception table.  Errors are reported

@@ -63,6 +63,12 @@ _SIGS = {
     "umans_profile": (C.c_int, [P, C.c_int]),
     "umans_profile_totals": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int)]),
+    "umans_diff_begin": (C.c_int, [P, C.c_int, C.c_int, P, C.c_float]),
+    "umans_diff_forward": (C.c_int, [P, C.POINTER(C.c_double)]),
+    "umans_diff_backward": (C.c_int, [P, P, P, P]),
+    "umans_diff_end": (C.c_int, [P]),
+    "umans_set_force_params": (C.c_int, [P, C.c_int, P]),
+    "umans_get_force_params": (C.c_int, [P, C.c_int, P]),
     "umans_debug_ref_expf": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_size_t)]),
     "umans_orca_velocities_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, C.c_float,
                                                 C.c_float, C.c_float, C.c_float, P, P]),

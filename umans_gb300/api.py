@@ -186,6 +186,53 @@ class Simulation:
         self._check(self._lib.umans_neighbours(self._h, int(cap), _p(ids), _p(d2), _p(cnt)))
         return ids, d2, cnt
 
+    @property
+    def num_scenarios(self) -> int:
+        ns = C.c_int()
+        self._check(self._lib.umans_batch_offsets(self._h, None, 0, C.byref(ns)))
+        return ns.value
+
+    # --- differentiable form (calibration) ------------------------------
+    def set_force_params(self, params, scenario: int = -1):
+        """(V0, sigma, k, tau0) of the SocialForcesAvoidance / PowerLaw costs
+        of one scenario (all when scenario < 0); NaN entries stay unchanged."""
+        a = np.ascontiguousarray(params, np.float32).reshape(4)
+        self._check(self._lib.umans_set_force_params(self._h, int(scenario), _p(a)))
+
+    def force_params(self, scenario: int = 0) -> np.ndarray:
+        a = np.zeros(4, np.float32)
+        self._check(self._lib.umans_get_force_params(self._h, int(scenario), _p(a)))
+        return a
+
+    def diff_begin(self, targets, checkpoint_every: int = 10, weight: float = 0.0):
+        """Start an episode from the current state: targets[t, i] is the
+        position agent i should have after step t + 1 (list order)."""
+        t = np.ascontiguousarray(targets, np.float32)
+        if t.ndim != 3 or t.shape[1:] != (self.n, 2):
+            raise ValueError("targets must have shape (steps, n, 2)")
+        self._check(self._lib.umans_diff_begin(self._h, t.shape[0], int(checkpoint_every), _p(t), float(weight)))
+        self._diff_steps = t.shape[0]
+
+    def diff_forward(self) -> float:
+        loss = C.c_double()
+        self._check(self._lib.umans_diff_forward(self._h, C.byref(loss)))
+        return loss.value
+
+    def diff_backward(self, with_state: bool = False):
+        """dL/d(V0, sigma, k, tau0) per scenario [num_scenarios, 4]; with
+        with_state also dL/d(initial positions) and dL/d(initial velocities)."""
+        dp = np.zeros((self.num_scenarios, 4), np.float32)
+        if not with_state:
+            self._check(self._lib.umans_diff_backward(self._h, _p(dp), None, None))
+            return dp
+        gp = np.zeros((self.n, 2), np.float32)
+        gv = np.zeros((self.n, 2), np.float32)
+        self._check(self._lib.umans_diff_backward(self._h, _p(dp), _p(gp), _p(gv)))
+        return dp, gp, gv
+
+    def diff_end(self):
+        self._check(self._lib.umans_diff_end(self._h))
+
 
 class Batch(Simulation):
     """Several independent scenarios stepped together on the GPU.

@@ -271,6 +271,50 @@ int umans_profile_totals(umans_sim* s, double* agent_kernel_ms, double* step_ms,
 	return UMANS_OK;
 }
 
+int umans_diff_begin(umans_sim* s, int steps, int checkpoint_every, const float* targets, float weight)
+{
+	if (!s || steps <= 0 || checkpoint_every <= 0 || (!targets && s->eng->num_agents() > 0))
+		return UMANS_ERR_ARGUMENT;
+	if (!s->eng->diff_begin(steps, checkpoint_every, targets, weight))
+		return fail(s, UMANS_ERR_ARGUMENT, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_diff_forward(umans_sim* s, double* loss)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->diff_forward(loss)) return fail(s, UMANS_ERR_DEVICE, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_diff_backward(umans_sim* s, float* dparams, float* dpos0, float* dvel0)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->diff_backward(dparams, dpos0, dvel0)) return fail(s, UMANS_ERR_DEVICE, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_diff_end(umans_sim* s)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	s->eng->diff_end();
+	return UMANS_OK;
+}
+
+int umans_set_force_params(umans_sim* s, int scenario, const float* params4)
+{
+	if (!s || !params4) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->set_force_params(scenario, params4)) return fail(s, UMANS_ERR_ARGUMENT, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_get_force_params(umans_sim* s, int scenario, float* params4)
+{
+	if (!s || !params4) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->get_force_params(scenario, params4)) return fail(s, UMANS_ERR_ARGUMENT, s->eng->error());
+	return UMANS_OK;
+}
+
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 {
 	if ((n > 0 && (!x || !y)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");

@@ -29,6 +29,7 @@
 
 #include "costs.cuh"
 #include "orca.cuh"
+#include "adjoint.cuh"
 
 namespace umans {
 
@@ -62,6 +63,16 @@ struct DevState {
 	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks
 	float cells_per_range;
 	ExpExceptions expx;   // host-expf exception table
+	// differentiable form: neighbour lists recorded during a forward step
+	// (list-order slot of the neighbour | displacement group << 28), and the
+	// adjoint buffers of k_adjoint
+	uint32_t* tape_list;  // [n * maxnb] or null
+	int* tape_cnt;        // [n]
+	const float2 *a_pos, *a_vel;        // state at the start of the step being reversed
+	const float2 *lam_out_p, *lam_out_v;
+	float2 *lam_in_p, *lam_in_v;
+	float2* tape_acc;     // [n]: acceleration before the clamp (gradient method)
+	float* dparams;       // [nscen * 4]: dL/d(V0, sigma, k, tau0)
 	int* slot_of_id;      // id -> list slot, -1 when absent
 	int id_bound;         // size of slot_of_id
 	AgentRecord* io;      // staging for AgentData exchange
@@ -899,7 +910,9 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 // force-based costs only (SocialForcesAvoidance, PowerLaw,
 // GoalReachingForce); the sampling, ORCA and finite-difference code is
 // compiled out, which lowers register use and raises occupancy.
-template <int MODE>
+// TAPE: also record the neighbour lists and the pre-clamp acceleration for
+// the differentiable form's backward pass
+template <int MODE, bool TAPE = false>
 __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
 {
 	extern __shared__ unsigned char smem[];
@@ -949,6 +962,13 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 			__syncwarp();
 			continue;
 		}
+		if (TAPE) {
+			for (int k = lane; k < K; k += 32) {
+				const uint32_t rr = L.ref[k];
+				S.tape_list[(size_t)slot * maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
+			}
+			if (lane == 0) S.tape_cnt[slot] = K;
+		}
 
 		// phase 5: contact forces (policy.cpp:107-141), independent of phase 4
 		float2 contact = V(0, 0);
@@ -987,6 +1007,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 			}
 			const float2 acc = vclamp(vmul(T, -1), A.maxacc);
 			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
+			if (TAPE && lane == 0) S.tape_acc[slot] = vmul(T, -1);
 		} else if (MODE == 0 && !viszero(A.pref)) {
 			CostPrep P;
 			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
@@ -1042,6 +1063,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					T = vadd(T, vmul(g, c.coeff));
 				}
 				acc = vmul(T, -1);
+				if (TAPE && lane == 0) S.tape_acc[slot] = acc;
 			} else if (MODE == 0) {
 				float2 best;
 				const CostDesc& c0 = pol.cost[0];
@@ -1111,6 +1133,167 @@ bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::st
 	cudaFree(dy);
 	if (e != cudaSuccess) { err = cudaGetErrorString(e); return false; }
 	return true;
+}
+
+// ------------------------------------------------------------------------
+// differentiable form
+// ------------------------------------------------------------------------
+// Adjoint of one step for policies made of SocialForcesAvoidance, PowerLaw
+// and GoalReachingForce under the gradient method, with the neighbour lists
+// the forward step recorded.  One warp per agent (list order): the forward
+// quantities are recomputed, then the adjoints of the agent's new position
+// and velocity are propagated to its own state, its neighbours' states
+// (atomicAdd) and the scenario's parameters (V0, sigma, k, tau0).
+// the neighbour's normalised preferred velocity, as the scatter computes it
+// from the adjoint pass's state
+__device__ __forceinline__ float2 goal_dir(const DevState& S, int j)
+{
+	const float2 d = vsub(S.goal[j], S.a_pos[j]);
+	const float4 prm = S.prm[j];
+	if (vsq(d) <= prm.x * prm.x) return V(0, 0);
+	return vnorm(vmul(vnorm(d), prm.y));
+}
+
+__global__ void __launch_bounds__(128) k_adjoint(DevState S)
+{
+	const int lane = threadIdx.x & 31;
+	const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int nw = (gridDim.x * blockDim.x) >> 5;
+	for (int i = gw; i < S.n; i += nw) {
+		const int sc = S.agent_scen[i];
+		const ScenDesc sd = S.scen[sc];
+		const PolicyDesc& pol = S.pols[S.pol[i]];
+		const float4 prm = S.prm[i];
+		AgentCtx A;
+		A.pos = S.a_pos[i]; A.vel = S.a_vel[i]; A.goal = S.goal[i];
+		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
+		A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
+		const float dt = sd.dt;
+		const float2 lp = S.lam_out_p[i], lvo = S.lam_out_v[i];
+		// p' = p + v'' dt, v'' = v' + C dt / 80
+		const float2 lvn = add2(lvo, mul2(lp, dt));
+		// per-lane partial adjoints, warp-summed at the end (lane 0 holds the
+		// agent's own terms)
+		float2 lpi = lane == 0 ? lp : v2(0, 0), lvi = v2(0, 0);
+		const float2 lC = mul2(lvn, dt / 80.0f);
+		// preferred velocity (agent.cpp:52-59)
+		const float2 w = sub2(A.goal, A.pos);
+		const bool at_goal = dot2(w, w) <= A.radius * A.radius;
+		A.pref = at_goal ? v2(0, 0) : vmul(vnorm(w), A.prefspeed);
+		const int K = S.tape_cnt[i];
+		const uint32_t* list = S.tape_list + (size_t)i * S.maxnb;
+		const float2 off[5] = { v2(0, 0), v2(-sd.width, -0.0f), v2(sd.width, -0.0f), v2(-0.0f, -sd.height),
+		                        v2(-0.0f, sd.height) };
+		// a = sum coeff F / m (ForceBasedFunction::GetGradient with policy.cpp:78-89)
+		// (the forward step recorded a before the clamp)
+		float2 lF[MAX_COSTS];
+		for (int c = 0; c < MAX_COSTS; ++c) lF[c] = v2(0, 0);
+		if (!viszero(A.pref)) {
+			const float2 a = S.tape_acc[i];
+			const float2 ac = vclamp(a, A.maxacc);
+			const float2 u = add2(A.vel, mul2(ac, dt));
+			const float2 lu = clamp_adj(u, A.maxspeed, lvn);
+			if (lane == 0) lvi = add2(lvi, lu);
+			const float2 la = clamp_adj(a, A.maxacc, mul2(lu, dt));
+			for (int c = 0; c < pol.ncost; ++c) lF[c] = mul2(la, pol.cost[c].coeff / pol.cost[c].p[5]);
+		}
+		float2 lpref = v2(0, 0);
+		float dV0 = 0, dsig = 0, dk = 0, dtau0 = 0;
+		for (int c = 0; c < pol.ncost; ++c) {
+			const CostDesc& cd = pol.cost[c];
+			if (cd.kind == K_GOALREACHING) {
+				const float mr = fmaxr(A.relax, dt);
+				if (lane == 0) { lpref = add2(lpref, mul2(lF[c], 1.0f / mr)); lvi = sub2(lvi, mul2(lF[c], 1.0f / mr)); }
+				continue;
+			}
+			if (viszero(A.pref)) continue;
+			const float rs = cd.range * cd.range;
+			for (int k = lane; k < K; k += 32) {
+				const uint32_t e = list[k];
+				const int j = (int)(e & 0x0FFFFFFFu);
+				const float2 pj = add2(S.a_pos[j], off[e >> 28]);
+				if (dot2(sub2(A.pos, pj), sub2(A.pos, pj)) > rs) continue;
+				const float2 vj = S.a_vel[j];
+				const float rj = S.prm[j].x;
+				float2 lpj = v2(0, 0), lvj = v2(0, 0);
+				if (cd.kind == K_SOCIALFORCES) {
+					const float2 wj = sub2(S.goal[j], S.a_pos[j]);
+					const float2 ebj = goal_dir(S, j);
+					const SfAdj r = sf_pair_adj(A, cd, pj, vj, ebj, rj, lF[c]);
+					lpi = add2(lpi, r.lR);
+					lpj = sub2(lpj, r.lR);
+					lvj = add2(lvj, r.lvj);
+					// Eb_j = (g_j - p_j)/|g_j - p_j| away from the goal
+					if (!viszero(ebj)) lpj = sub2(lpj, normalize_adj(wj, r.lEb));
+					dV0 += r.lV0;
+					dsig += r.lsigma;
+				} else {
+					const PlAdj r = pl_pair_adj(A, cd, pj, vj, rj, lF[c]);
+					lpi = add2(lpi, r.lx);
+					lpj = sub2(lpj, r.lx);
+					lvi = add2(lvi, r.lv);
+					lvj = sub2(lvj, r.lv);
+					dk += r.lk;
+					dtau0 += r.ltau0;
+				}
+				atomicAdd(&S.lam_in_p[j].x, lpj.x); atomicAdd(&S.lam_in_p[j].y, lpj.y);
+				atomicAdd(&S.lam_in_v[j].x, lvj.x); atomicAdd(&S.lam_in_v[j].y, lvj.y);
+			}
+		}
+		// contact forces (all neighbours): C = sum scale (rsum - |D|) D/|D|
+		if (pol.contact_scale > 0) {
+			for (int k = lane; k < K; k += 32) {
+				const uint32_t e = list[k];
+				const int j = (int)(e & 0x0FFFFFFFu);
+				const float2 D = sub2(A.pos, add2(S.a_pos[j], off[e >> 28]));
+				const float2 lD = contact_adj(D, A.radius + S.prm[j].x, pol.contact_scale, lC);
+				if (lD.x != 0 || lD.y != 0) {
+					lpi = add2(lpi, lD);
+					atomicAdd(&S.lam_in_p[j].x, -lD.x); atomicAdd(&S.lam_in_p[j].y, -lD.y);
+				}
+			}
+		}
+		// warp sums (lane 0 also holds the goal-force terms)
+		float vals[8] = { lpi.x, lpi.y, lvi.x, lvi.y, dV0, dsig, dk, dtau0 };
+		for (int q = 0; q < 8; ++q)
+			for (int o = 16; o > 0; o >>= 1) vals[q] += __shfl_xor_sync(0xffffffffu, vals[q], o);
+		if (lane == 0) {
+			float2 P = v2(vals[0], vals[1]);
+			if (!at_goal) P = sub2(P, mul2(normalize_adj(w, lpref), A.prefspeed));   // pref = s (g - p)/|g - p|
+			atomicAdd(&S.lam_in_p[i].x, P.x); atomicAdd(&S.lam_in_p[i].y, P.y);
+			atomicAdd(&S.lam_in_v[i].x, vals[2]); atomicAdd(&S.lam_in_v[i].y, vals[3]);
+			float* dp = S.dparams + 4 * sc;
+			if (vals[4] != 0) atomicAdd(dp + 0, vals[4]);
+			if (vals[5] != 0) atomicAdd(dp + 1, vals[5]);
+			if (vals[6] != 0) atomicAdd(dp + 2, vals[6]);
+			if (vals[7] != 0) atomicAdd(dp + 3, vals[7]);
+		}
+		__syncwarp();
+	}
+}
+
+// loss += w |p - target|^2 summed over agents (double accumulation)
+__global__ void k_loss(DevState S, const float2* target, float w, double* loss)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	float v = 0;
+	if (i < S.n) {
+		const float2 d = sub2(S.pos[i], target[i]);
+		v = w * dot2(d, d);
+	}
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	if ((threadIdx.x & 31) == 0 && v != 0) atomicAdd(loss, (double)v);
+}
+
+// lam_p = lam_p_in + 2 w (pos - target); lam_v = lam_v_in
+__global__ void k_inject(int n, const float2* pos, const float2* target, float w, const float2* lpin,
+                         const float2* lvin, float2* lpout, float2* lvout)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float2 d = sub2(pos[i], target[i]);
+	lpout[i] = add2(lpin[i], mul2(d, 2 * w));
+	lvout[i] = lvin[i];
 }
 
 // GetAgentPositions (APIFunctions.cpp:90-115): one record per agent
@@ -1214,7 +1397,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	for (size_t k = 0; k < scs_.size(); ++k) {
 		const Scenario& sc = scs_[k];
 		const int pbase = (int)pols_.size();
-		for (const auto& p : sc.policies) pols_.push_back(p);
+		for (const auto& p : sc.policies) { pols_.push_back(p); pol_scen_.push_back((int)k); }
 		ScenDesc& D = scen_[k];
 		D.world = sc.world; D.width = sc.width; D.height = sc.height; D.dt = sc.dt;
 		float mr = 0;
@@ -1493,6 +1676,8 @@ bool Engine::configure()
 	if (smem > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	}
 	mode_ = 1;
 	for (const auto& p : pols_) {
@@ -1530,7 +1715,10 @@ void Engine::enqueue_step()
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
-	if (mode_ == 1) k_agent<1><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	if (S.tape_list) {
+		if (mode_ == 1) k_agent<1, true><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+		else k_agent<0, true><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	} else if (mode_ == 1) k_agent<1><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
 	else k_agent<0><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
@@ -1955,10 +2143,256 @@ bool Engine::autotune(int trial_steps, EngineOptions* chosen)
 void* Engine::device_positions() const { return d_->pos; }
 void* Engine::device_velocities() const { return d_->vel; }
 
+// ------------------------------------------------------------------------
+// differentiable form (host)
+// ------------------------------------------------------------------------
+bool Engine::set_force_params(int scen, const float* p4)
+{
+	if (!sync()) return false;
+	if (scen >= (int)scen_.size()) { err_ = "no scenario " + std::to_string(scen); return false; }
+	for (size_t pi = 0; pi < pols_.size(); ++pi) {
+		if (scen >= 0 && pol_scen_[pi] != scen) continue;
+		PolicyDesc& P = pols_[pi];
+		for (int c = 0; c < P.ncost; ++c) {
+			CostDesc& C = P.cost[c];
+			bool changed = false;
+			auto put = [&](int k, float v) { if (!std::isnan(v)) { C.p[k] = v; changed = true; } };
+			if (C.kind == K_SOCIALFORCES) { put(1, p4[0]); put(2, p4[1]); }
+			else if (C.kind == K_POWERLAW) { put(0, p4[2]); put(1, p4[3]); }
+			if (!changed) continue;
+			char* dst = (char*)d_->pols + pi * sizeof(PolicyDesc) + offsetof(PolicyDesc, cost) + c * sizeof(CostDesc) +
+			            offsetof(CostDesc, p);
+			CK(cudaMemcpy(dst, C.p, sizeof(C.p), cudaMemcpyHostToDevice));
+		}
+	}
+	return true;
+}
+
+bool Engine::get_force_params(int scen, float* p4)
+{
+	if (scen < 0 || scen >= (int)scen_.size()) { err_ = "no scenario " + std::to_string(scen); return false; }
+	for (int k = 0; k < 4; ++k) p4[k] = NAN;
+	for (size_t pi = 0; pi < pols_.size(); ++pi) {
+		if (pol_scen_[pi] != scen) continue;
+		const PolicyDesc& P = pols_[pi];
+		for (int c = 0; c < P.ncost; ++c) {
+			const CostDesc& C = P.cost[c];
+			if (C.kind == K_SOCIALFORCES && std::isnan(p4[0])) { p4[0] = C.p[1]; p4[1] = C.p[2]; }
+			if (C.kind == K_POWERLAW && std::isnan(p4[2])) { p4[2] = C.p[0]; p4[3] = C.p[1]; }
+		}
+	}
+	return true;
+}
+
+void Engine::diff_free()
+{
+	Diff& D = df_;
+	void* ptrs[] = { D.s0_pos, D.s0_vel, D.s0_view, D.s0_vwf, D.s0_rng, D.targets, D.ck_pos, D.ck_vel, D.seg_pos,
+	                 D.seg_vel, D.seg_acc, D.tape, D.tape_cnt, D.lam_p, D.lam_v, D.lo_p, D.lo_v, D.dparams, D.loss };
+	for (void* p : ptrs)
+		if (p) cudaFree(p);
+	D = Diff();
+}
+
+void Engine::diff_end()
+{
+	if (stream_) cudaStreamSynchronize(stream_);
+	diff_free();
+}
+
+bool Engine::diff_begin(int steps, int every, const float* targets, float weight)
+{
+	if (!sync()) return false;
+	diff_free();
+	if (steps <= 0 || every <= 0) { err_ = "steps and checkpoint interval must be positive"; return false; }
+	if (!pending_.empty() || any_remove_at_goal_) {
+		err_ = "the differentiable form needs a fixed agent set (no delayed starts, no removal at the goal)";
+		return false;
+	}
+	for (size_t pi = 0; pi < pols_.size(); ++pi) {
+		const PolicyDesc& P = pols_[pi];
+		bool ok = P.method == M_GRADIENT;
+		for (int c = 0; c < P.ncost; ++c) {
+			const int k = P.cost[c].kind;
+			ok &= k == K_SOCIALFORCES || k == K_POWERLAW || k == K_GOALREACHING;
+		}
+		if (!ok) {
+			err_ = "the differentiable form supports gradient-method policies made of SocialForcesAvoidance, "
+			       "PowerLaw and GoalReachingForce only";
+			return false;
+		}
+	}
+	Diff& D = df_;
+	const int n = n_;
+	D.steps = steps; D.every = std::min(every, steps); D.n = n;
+	D.nck = (steps + D.every - 1) / D.every;
+	D.weight = weight > 0 ? weight : (float)(1.0 / ((double)steps * std::max(n, 1)));
+	const size_t nn = std::max(n, 1);
+	if (!dalloc(D.s0_pos, nn, err_) || !dalloc(D.s0_vel, nn, err_) || !dalloc(D.s0_view, nn, err_) ||
+	    !dalloc(D.s0_vwf, nn, err_) || !dalloc(D.s0_rng, nn, err_) || !dalloc(D.targets, nn * steps, err_) ||
+	    !dalloc(D.ck_pos, nn * D.nck, err_) || !dalloc(D.ck_vel, nn * D.nck, err_) ||
+	    !dalloc(D.seg_pos, nn * (D.every + 1), err_) || !dalloc(D.seg_vel, nn * (D.every + 1), err_) ||
+	    !dalloc(D.seg_acc, nn * D.every, err_) || !dalloc(D.tape_cnt, nn * D.every, err_) ||
+	    !dalloc(D.lam_p, nn, err_) || !dalloc(D.lam_v, nn, err_) || !dalloc(D.lo_p, nn, err_) ||
+	    !dalloc(D.lo_v, nn, err_) || !dalloc(D.dparams, 4 * scen_.size(), err_) || !dalloc(D.loss, 1, err_)) {
+		diff_free();
+		return false;
+	}
+	const DevState& S = *d_;
+	if (n > 0) {
+		CK(cudaMemcpy(D.targets, targets, sizeof(float2) * (size_t)n * steps, cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(D.s0_pos, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice));
+		CK(cudaMemcpy(D.s0_vel, S.vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice));
+		CK(cudaMemcpy(D.s0_view, S.view, sizeof(float2) * n, cudaMemcpyDeviceToDevice));
+		CK(cudaMemcpy(D.s0_vwf, S.vwf, sizeof(float2) * n, cudaMemcpyDeviceToDevice));
+		CK(cudaMemcpy(D.s0_rng, S.rng, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice));
+	}
+	D.t0 = time_;
+	D.times0 = times_;
+	return true;
+}
+
+bool Engine::diff_restore_start()
+{
+	Diff& D = df_;
+	const DevState& S = *d_;
+	if (D.n > 0) {
+		CK(cudaMemcpyAsync(S.pos, D.s0_pos, sizeof(float2) * D.n, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.vel, D.s0_vel, sizeof(float2) * D.n, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.view, D.s0_view, sizeof(float2) * D.n, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.vwf, D.s0_vwf, sizeof(float2) * D.n, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.rng, D.s0_rng, sizeof(uint32_t) * D.n, cudaMemcpyDeviceToDevice, stream_));
+	}
+	time_ = D.t0;
+	times_ = D.times0;
+	return true;
+}
+
+// Waits for the stream; true when no device condition was raised.  A
+// neighbour-capacity overflow is reported through *overflow (the caller
+// re-runs with a doubled capacity).
+bool Engine::diff_check_status()
+{
+	CK(cudaStreamSynchronize(stream_));
+	int st = 0;
+	CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
+	if (st == 0) return true;
+	CK(cudaMemset(d_->status, 0, sizeof(int)));
+	if ((st & ST_NEIGHBOUR_OVERFLOW) && maxnb_ < 3072) {
+		maxnb_ = std::min(3072, maxnb_ * 2);
+		invalidate_graph();
+		err_ = "overflow";
+		return false;
+	}
+	if (st & ST_NEIGHBOUR_OVERFLOW) err_ = "a neighbour list is longer than " + std::to_string(maxnb_) + " entries";
+	else if (st & ST_GRID_OVERFLOW) err_ = "non-finite agent positions";
+	else err_ = "device status " + std::to_string(st);
+	return false;
+}
+
+bool Engine::diff_forward(double* loss)
+{
+	Diff& D = df_;
+	if (D.steps == 0) { err_ = "no differentiable episode (call diff_begin first)"; return false; }
+	if (!sync()) return false;
+	D.forward_done = false;
+	const int n = D.n;
+	for (;;) {
+		if (!diff_restore_start()) return false;
+		if (configured_maxnb_ != maxnb_ && !configure()) return false;
+		CK(cudaMemsetAsync(D.loss, 0, sizeof(double), stream_));
+		for (int t = 0; t < D.steps; ++t) {
+			if (t % D.every == 0 && n > 0) {
+				const size_t c = (size_t)(t / D.every) * n;
+				CK(cudaMemcpyAsync(D.ck_pos + c, d_->pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+				CK(cudaMemcpyAsync(D.ck_vel + c, d_->vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+			}
+			if (!run_steps(1)) return false;
+			if (n > 0) k_loss<<<(n + 255) / 256, 256, 0, stream_>>>(*d_, D.targets + (size_t)t * n, D.weight, D.loss);
+		}
+		CK(cudaGetLastError());
+		if (diff_check_status()) break;
+		if (err_ != "overflow") return false;
+	}
+	D.forward_done = true;
+	if (loss) CK(cudaMemcpy(loss, D.loss, sizeof(double), cudaMemcpyDeviceToHost));
+	return true;
+}
+
+bool Engine::diff_alloc_tape()
+{
+	Diff& D = df_;
+	if (D.tape && D.tape_nb == maxnb_) return true;
+	if (D.tape) cudaFree(D.tape);
+	D.tape = nullptr;
+	D.tape_nb = maxnb_;
+	return dalloc(D.tape, (size_t)std::max(D.n, 1) * D.every * maxnb_, err_);
+}
+
+bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
+{
+	Diff& D = df_;
+	if (!D.forward_done) { err_ = "diff_backward needs a completed diff_forward"; return false; }
+	if (!diff_alloc_tape()) return false;
+	DevState& S = *d_;
+	const int n = D.n;
+	const size_t nb2 = sizeof(float2) * std::max(n, 1);
+	CK(cudaMemsetAsync(D.lam_p, 0, nb2, stream_));
+	CK(cudaMemsetAsync(D.lam_v, 0, nb2, stream_));
+	CK(cudaMemsetAsync(D.dparams, 0, sizeof(float) * 4 * scen_.size(), stream_));
+	const int adj_blocks = std::max(1, std::min((n + 3) / 4, num_sms_ * 16));
+	for (int c = D.nck - 1; c >= 0 && n > 0; --c) {
+		const int t0 = c * D.every, m = std::min(D.every, D.steps - t0);
+		// recompute the segment from its checkpoint, recording lists and states
+		CK(cudaMemcpyAsync(S.pos, D.ck_pos + (size_t)c * n, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+		CK(cudaMemcpyAsync(S.vel, D.ck_vel + (size_t)c * n, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+		for (int s = 0; s < m; ++s) {
+			CK(cudaMemcpyAsync(D.seg_pos + (size_t)s * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+			CK(cudaMemcpyAsync(D.seg_vel + (size_t)s * n, S.vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+			S.tape_list = D.tape + (size_t)s * n * maxnb_;
+			S.tape_cnt = D.tape_cnt + (size_t)s * n;
+			S.tape_acc = D.seg_acc + (size_t)s * n;
+			enqueue_step();
+			S.tape_list = nullptr; S.tape_cnt = nullptr; S.tape_acc = nullptr;
+		}
+		CK(cudaMemcpyAsync(D.seg_pos + (size_t)m * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+		// reverse the segment
+		for (int s = m - 1; s >= 0; --s) {
+			k_inject<<<(n + 255) / 256, 256, 0, stream_>>>(n, D.seg_pos + (size_t)(s + 1) * n,
+			                                               D.targets + (size_t)(t0 + s) * n, D.weight, D.lam_p,
+			                                               D.lam_v, D.lo_p, D.lo_v);
+			CK(cudaMemsetAsync(D.lam_p, 0, nb2, stream_));
+			CK(cudaMemsetAsync(D.lam_v, 0, nb2, stream_));
+			DevState A = S;
+			A.tape_list = D.tape + (size_t)s * n * maxnb_;
+			A.tape_cnt = D.tape_cnt + (size_t)s * n;
+			A.tape_acc = D.seg_acc + (size_t)s * n;
+			A.a_pos = D.seg_pos + (size_t)s * n;
+			A.a_vel = D.seg_vel + (size_t)s * n;
+			A.lam_out_p = D.lo_p; A.lam_out_v = D.lo_v;
+			A.lam_in_p = D.lam_p; A.lam_in_v = D.lam_v;
+			A.dparams = D.dparams;
+			k_adjoint<<<adj_blocks, 128, 0, stream_>>>(A);
+		}
+	}
+	CK(cudaGetLastError());
+	if (!diff_check_status()) {
+		if (err_ == "overflow") err_ = "neighbour lists of the recomputed segment outgrew the capacity";
+		return false;
+	}
+	if (dparams) CK(cudaMemcpy(dparams, D.dparams, sizeof(float) * 4 * scen_.size(), cudaMemcpyDeviceToHost));
+	if (dpos0 && n > 0) CK(cudaMemcpy(dpos0, D.lam_p, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+	if (dvel0 && n > 0) CK(cudaMemcpy(dvel0, D.lam_v, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+	if (!diff_restore_start()) return false;
+	CK(cudaStreamSynchronize(stream_));
+	return true;
+}
+
 Engine::~Engine()
 {
 	if (stream_) cudaStreamSynchronize(stream_);
 	invalidate_graph();
+	diff_free();
 	if (d_) {
 		DevState& S = *d_;
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,

@@ -89,6 +89,29 @@ public:
 	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; }
 	int kernels_per_step() const;
 
+	// ---- differentiable form ------------------------------------------
+	// Episode: `steps` steps from the current state (recorded as the
+	// episode's start), loss L = weight * sum_t sum_i |p_i(t) - target_i(t)|^2
+	// over t = 1..steps (targets: steps x n x 2 floats, list order; weight
+	// <= 0 means 1 / (steps * n)).  Checkpoints every `every` steps; the
+	// backward pass recomputes each segment from its checkpoint with the
+	// neighbour lists recorded and reverses it with k_adjoint.  Every policy
+	// must use the gradient method with SocialForcesAvoidance, PowerLaw and
+	// GoalReachingForce costs only; agents are neither added nor removed.
+	bool diff_begin(int steps, int every, const float* targets, float weight);
+	bool diff_forward(double* loss);   // from the episode's start state
+	// dparams: [num_scenarios x 4] dL/d(V0, sigma, k, tau0); dpos0/dvel0:
+	// [n x 2] dL/d(initial positions, velocities) (each may be null).  The
+	// state is then the episode's start state again.
+	bool diff_backward(float* dparams, float* dpos0, float* dvel0);
+	void diff_end();
+	// (V0, sigma) of the SocialForcesAvoidance costs and (k, tau0) of the
+	// PowerLaw costs of scenario `scen` (all scenarios when scen < 0); NaN
+	// entries are left unchanged.  get: NaN where the scenario has no such cost.
+	bool set_force_params(int scen, const float* p4);
+	bool get_force_params(int scen, float* p4);
+	int diff_kernels_forward_per_step() const { return kernels_per_step() + 1; }
+
 private:
 	Engine() = default;
 	bool init(const std::vector<std::string>& xmls, const EngineOptions& opt);
@@ -149,6 +172,30 @@ private:
 	double snap_time_ = 0;
 	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
 	int prof_steps_ = 0;
+	std::vector<int> pol_scen_;   // scenario of each policy
+
+	// differentiable form (device buffers; see diff_begin)
+	struct Diff {
+		int steps = 0, every = 0, nck = 0, n = 0, tape_nb = 0;
+		float weight = 0;
+		bool forward_done = false;
+		double t0 = 0;
+		std::vector<double> times0;
+		float2 *s0_pos = nullptr, *s0_vel = nullptr, *s0_view = nullptr, *s0_vwf = nullptr;
+		uint32_t* s0_rng = nullptr;
+		float2* targets = nullptr;                   // steps x n
+		float2 *ck_pos = nullptr, *ck_vel = nullptr;   // nck x n
+		float2 *seg_pos = nullptr, *seg_vel = nullptr, *seg_acc = nullptr;   // (every + 1) x n
+		uint32_t* tape = nullptr;                    // every x n x tape_nb
+		int* tape_cnt = nullptr;                     // every x n
+		float2 *lam_p = nullptr, *lam_v = nullptr, *lo_p = nullptr, *lo_v = nullptr;
+		float* dparams = nullptr;
+		double* loss = nullptr;
+	} df_;
+	bool diff_restore_start();
+	bool diff_alloc_tape();
+	bool diff_check_status();
+	void diff_free();
 };
 
 }  // namespace umans
