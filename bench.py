@@ -47,11 +47,15 @@ SF_FLOP_PER_PAIR = 67
 SF_FLOP_PER_AGENT = 40
 
 
-def workload(name: str, tmp: str):
+def workload(name: str, tmp: str, agents: int = 0):
+    """agents > 0 scales the SocialForces workload at the same density
+    (smaller cases for profiler captures)."""
     from umans_gb300 import scenarios as S
     if name == "socialforces_toric":
-        sc = S.socialforces_toric()
-        cfg = dict(workload="socialforces_toric", agents=100_000, world="toric 400x400 m",
+        n = agents or 100_000
+        sc = S.socialforces_toric(n, density=100_000 / 400.0 ** 2) if agents else S.socialforces_toric()
+        side = math.sqrt(n / (100_000 / 400.0 ** 2))
+        cfg = dict(workload="socialforces_toric", agents=n, world=f"toric {side:.0f}x{side:.0f} m",
                    policy="SocialForcesAvoidance(range 5)+GoalReachingForce, gradient", dt=0.1)
     elif name == "karamouzas_corridor":
         sc = S.karamouzas_corridor()
@@ -287,7 +291,7 @@ def run_reference(args):
     if rank != 0:
         return
     with tempfile.TemporaryDirectory() as tmp:
-        path, n, cfg = workload(args.workload, tmp)
+        path, n, cfg = workload(args.workload, tmp, args.agents)
         threads = os.cpu_count() or 1
         from oracle import ref as oref
         if oref.available():
@@ -316,7 +320,7 @@ def run_ours(args):
     import torch
     torch.cuda.set_device(local)
     with tempfile.TemporaryDirectory() as tmp:
-        path, n, cfg = workload(args.workload, tmp)
+        path, n, cfg = workload(args.workload, tmp, args.agents)
         sim = Simulation(path)
         stream = torch.cuda.ExternalStream(sim.stream)
         flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -391,7 +395,7 @@ def run_ours(args):
         e2e_value = world * n * args.steps / te
         cpu = cpu_baseline(path, n) if (rank == 0 and world == 1 and not args.no_cpu) else None
         batched = None if args.no_batch else batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
-        diff = None if args.no_diff else diff_leg(tmp)
+        diff = None if args.no_diff else diff_leg(tmp, sets=args.diff_sets)
     if rank != 0:
         return
     cfg = dict(cfg, l2="flushed (256 MiB write) before every timed step; state ~10 MB would fit in L2",
@@ -433,6 +437,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form leg")
+    ap.add_argument("--agents", type=int, default=0,
+                    help="agents of the SocialForces workload at the same density (default 100000)")
+    ap.add_argument("--diff-sets", type=int, default=256, help="parameter sets of the differentiable leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

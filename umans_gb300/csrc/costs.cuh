@@ -23,13 +23,23 @@ struct NbView {
 	const float2* sV;        // cell-sorted velocities
 	const float4* sB;        // cell-sorted (pref.x, pref.y, radius, -)
 	const float4* sE;        // cell-sorted (normalised pref.x, pref.y, speed, -)
-	float2 off[5];           // PhantomAgent offsets per displacement group
+	float W, H;              // toric world size (PhantomAgent offsets)
 };
+
+// PhantomAgent position offset of displacement group g (worldToric.cpp:61-79):
+// 0 none, 1 (-W, -0), 2 (W, -0), 3 (-0, -H), 4 (-0, H).  Selected in
+// registers (an indexed table would live in local memory).
+UD float2 group_offset(uint32_t g, float W, float H)
+{
+	const float ox = g == 1 ? -W : (g == 2 ? W : (g == 0 ? 0.0f : -0.0f));
+	const float oy = g == 3 ? -H : (g == 4 ? H : (g == 0 ? 0.0f : -0.0f));
+	return V(ox, oy);
+}
 
 UD float2 nb_pos(const NbView& N, int k)
 {
 	const uint32_t r = N.ref[k];
-	return vadd(N.sP[r & 0x0FFFFFFFu], N.off[r >> 28]);
+	return vadd(N.sP[r & 0x0FFFFFFFu], group_offset(r >> 28, N.W, N.H));
 }
 UD float2 nb_vel(const NbView& N, int k) { return N.sV[N.ref[k] & 0x0FFFFFFFu]; }
 UD float nb_radius(const NbView& N, int k) { return N.sB[N.ref[k] & 0x0FFFFFFFu].z; }

@@ -81,28 +81,38 @@ UD float vcosangle(float2 a, float2 b)
 	return vdot(a, b) / lf;
 }
 
-// angle(a, b) > thr, with cos_thr = cos(thr) to within 1e-7.  angle() is
-// never negative and returns 0 for zero-length inputs or |frac| > 1.
+// angle(a, b) > thr, with cos_thr = cos(thr) to within 1e-7 and thr below
+// 178 degrees.  angle() is never negative and returns 0 for zero-length
+// inputs or |frac| > 1.  For nearly opposite vectors (c <= -0.9999) angle()
+// is either about 180 degrees (> thr) or, when the double quotient
+// frac = dot / lengths falls below -1, exactly 0; with dot and lengths both
+// floats, frac < -1 holds exactly when -dot > lengths (two distinct floats
+// differ by at least 2^-24 relative, far above the double rounding of the
+// quotient), so no double arithmetic is needed there.
 UD bool angle_greater(float2 a, float2 b, float thr, float cos_thr)
 {
 	if (thr < 0) return true;
 	const float lf = vmag(a) * vmag(b);
 	if (lf == 0) return false;
-	const float c = vdot(a, b) / lf;
+	const float d = vdot(a, b);
+	const float c = d / lf;
 	if (c > cos_thr + 1e-6f) return false;                   // clearly smaller (or frac > 1)
 	if (c < cos_thr - 1e-6f && c > -0.9999f) return true;    // clearly larger
+	if (c <= -0.9999f) return !(-d > lf);
 	return vangle_exact(a, b) > thr;
 }
 
-// angle(a, b) < thr
+// angle(a, b) < thr (same conditions)
 UD bool angle_less(float2 a, float2 b, float thr, float cos_thr)
 {
 	if (thr <= 0) return false;
 	const float lf = vmag(a) * vmag(b);
 	if (lf == 0) return true;
-	const float c = vdot(a, b) / lf;
+	const float d = vdot(a, b);
+	const float c = d / lf;
 	if (c > cos_thr + 1e-6f) return true;
 	if (c < cos_thr - 1e-6f && c > -0.9999f) return false;
+	if (c <= -0.9999f) return -d > lf;
 	return vangle_exact(a, b) < thr;
 }
 

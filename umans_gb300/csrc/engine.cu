@@ -577,10 +577,9 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : 1e-6f);
 	}
 	// PhantomAgent position offset = -displacement; distSqr in float
-	const float2 off[5] = { V(0, 0), V(-W, -0.0f), V(W, -0.0f), V(-0.0f, -H), V(-0.0f, H) };
 	for (int k = lane; k < K; k += 32) {
 		const uint32_t rr = L.ref[k];
-		const float2 ph = vadd(S.sP[rr & 0x0FFFFFFFu], off[rr >> 28]);
+		const float2 ph = vadd(S.sP[rr & 0x0FFFFFFFu], group_offset(rr >> 28, W, H));
 		L.key[k] = vsq(vsub(p, ph));
 	}
 	__syncwarp();
@@ -949,8 +948,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		const int K = gather(S, G, S.cell_base[sc], sd.world, sd.width, sd.height, L, t, A.pos, pol.range, lane, &overflow);
 		NbView N;
 		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB; N.sE = S.sE;
-		N.off[0] = V(0, 0); N.off[1] = V(-sd.width, -0.0f); N.off[2] = V(sd.width, -0.0f);
-		N.off[3] = V(-0.0f, -sd.height); N.off[4] = V(-0.0f, sd.height);
+		N.W = sd.width; N.H = sd.height;
 
 		if (dump) {
 			const int cap = S.dump_cap;
@@ -1182,8 +1180,6 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 		A.pref = at_goal ? v2(0, 0) : vmul(vnorm(w), A.prefspeed);
 		const int K = S.tape_cnt[i];
 		const uint32_t* list = S.tape_list + (size_t)i * S.maxnb;
-		const float2 off[5] = { v2(0, 0), v2(-sd.width, -0.0f), v2(sd.width, -0.0f), v2(-0.0f, -sd.height),
-		                        v2(-0.0f, sd.height) };
 		// a = sum coeff F / m (ForceBasedFunction::GetGradient with policy.cpp:78-89)
 		// (the forward step recorded a before the clamp)
 		float2 lF[MAX_COSTS];
@@ -1211,7 +1207,7 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 			for (int k = lane; k < K; k += 32) {
 				const uint32_t e = list[k];
 				const int j = (int)(e & 0x0FFFFFFFu);
-				const float2 pj = add2(S.a_pos[j], off[e >> 28]);
+				const float2 pj = add2(S.a_pos[j], group_offset(e >> 28, sd.width, sd.height));
 				if (dot2(sub2(A.pos, pj), sub2(A.pos, pj)) > rs) continue;
 				const float2 vj = S.a_vel[j];
 				const float rj = S.prm[j].x;
@@ -1245,7 +1241,7 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 			for (int k = lane; k < K; k += 32) {
 				const uint32_t e = list[k];
 				const int j = (int)(e & 0x0FFFFFFFu);
-				const float2 D = sub2(A.pos, add2(S.a_pos[j], off[e >> 28]));
+				const float2 D = sub2(A.pos, add2(S.a_pos[j], group_offset(e >> 28, sd.width, sd.height)));
 				const float2 lD = contact_adj(D, A.radius + S.prm[j].x, pol.contact_scale, lC);
 				if (lD.x != 0 || lD.y != 0) {
 					lpi = add2(lpi, lD);
