@@ -359,16 +359,19 @@ __device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
 	}
 }
 
-// Sort of [s, s+len), len <= 128, in registers: each lane holds up to 4
-// packed keys (float key bits with the low PB bits replaced by the position
-// in the segment; positive floats order like their bit patterns) and a
-// shuffle bitonic network sorts them; the entries are then permuted.  Keys
-// that agree above the low PB bits may come out in either order: the
-// near-tie pass that follows (relative window 2^-16, wider than the 2^-17
-// truncation)
-// re-orders them with the exact double distance and the id.
+// Sort of [s, s+len), len <= 32 * M (M = 1, 2, 4), in registers: each lane
+// holds M packed keys (float key bits with the low PB bits replaced by the
+// position in the segment; positive floats order like their bit patterns)
+// and a shuffle bitonic network sorts them.  The entries are then permuted
+// through registers holding only the references: the key and the id of an
+// entry are recomputed from its reference exactly as the gather computed
+// them (same expression, same operands).  Keys that agree above the low PB
+// bits may come out in either order: the near-tie pass that follows
+// (relative window 2^(PB-22), twice the 2^(PB-23) truncation) re-orders
+// them with the exact double distance and the id.
 template <int M>
-__device__ __forceinline__ void warp_sort_regs(const WarpLists& L, int s, int len, int lane)
+__device__ __forceinline__ void warp_sort_regs(const DevState& S, const WarpLists& L, int s, int len, int lane,
+                                               float2 q)
 {
 	constexpr int PB = (M == 1) ? 5 : (M == 2) ? 6 : 7;
 	constexpr uint32_t PMASK = (1u << PB) - 1u;
@@ -404,22 +407,23 @@ __device__ __forceinline__ void warp_sort_regs(const WarpLists& L, int s, int le
 			}
 		}
 	}
-	uint32_t r[M];
-	float k[M];
-	int d[M];
 #pragma unroll
 	for (int m = 0; m < M; ++m) {
 		const int i = m * 32 + lane;
-		if (i < len) {
-			const int src = s + (int)(u[m] & PMASK);
-			r[m] = L.ref[src]; k[m] = L.key[src]; d[m] = L.nid[src];
-		}
+		u[m] = (i < len) ? L.ref[s + (int)(u[m] & PMASK)] : 0u;
 	}
 	__syncwarp();
 #pragma unroll
 	for (int m = 0; m < M; ++m) {
 		const int i = m * 32 + lane;
-		if (i < len) { L.ref[s + i] = r[m]; L.key[s + i] = k[m]; L.nid[s + i] = d[m]; }
+		if (i < len) {
+			const int tt = (int)(u[m] & 0x0FFFFFFFu);
+			const float2 cp = S.sP[tt];
+			const float dx = q.x - cp.x, dy = q.y - cp.y;
+			L.ref[s + i] = u[m];
+			L.key[s + i] = dx * dx + dy * dy;
+			L.nid[s + i] = S.sId[tt];
+		}
 	}
 	__syncwarp();
 }
@@ -433,9 +437,9 @@ __device__ __forceinline__ double exact_key(float2 q, float2 c)
 }
 
 // Float keys order the list except within runs of near-equal keys (relative
-// gap <= win: 1e-6 after the exact-key sort, 2^-16 after the packed-key
-// register sort), whose order is settled with the reference's double
-// distance (then id).  Runs are rare; lane 0 handles them.
+// gap <= win: 1e-6 after the exact-key sort, 2^-16 or 2^-15 after the
+// packed-key register sorts), whose order is settled with the reference's
+// double distance (then id).  Runs are rare; lane 0 handles them.
 __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane, float win)
 {
 	bool close = false;
@@ -571,10 +575,11 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 		if (K > maxnb) { *overflow = true; K = maxnb; }
 		__syncwarp();
 		const int len = K - gs;
-		if (len <= 32) warp_sort_regs<1>(L, gs, len, lane);
-		else if (len <= 64) warp_sort_regs<2>(L, gs, len, lane);
+		if (len <= 32) warp_sort_regs<1>(S, L, gs, len, lane, q);
+		else if (len <= 64) warp_sort_regs<2>(S, L, gs, len, lane, q);
+		else if (len <= 128) warp_sort_regs<4>(S, L, gs, len, lane, q);
 		else warp_sort(L, gs, len, lane);
-		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : 1e-6f);
+		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : (len <= 128 ? 0x1p-15f : 1e-6f));
 	}
 	// PhantomAgent position offset = -displacement; distSqr in float
 	for (int k = lane; k < K; k += 32) {
