@@ -378,17 +378,21 @@ def run_ours(args):
         lib.GetAgentPositions(C.byref(ptr), C.byref(cnt_c))
         host = (_lib.AgentData * n)()
         C.memmove(host, ptr, C.sizeof(_lib.AgentData) * n)
+        # each step sends the previous step's records back (the buffer
+        # GetAgentPositions returned, a host buffer owned by the library)
+        cur = host
         for _ in range(args.warmup):
-            lib.SetAgentPositions(host, n)
+            lib.SetAgentPositions(cur, n)
             lib.DoSimulationSteps(1)
             lib.GetAgentPositions(C.byref(ptr), C.byref(cnt_c))
+            cur = ptr
         barrier(dist)
         te = time.perf_counter()
         for _ in range(args.steps):
-            lib.SetAgentPositions(host, n)
+            lib.SetAgentPositions(cur, n)
             lib.DoSimulationSteps(1)
             lib.GetAgentPositions(C.byref(ptr), C.byref(cnt_c))
-            C.memmove(host, ptr, C.sizeof(_lib.AgentData) * n)
+            cur = ptr
         te = time.perf_counter() - te
         te = max_over_ranks(dist, te)
         u.cleanUp()

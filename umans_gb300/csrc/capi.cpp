@@ -346,13 +346,35 @@ const char* umans_last_error(umans_sim* s)
 // reference-compatible global interface (src/Library/APIFunctions.cpp)
 // ---------------------------------------------------------------------------
 static umans_sim* g_sim = nullptr;
-static std::vector<AgentData> g_agent_data;
+// the AgentData buffer GetAgentPositions hands out (library-owned, valid
+// until the next resize or CleanUp), page-locked so that the device writes
+// it directly
+struct AgentBuffer {
+	AgentData* p = nullptr;
+	size_t cap = 0;
+	size_t size() const { return cap; }
+	AgentData* data() { return p; }
+	void release()
+	{
+		if (p) cudaFreeHost(p);
+		p = nullptr;
+		cap = 0;
+	}
+};
+static AgentBuffer g_agent_data;
 
 // resizeAgentData: APIFunctions.cpp:37-45 (power-of-two capacity)
-static void resize_agent_data(size_t n)
+static bool resize_agent_data(size_t n)
 {
 	size_t cap = (size_t)std::pow(2, 1 + (int)std::ceil(std::log2((double)std::max<size_t>(n, 1))));
-	g_agent_data.assign(cap, AgentData{});
+	g_agent_data.release();
+	if (cudaMallocHost(&g_agent_data.p, sizeof(AgentData) * cap) != cudaSuccess) {
+		g_agent_data.p = nullptr;
+		return false;
+	}
+	std::memset(g_agent_data.p, 0, sizeof(AgentData) * cap);
+	g_agent_data.cap = cap;
+	return true;
 }
 
 bool StartSimulation(const char* configFileName, int nrThreads)
@@ -384,7 +406,7 @@ bool GetAgentPositions(AgentData** result_agentData, int* result_nrAgents)
 {
 	if (!g_sim || !result_agentData || !result_nrAgents) return false;
 	const size_t n = (size_t)g_sim->eng->num_agents();
-	if (n > g_agent_data.size() || n * 4 < g_agent_data.size()) resize_agent_data(n);
+	if ((n > g_agent_data.size() || n * 4 < g_agent_data.size()) && !resize_agent_data(n)) return false;
 	if (!g_sim->eng->get_agent_data(g_agent_data.data())) return false;
 	*result_agentData = g_agent_data.data();
 	*result_nrAgents = (int)n;
@@ -427,8 +449,7 @@ bool CleanUp(void)
 	if (!g_sim) return false;
 	umans_destroy(g_sim);
 	g_sim = nullptr;
-	g_agent_data.clear();
-	g_agent_data.shrink_to_fit();
+	g_agent_data.release();
 	return true;
 }
 

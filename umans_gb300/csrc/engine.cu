@@ -72,6 +72,7 @@ struct DevState {
 	const float2 *lam_out_p, *lam_out_v;
 	float2 *lam_in_p, *lam_in_v;
 	float2* tape_acc;     // [n]: acceleration before the clamp (gradient method)
+	float4* adj_nb;       // [n]: Eb, 1/|goal - pos|, speed (k_adj_prep)
 	float* dparams;       // [nscen * 4]: dL/d(V0, sigma, k, tau0)
 	int* slot_of_id;      // id -> list slot, -1 when absent
 	int id_bound;         // size of slot_of_id
@@ -1147,16 +1148,34 @@ bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::st
 // quantities are recomputed, then the adjoints of the agent's new position
 // and velocity are propagated to its own state, its neighbours' states
 // (atomicAdd) and the scenario's parameters (V0, sigma, k, tau0).
-// the neighbour's normalised preferred velocity, as the scatter computes it
-// from the adjoint pass's state
-__device__ __forceinline__ float2 goal_dir(const DevState& S, int j)
+// Per-agent terms that the neighbours' adjoints read, from the state at the
+// start of the step being reversed: the normalised goal direction Eb (as the
+// scatter computes it for SocialForcesAvoidance), 1/|goal - pos| (0 at the
+// goal: Eb is then constant) and the speed.
+__global__ void k_adj_prep(DevState S)
 {
-	const float2 d = vsub(S.goal[j], S.a_pos[j]);
-	const float4 prm = S.prm[j];
-	if (vsq(d) <= prm.x * prm.x) return V(0, 0);
-	return vnorm(vmul(vnorm(d), prm.y));
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= S.n) return;
+	const float2 d = vsub(S.goal[i], S.a_pos[i]);
+	const float4 prm = S.prm[i];
+	const float2 v = S.a_vel[i];
+	float2 eb = V(0, 0);
+	float invw = 0;
+	if (!(vsq(d) <= prm.x * prm.x)) {
+		eb = vnorm(vmul(vnorm(d), prm.y));
+		if (!viszero(eb)) invw = 1.0f / vmag(d);
+	}
+	S.adj_nb[i] = make_float4(eb.x, eb.y, invw, vmag(v));
 }
 
+// Adjoint of one step for policies made of SocialForcesAvoidance, PowerLaw
+// and GoalReachingForce under the gradient method, with the neighbour lists
+// the forward step recorded.  One warp per agent (list order), one lane per
+// neighbour: the pair's force adjoints (every cost) and contact adjoint are
+// formed together, the agent's own terms summed over the warp, and the
+// neighbour's terms added to its adjoint with one atomic per nonzero
+// component.  The parameters' adjoints (V0, sigma, k, tau0) are summed per
+// scenario.
 __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 {
 	const int lane = threadIdx.x & 31;
@@ -1183,75 +1202,79 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 		const float2 w = sub2(A.goal, A.pos);
 		const bool at_goal = dot2(w, w) <= A.radius * A.radius;
 		A.pref = at_goal ? v2(0, 0) : vmul(vnorm(w), A.prefspeed);
+		const bool moving = !viszero(A.pref);
 		const int K = S.tape_cnt[i];
 		const uint32_t* list = S.tape_list + (size_t)i * S.maxnb;
-		// a = sum coeff F / m (ForceBasedFunction::GetGradient with policy.cpp:78-89)
-		// (the forward step recorded a before the clamp)
-		float2 lF[MAX_COSTS];
-		for (int c = 0; c < MAX_COSTS; ++c) lF[c] = v2(0, 0);
-		if (!viszero(A.pref)) {
+		// a = sum coeff F / m (ForceBasedFunction::GetGradient with
+		// policy.cpp:78-89); the forward step recorded a before the clamp
+		float2 la = v2(0, 0);
+		if (moving) {
 			const float2 a = S.tape_acc[i];
 			const float2 ac = vclamp(a, A.maxacc);
 			const float2 u = add2(A.vel, mul2(ac, dt));
 			const float2 lu = clamp_adj(u, A.maxspeed, lvn);
 			if (lane == 0) lvi = add2(lvi, lu);
-			const float2 la = clamp_adj(a, A.maxacc, mul2(lu, dt));
-			for (int c = 0; c < pol.ncost; ++c) lF[c] = mul2(la, pol.cost[c].coeff / pol.cost[c].p[5]);
+			la = clamp_adj(a, A.maxacc, mul2(lu, dt));
 		}
 		float2 lpref = v2(0, 0);
 		float dV0 = 0, dsig = 0, dk = 0, dtau0 = 0;
 		for (int c = 0; c < pol.ncost; ++c) {
 			const CostDesc& cd = pol.cost[c];
-			if (cd.kind == K_GOALREACHING) {
+			if (cd.kind == K_GOALREACHING && lane == 0) {
+				const float2 lF = mul2(la, cd.coeff / cd.p[5]);
 				const float mr = fmaxr(A.relax, dt);
-				if (lane == 0) { lpref = add2(lpref, mul2(lF[c], 1.0f / mr)); lvi = sub2(lvi, mul2(lF[c], 1.0f / mr)); }
-				continue;
+				lpref = add2(lpref, mul2(lF, 1.0f / mr));
+				lvi = sub2(lvi, mul2(lF, 1.0f / mr));
 			}
-			if (viszero(A.pref)) continue;
-			const float rs = cd.range * cd.range;
+		}
+		const bool contact = pol.contact_scale > 0;
+		if (moving || contact) {
 			for (int k = lane; k < K; k += 32) {
 				const uint32_t e = list[k];
 				const int j = (int)(e & 0x0FFFFFFFu);
 				const float2 pj = add2(S.a_pos[j], group_offset(e >> 28, sd.width, sd.height));
-				if (dot2(sub2(A.pos, pj), sub2(A.pos, pj)) > rs) continue;
-				const float2 vj = S.a_vel[j];
+				const float2 D = sub2(A.pos, pj);
+				const float d2 = dot2(D, D);
 				const float rj = S.prm[j].x;
 				float2 lpj = v2(0, 0), lvj = v2(0, 0);
-				if (cd.kind == K_SOCIALFORCES) {
-					const float2 wj = sub2(S.goal[j], S.a_pos[j]);
-					const float2 ebj = goal_dir(S, j);
-					const SfAdj r = sf_pair_adj(A, cd, pj, vj, ebj, rj, lF[c]);
-					lpi = add2(lpi, r.lR);
-					lpj = sub2(lpj, r.lR);
-					lvj = add2(lvj, r.lvj);
-					// Eb_j = (g_j - p_j)/|g_j - p_j| away from the goal
-					if (!viszero(ebj)) lpj = sub2(lpj, normalize_adj(wj, r.lEb));
-					dV0 += r.lV0;
-					dsig += r.lsigma;
-				} else {
-					const PlAdj r = pl_pair_adj(A, cd, pj, vj, rj, lF[c]);
-					lpi = add2(lpi, r.lx);
-					lpj = sub2(lpj, r.lx);
-					lvi = add2(lvi, r.lv);
-					lvj = sub2(lvj, r.lv);
-					dk += r.lk;
-					dtau0 += r.ltau0;
+				if (moving) {
+					const float2 vj = S.a_vel[j];
+					const float4 nb = S.adj_nb[j];
+					for (int c = 0; c < pol.ncost; ++c) {
+						const CostDesc& cd = pol.cost[c];
+						if (cd.kind == K_GOALREACHING || d2 > cd.range * cd.range) continue;
+						const float2 lF = mul2(la, cd.coeff / cd.p[5]);
+						if (cd.kind == K_SOCIALFORCES) {
+							const float2 ebj = v2(nb.x, nb.y);
+							const SfAdj r = sf_pair_adj(A, cd, pj, vj, ebj, rj, lF);
+							lpi = add2(lpi, r.lR);
+							lpj = sub2(lpj, r.lR);
+							lvj = add2(lvj, r.lvj);
+							// Eb_j = (g_j - p_j)/|g_j - p_j| away from the goal
+							lpj = sub2(lpj, mul2(sub2(r.lEb, mul2(ebj, dot2(ebj, r.lEb))), nb.z));
+							dV0 += r.lV0;
+							dsig += r.lsigma;
+						} else {
+							const PlAdj r = pl_pair_adj(A, cd, pj, vj, rj, lF);
+							lpi = add2(lpi, r.lx);
+							lpj = sub2(lpj, r.lx);
+							lvi = add2(lvi, r.lv);
+							lvj = sub2(lvj, r.lv);
+							dk += r.lk;
+							dtau0 += r.ltau0;
+						}
+					}
 				}
-				atomicAdd(&S.lam_in_p[j].x, lpj.x); atomicAdd(&S.lam_in_p[j].y, lpj.y);
-				atomicAdd(&S.lam_in_v[j].x, lvj.x); atomicAdd(&S.lam_in_v[j].y, lvj.y);
-			}
-		}
-		// contact forces (all neighbours): C = sum scale (rsum - |D|) D/|D|
-		if (pol.contact_scale > 0) {
-			for (int k = lane; k < K; k += 32) {
-				const uint32_t e = list[k];
-				const int j = (int)(e & 0x0FFFFFFFu);
-				const float2 D = sub2(A.pos, add2(S.a_pos[j], group_offset(e >> 28, sd.width, sd.height)));
-				const float2 lD = contact_adj(D, A.radius + S.prm[j].x, pol.contact_scale, lC);
-				if (lD.x != 0 || lD.y != 0) {
+				// contact forces (all neighbours): C = sum scale (rsum - |D|) D/|D|
+				if (contact) {
+					const float2 lD = contact_adj(D, A.radius + rj, pol.contact_scale, lC);
 					lpi = add2(lpi, lD);
-					atomicAdd(&S.lam_in_p[j].x, -lD.x); atomicAdd(&S.lam_in_p[j].y, -lD.y);
+					lpj = sub2(lpj, lD);
 				}
+				if (lpj.x != 0) atomicAdd(&S.lam_in_p[j].x, lpj.x);
+				if (lpj.y != 0) atomicAdd(&S.lam_in_p[j].y, lpj.y);
+				if (lvj.x != 0) atomicAdd(&S.lam_in_v[j].x, lvj.x);
+				if (lvj.y != 0) atomicAdd(&S.lam_in_v[j].y, lvj.y);
 			}
 		}
 		// warp sums (lane 0 also holds the goal-force terms)
@@ -1583,6 +1606,31 @@ bool Engine::upload_all()
 	return true;
 }
 
+// true when p is page-locked (or registered) host memory
+static bool is_pinned(const void* p)
+{
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeHost;
+}
+
+// Page-locked staging for AgentData exchange with pageable caller buffers:
+// a host copy into it plus a page-locked transfer beats the driver's
+// pageable path.
+bool Engine::stage(size_t records)
+{
+	if (records <= io_host_cap_) return true;
+	if (io_host_) cudaFreeHost(io_host_);
+	io_host_ = nullptr;
+	io_host_cap_ = 0;
+	CK(cudaMallocHost(&io_host_, sizeof(AgentRecord) * records));
+	io_host_cap_ = records;
+	return true;
+}
+
 bool Engine::get_agent_data(void* out)
 {
 	DevState& S = *d_;
@@ -1590,8 +1638,16 @@ bool Engine::get_agent_data(void* out)
 	if (n_ == 0) return true;
 	S.n = n_;
 	k_pack<<<(n_ + 255) / 256, 256, 0, stream_>>>(S);
-	CK(cudaMemcpyAsync(out, S.io, sizeof(AgentRecord) * n_, cudaMemcpyDeviceToHost, stream_));
+	const size_t bytes = sizeof(AgentRecord) * n_;
+	if (is_pinned(out)) {
+		CK(cudaMemcpyAsync(out, S.io, bytes, cudaMemcpyDeviceToHost, stream_));
+		CK(cudaStreamSynchronize(stream_));
+		return true;
+	}
+	if (!stage(n_)) return false;
+	CK(cudaMemcpyAsync(io_host_, S.io, bytes, cudaMemcpyDeviceToHost, stream_));
 	CK(cudaStreamSynchronize(stream_));
+	std::memcpy(out, io_host_, bytes);
 	return true;
 }
 
@@ -1601,7 +1657,14 @@ bool Engine::set_agent_data(const void* in, int m)
 	if (!sync()) return false;
 	if (m <= 0) return true;
 	if (m > cap_ && !dalloc(S.io, (size_t)m, err_)) return false;
-	CK(cudaMemcpyAsync(S.io, in, sizeof(AgentRecord) * m, cudaMemcpyHostToDevice, stream_));
+	const size_t bytes = sizeof(AgentRecord) * m;
+	if (is_pinned(in)) {
+		CK(cudaMemcpyAsync(S.io, in, bytes, cudaMemcpyHostToDevice, stream_));
+	} else {
+		if (!stage(m)) return false;
+		std::memcpy(io_host_, in, bytes);
+		CK(cudaMemcpyAsync(S.io, io_host_, bytes, cudaMemcpyHostToDevice, stream_));
+	}
 	k_unpack<<<(m + 255) / 256, 256, 0, stream_>>>(S, m);
 	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(stream_));
@@ -1801,6 +1864,7 @@ bool Engine::remove_at_goal()
 bool Engine::run_steps(int nsteps)
 {
 	if (configured_maxnb_ != maxnb_ && !configure()) return false;
+	steps_pending_ = true;
 	for (int s = 0; s < nsteps; ++s) {
 		if (opt_.use_graph && !profile_) {
 			if (!graph_valid_ && !capture_graph()) return false;
@@ -1904,12 +1968,14 @@ bool Engine::step(int nsteps)
 // the batch; other device conditions are reported.
 bool Engine::sync()
 {
+	if (!steps_pending_) return true;   // nothing enqueued since the last check
 	for (;;) {
 		CK(cudaStreamSynchronize(stream_));
 		int st = 0;
 		CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
 		if (st == 0) {
 			snap_valid_ = false;
+			steps_pending_ = false;
 			return true;
 		}
 		CK(cudaMemset(d_->status, 0, sizeof(int)));
@@ -2189,7 +2255,8 @@ void Engine::diff_free()
 {
 	Diff& D = df_;
 	void* ptrs[] = { D.s0_pos, D.s0_vel, D.s0_view, D.s0_vwf, D.s0_rng, D.targets, D.ck_pos, D.ck_vel, D.seg_pos,
-	                 D.seg_vel, D.seg_acc, D.tape, D.tape_cnt, D.lam_p, D.lam_v, D.lo_p, D.lo_v, D.dparams, D.loss };
+	                 D.seg_vel, D.seg_acc, D.tape, D.tape_cnt, D.lam_p, D.lam_v, D.lo_p, D.lo_v, D.adj_nb, D.dparams,
+	                 D.loss };
 	for (void* p : ptrs)
 		if (p) cudaFree(p);
 	D = Diff();
@@ -2235,7 +2302,8 @@ bool Engine::diff_begin(int steps, int every, const float* targets, float weight
 	    !dalloc(D.seg_pos, nn * (D.every + 1), err_) || !dalloc(D.seg_vel, nn * (D.every + 1), err_) ||
 	    !dalloc(D.seg_acc, nn * D.every, err_) || !dalloc(D.tape_cnt, nn * D.every, err_) ||
 	    !dalloc(D.lam_p, nn, err_) || !dalloc(D.lam_v, nn, err_) || !dalloc(D.lo_p, nn, err_) ||
-	    !dalloc(D.lo_v, nn, err_) || !dalloc(D.dparams, 4 * scen_.size(), err_) || !dalloc(D.loss, 1, err_)) {
+	    !dalloc(D.lo_v, nn, err_) || !dalloc(D.adj_nb, nn, err_) || !dalloc(D.dparams, 4 * scen_.size(), err_) ||
+	    !dalloc(D.loss, 1, err_)) {
 		diff_free();
 		return false;
 	}
@@ -2298,19 +2366,43 @@ bool Engine::diff_forward(double* loss)
 	if (!sync()) return false;
 	D.forward_done = false;
 	const int n = D.n;
+	// the last segment is recorded as it runs (lists, states, accelerations),
+	// so that the backward pass starts reversing without recomputing it
+	const int last0 = (D.nck - 1) * D.every;
+	DevState& S = *d_;
 	for (;;) {
 		if (!diff_restore_start()) return false;
 		if (configured_maxnb_ != maxnb_ && !configure()) return false;
+		if (!diff_alloc_tape()) return false;
 		CK(cudaMemsetAsync(D.loss, 0, sizeof(double), stream_));
 		for (int t = 0; t < D.steps; ++t) {
 			if (t % D.every == 0 && n > 0) {
 				const size_t c = (size_t)(t / D.every) * n;
-				CK(cudaMemcpyAsync(D.ck_pos + c, d_->pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
-				CK(cudaMemcpyAsync(D.ck_vel + c, d_->vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+				CK(cudaMemcpyAsync(D.ck_pos + c, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+				CK(cudaMemcpyAsync(D.ck_vel + c, S.vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
 			}
-			if (!run_steps(1)) return false;
-			if (n > 0) k_loss<<<(n + 255) / 256, 256, 0, stream_>>>(*d_, D.targets + (size_t)t * n, D.weight, D.loss);
+			if (t >= last0 && n > 0) {
+				const int st = t - last0;
+				CK(cudaMemcpyAsync(D.seg_pos + (size_t)st * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice,
+				                   stream_));
+				CK(cudaMemcpyAsync(D.seg_vel + (size_t)st * n, S.vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice,
+				                   stream_));
+				S.tape_list = D.tape + (size_t)st * n * maxnb_;
+				S.tape_cnt = D.tape_cnt + (size_t)st * n;
+				S.tape_acc = D.seg_acc + (size_t)st * n;
+				steps_pending_ = true;
+				enqueue_step();
+				S.tape_list = nullptr; S.tape_cnt = nullptr; S.tape_acc = nullptr;
+				time_ += sc_.dt;
+				for (size_t k = 0; k < times_.size(); ++k) times_[k] += scen_[k].dt;
+			} else if (!run_steps(1)) {
+				return false;
+			}
+			if (n > 0) k_loss<<<(n + 255) / 256, 256, 0, stream_>>>(S, D.targets + (size_t)t * n, D.weight, D.loss);
 		}
+		if (n > 0)
+			CK(cudaMemcpyAsync(D.seg_pos + (size_t)(D.steps - last0) * n, S.pos, sizeof(float2) * n,
+			                   cudaMemcpyDeviceToDevice, stream_));
 		CK(cudaGetLastError());
 		if (diff_check_status()) break;
 		if (err_ != "overflow") return false;
@@ -2341,13 +2433,14 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 	CK(cudaMemsetAsync(D.lam_p, 0, nb2, stream_));
 	CK(cudaMemsetAsync(D.lam_v, 0, nb2, stream_));
 	CK(cudaMemsetAsync(D.dparams, 0, sizeof(float) * 4 * scen_.size(), stream_));
-	const int adj_blocks = std::max(1, std::min((n + 3) / 4, num_sms_ * 16));
+	const int adj_blocks = std::max(1, std::min((n + 3) / 4, num_sms_ * 5));
 	for (int c = D.nck - 1; c >= 0 && n > 0; --c) {
 		const int t0 = c * D.every, m = std::min(D.every, D.steps - t0);
 		// recompute the segment from its checkpoint, recording lists and states
+		// (the forward pass recorded the last one)
 		CK(cudaMemcpyAsync(S.pos, D.ck_pos + (size_t)c * n, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
 		CK(cudaMemcpyAsync(S.vel, D.ck_vel + (size_t)c * n, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
-		for (int s = 0; s < m; ++s) {
+		for (int s = 0; s < m && c < D.nck - 1; ++s) {
 			CK(cudaMemcpyAsync(D.seg_pos + (size_t)s * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
 			CK(cudaMemcpyAsync(D.seg_vel + (size_t)s * n, S.vel, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
 			S.tape_list = D.tape + (size_t)s * n * maxnb_;
@@ -2356,7 +2449,9 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 			enqueue_step();
 			S.tape_list = nullptr; S.tape_cnt = nullptr; S.tape_acc = nullptr;
 		}
-		CK(cudaMemcpyAsync(D.seg_pos + (size_t)m * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice, stream_));
+		if (c < D.nck - 1)
+			CK(cudaMemcpyAsync(D.seg_pos + (size_t)m * n, S.pos, sizeof(float2) * n, cudaMemcpyDeviceToDevice,
+			                   stream_));
 		// reverse the segment
 		for (int s = m - 1; s >= 0; --s) {
 			k_inject<<<(n + 255) / 256, 256, 0, stream_>>>(n, D.seg_pos + (size_t)(s + 1) * n,
@@ -2373,6 +2468,8 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 			A.lam_out_p = D.lo_p; A.lam_out_v = D.lo_v;
 			A.lam_in_p = D.lam_p; A.lam_in_v = D.lam_v;
 			A.dparams = D.dparams;
+			A.adj_nb = D.adj_nb;
+			k_adj_prep<<<(n + 255) / 256, 256, 0, stream_>>>(A);
 			k_adjoint<<<adj_blocks, 128, 0, stream_>>>(A);
 		}
 	}
@@ -2394,6 +2491,7 @@ Engine::~Engine()
 	if (stream_) cudaStreamSynchronize(stream_);
 	invalidate_graph();
 	diff_free();
+	if (io_host_) cudaFreeHost(io_host_);
 	if (d_) {
 		DevState& S = *d_;
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,

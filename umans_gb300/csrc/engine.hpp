@@ -169,10 +169,14 @@ private:
 	uint32_t* snap_rng_ = nullptr;
 	int snap_cap_ = 0, snap_steps_ = 0;
 	bool snap_valid_ = false;
+	bool steps_pending_ = false;   // steps enqueued whose status has not been read
 	double snap_time_ = 0;
 	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
 	int prof_steps_ = 0;
 	std::vector<int> pol_scen_;   // scenario of each policy
+	AgentRecord* io_host_ = nullptr;   // page-locked staging for AgentData exchange
+	size_t io_host_cap_ = 0;
+	bool stage(size_t records);
 
 	// differentiable form (device buffers; see diff_begin)
 	struct Diff {
@@ -189,6 +193,7 @@ private:
 		uint32_t* tape = nullptr;                    // every x n x tape_nb
 		int* tape_cnt = nullptr;                     // every x n
 		float2 *lam_p = nullptr, *lam_v = nullptr, *lo_p = nullptr, *lo_v = nullptr;
+		float4* adj_nb = nullptr;                    // n: neighbour terms of the step being reversed
 		float* dparams = nullptr;
 		double* loss = nullptr;
 	} df_;
