@@ -64,3 +64,40 @@ def test_empty_world_and_single_agent(tmp_path):
     s.set_goal(i, 3, 0)
     s.step(5)
     assert s.positions()[0, 0] > 0.1
+
+
+def test_returned_buffer_fed_back_and_pageable_input(tmp_path):
+    """The e2e loop: the (page-locked) buffer GetAgentPositions returns is sent
+    back by SetAgentPositions; a pageable copy gives the same result."""
+    import ctypes as C
+    from umans_gb300 import _lib
+    path = S.model_crossing("SocialForces", n=60).write(str(tmp_path / "x.xml"))
+    lib = _lib.load()
+    ref = Simulation(path)
+    ref.step(8)
+    want = ref.state()
+    assert lib.StartSimulation(path.encode(), 1)
+    ptr = C.POINTER(AgentData)()
+    n = C.c_int()
+    cur = None
+    for k in range(8):
+        if cur is not None:
+            assert lib.SetAgentPositions(cur, n.value)
+        assert lib.DoSimulationSteps(1)
+        assert lib.GetAgentPositions(C.byref(ptr), C.byref(n))
+        cur = ptr if k % 2 == 0 else (AgentData * n.value).from_buffer_copy(
+            C.string_at(ptr, C.sizeof(AgentData) * n.value))
+    pos = np.array([[ptr[i].position_x, ptr[i].position_y] for i in range(n.value)], np.float32)
+    vel = np.array([[ptr[i].velocity_x, ptr[i].velocity_y] for i in range(n.value)], np.float32)
+    assert np.array_equal(pos, want["pos"]) and np.array_equal(vel, want["vel"])
+    assert lib.CleanUp()
+
+
+def test_async_steps_then_host_reads(tmp_path):
+    path = S.model_crossing("PowerLaw", n=50).write(str(tmp_path / "p.xml"))
+    a, b = Simulation(path), Simulation(path)
+    for _ in range(5):
+        a.step_async(2)
+    b.step(10)
+    assert np.array_equal(a.positions(), b.positions())
+    assert a.time == b.time
