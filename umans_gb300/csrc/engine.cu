@@ -313,20 +313,21 @@ __global__ void k_scatter(DevState S)
 struct WarpLists {
 	uint32_t* ref;   // (displacement group << 28) | cell-sorted index
 	float* key;      // sort key, then PhantomAgent::distSqr
-	int* nid;        // neighbour id (tie-break); reused for per-neighbour x terms
+	int* nid;        // scratch: per-neighbour x terms of the ordered force sums
 	float* aux;      // per-neighbour y terms
 };
 
-__device__ __forceinline__ bool nb_less(const WarpLists& L, int a, int b)
+// (key, id) order; ids are read from the cell-sorted copy when keys tie
+__device__ __forceinline__ bool nb_less(const DevState& S, const WarpLists& L, int a, int b)
 {
 	const float ka = L.key[a], kb = L.key[b];
-	return ka < kb || (ka == kb && L.nid[a] < L.nid[b]);
+	if (ka != kb) return ka < kb;
+	return S.sId[L.ref[a] & 0x0FFFFFFFu] < S.sId[L.ref[b] & 0x0FFFFFFFu];
 }
-__device__ __forceinline__ void nb_cmpswap(const WarpLists& L, int lo, int hi)
+__device__ __forceinline__ void nb_cmpswap(const DevState& S, const WarpLists& L, int lo, int hi)
 {
-	if (nb_less(L, hi, lo)) {
+	if (nb_less(S, L, hi, lo)) {
 		float k = L.key[lo]; L.key[lo] = L.key[hi]; L.key[hi] = k;
-		int d = L.nid[lo]; L.nid[lo] = L.nid[hi]; L.nid[hi] = d;
 		uint32_t r = L.ref[lo]; L.ref[lo] = L.ref[hi]; L.ref[hi] = r;
 	}
 }
@@ -334,7 +335,7 @@ __device__ __forceinline__ void nb_cmpswap(const WarpLists& L, int lo, int hi)
 // ascending bitonic sort of [s, s+len) by (key, id); the network compares
 // only i < j pairs with the min going to i, so the missing elements of the
 // power-of-two padding behave as +infinity and are simply skipped.
-__device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
+__device__ void warp_sort(const DevState& S, const WarpLists& L, int s, int len, int lane)
 {
 	if (len <= 1) return;
 	int lp = 0;
@@ -346,14 +347,14 @@ __device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
 		for (int k = lane; k < halfP; k += 32) {
 			const int blk = k >> lh, pos = k & ((1 << lh) - 1);
 			const int lo = (blk << ls) + pos, hi = (blk << ls) + (1 << ls) - 1 - pos;
-			if (hi < len) nb_cmpswap(L, s + lo, s + hi);
+			if (hi < len) nb_cmpswap(S, L, s + lo, s + hi);
 		}
 		__syncwarp();
 		// half-cleaners with distance 2^lj
 		for (int lj = lh - 1; lj >= 0; --lj) {
 			for (int k = lane; k < halfP; k += 32) {
 				const int lo = ((k >> lj) << (lj + 1)) | (k & ((1 << lj) - 1)), hi = lo + (1 << lj);
-				if (hi < len) nb_cmpswap(L, s + lo, s + hi);
+				if (hi < len) nb_cmpswap(S, L, s + lo, s + hi);
 			}
 			__syncwarp();
 		}
@@ -364,9 +365,9 @@ __device__ void warp_sort(const WarpLists& L, int s, int len, int lane)
 // holds M packed keys (float key bits with the low PB bits replaced by the
 // position in the segment; positive floats order like their bit patterns)
 // and a shuffle bitonic network sorts them.  The entries are then permuted
-// through registers holding only the references: the key and the id of an
-// entry are recomputed from its reference exactly as the gather computed
-// them (same expression, same operands).  Keys that agree above the low PB
+// through registers holding only the references: the key of an entry is
+// recomputed from its reference exactly as the gather computed it (same
+// expression, same operands).  Keys that agree above the low PB
 // bits may come out in either order: the near-tie pass that follows
 // (relative window 2^(PB-22), twice the 2^(PB-23) truncation) re-orders
 // them with the exact double distance and the id.
@@ -423,7 +424,6 @@ __device__ __forceinline__ void warp_sort_regs(const DevState& S, const WarpList
 			const float dx = q.x - cp.x, dy = q.y - cp.y;
 			L.ref[s + i] = u[m];
 			L.key[s + i] = dx * dx + dy * dy;
-			L.nid[s + i] = S.sId[tt];
 		}
 	}
 	__syncwarp();
@@ -439,8 +439,11 @@ __device__ __forceinline__ double exact_key(float2 q, float2 c)
 
 // Float keys order the list except within runs of near-equal keys (relative
 // gap <= win: 1e-6 after the exact-key sort, 2^-16 or 2^-15 after the
-// packed-key register sorts), whose order is settled with the reference's
-// double distance (then id).  Runs are rare; lane 0 handles them.
+// packed-key register sorts, whose keys are truncated), which lane 0
+// re-sorts in the reference's order.  Float keys carry a relative error below
+// 2.5e-7 (one rounding of each difference, square and sum), so two keys more
+// than 1e-6 apart order as the exact ones do; closer pairs are compared on the
+// reference's double distance, then the id.
 __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane, float win)
 {
 	bool close = false;
@@ -452,35 +455,30 @@ __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int 
 	if (lane == 0) {
 		int k = s;
 		while (k + 1 < e) {
-			const float a = L.key[k], b = L.key[k + 1];
-			if (!(b - a <= win * b)) { ++k; continue; }
+			if (!(L.key[k + 1] - L.key[k] <= win * L.key[k + 1])) { ++k; continue; }
 			const int r0 = k;
 			while (k + 1 < e && L.key[k + 1] - L.key[k] <= win * L.key[k + 1]) ++k;
 			const int r1 = k;   // inclusive
-			// insertion sort of the run on (exact double key, id); the exact keys
-			// are kept in place of the float keys meanwhile
-			double dk[16];
-			const bool small = r1 - r0 < 16;
-			for (int x = r0; x <= r1; ++x) {
-				const double d = exact_key(q, S.sP[L.ref[x] & 0x0FFFFFFFu]);
-				if (small) dk[x - r0] = d;
-			}
 			for (int x = r0 + 1; x <= r1; ++x) {
 				const uint32_t rx = L.ref[x];
-				const int ix = L.nid[x];
 				const float kx = L.key[x];
-				const double dx = small ? dk[x - r0] : exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
 				int y = x - 1;
 				while (y >= r0) {
-					const double dy = small ? dk[y - r0] : exact_key(q, S.sP[L.ref[y] & 0x0FFFFFFFu]);
-					if (dy > dx || (dy == dx && L.nid[y] > ix)) {
-						L.ref[y + 1] = L.ref[y]; L.nid[y + 1] = L.nid[y]; L.key[y + 1] = L.key[y];
-						if (small) dk[y + 1 - r0] = dy;
-						--y;
-					} else break;
+					const uint32_t ry = L.ref[y];
+					const float ky = L.key[y];
+					bool after;   // entry y belongs after entry x
+					if (ky - kx > 1e-6f * ky) after = true;
+					else if (kx - ky > 1e-6f * kx) after = false;
+					else {
+						const double dx = exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
+						const double dy = exact_key(q, S.sP[ry & 0x0FFFFFFFu]);
+						after = dy > dx || (dy == dx && S.sId[ry & 0x0FFFFFFFu] > S.sId[rx & 0x0FFFFFFFu]);
+					}
+					if (!after) break;
+					L.ref[y + 1] = ry; L.key[y + 1] = ky;
+					--y;
 				}
-				L.ref[y + 1] = rx; L.nid[y + 1] = ix; L.key[y + 1] = kx;
-				if (small) dk[y + 1 - r0] = dx;
+				L.ref[y + 1] = rx; L.key[y + 1] = kx;
 			}
 			++k;
 		}
@@ -496,7 +494,7 @@ __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int 
 __device__ int gather(const DevState& S, const GridParams& G, int cb, int world, float W, float H, const WarpLists& L,
                       int t, float2 p, float r, int lane, bool* overflow)
 {
-	int K = 0;
+	int K = 0, K0 = 0;
 	const int maxnb = S.maxnb;
 	if (!(r > 0)) return 0;   // dist < r*r never holds for r = 0
 	const float r2 = r * r;
@@ -567,23 +565,25 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 					if (idx < maxnb) {
 						L.ref[idx] = ((uint32_t)g << 28) | (uint32_t)tt;
 						L.key[idx] = d2f;
-						L.nid[idx] = S.sId[tt];
 					}
 				}
 				K += __popc(m);
 			}
 		}
 		if (K > maxnb) { *overflow = true; K = maxnb; }
+		if (g == 0) K0 = K;
 		__syncwarp();
 		const int len = K - gs;
 		if (len <= 32) warp_sort_regs<1>(S, L, gs, len, lane, q);
 		else if (len <= 64) warp_sort_regs<2>(S, L, gs, len, lane, q);
 		else if (len <= 128) warp_sort_regs<4>(S, L, gs, len, lane, q);
-		else warp_sort(L, gs, len, lane);
+		else warp_sort(S, L, gs, len, lane);
 		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : (len <= 128 ? 0x1p-15f : 1e-6f));
 	}
-	// PhantomAgent position offset = -displacement; distSqr in float
-	for (int k = lane; k < K; k += 32) {
+	// PhantomAgent position offset = -displacement; distSqr in float.  For
+	// the undisplaced group the sort keys are already that value (same
+	// operands, same operations), so only displaced entries are recomputed.
+	for (int k = K0 + lane; k < K; k += 32) {
 		const uint32_t rr = L.ref[k];
 		const float2 ph = vadd(S.sP[rr & 0x0FFFFFFFu], group_offset(rr >> 28, W, H));
 		L.key[k] = vsq(vsub(p, ph));
@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	uint32_t* base = reinterpret_cast<uint32_t*>(smem) + (size_t)wib * 4 * maxnb;
 	WarpLists L{ base, reinterpret_cast<float*>(base + maxnb), reinterpret_cast<int*>(base + 2 * maxnb),
 	             reinterpret_cast<float*>(base + 3 * maxnb) };
-	float* fx = reinterpret_cast<float*>(L.nid);   // per-neighbour terms (ids no longer needed)
+	float* fx = reinterpret_cast<float*>(L.nid);   // per-neighbour terms
 	float* fy = L.aux;
 	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
 	float4* proj = lines + maxnb;
@@ -959,7 +959,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		if (dump) {
 			const int cap = S.dump_cap;
 			for (int k = lane; k < K && k < cap; k += 32) {
-				S.dump_ids[(size_t)slot * cap + k] = L.nid[k];
+				S.dump_ids[(size_t)slot * cap + k] = S.sId[L.ref[k] & 0x0FFFFFFFu];
 				S.dump_d2[(size_t)slot * cap + k] = L.key[k];
 			}
 			if (lane == 0) S.dump_cnt[slot] = K;
