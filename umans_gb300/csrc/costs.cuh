@@ -71,33 +71,64 @@ UD float ttc_first(const AgentCtx& A, const NbView& N, float2 vel, float maxDist
 	return minT;
 }
 
+// Pair-invariant terms of SocialForcesAvoidance for one agent and cost:
+// -V0/sigma is the first factor of d_V as written (so precomputing it changes
+// no rounding), |vel| is the agent's factor of the view test's lengths.
+struct SfConst {
+	float dtp, sigma, nV0s, vmag_vel;
+};
+UD SfConst sf_const(const AgentCtx& A, const CostDesc& c)
+{
+	SfConst K;
+	K.dtp = c.p[0];
+	K.sigma = c.p[2];
+	K.nV0s = -c.p[1] / c.p[2];
+	K.vmag_vel = vmag(A.vel);
+	return K;
+}
+
+// angle(a, b) < thr (devmath.cuh angle_less) with |a| and |b| given
+UD bool angle_less_m(float2 a, float2 b, float ma, float mb, float thr, float cos_thr)
+{
+	const float lf = ma * mb;
+	if (lf == 0) return true;
+	const float d = vdot(a, b);
+	const float c = d / lf;
+	if (c > cos_thr + 1e-6f) return true;
+	if (c < cos_thr - 1e-6f && c > -0.9999f) return false;
+	if (c <= -0.9999f) return -d > lf;
+	return vangle_exact(a, b) < thr;
+}
+
 // SocialForcesAvoidance::ComputeAgentInteractionForce: SocialForcesAvoidance.cpp:26-110
 // E = (Eb.x, Eb.y, vb): the neighbour's normalised preferred velocity and
 // its speed (SocialForcesAvoidance.cpp:58-59), precomputed once per agent
-UD float2 sf_force(const AgentCtx& A, const CostDesc& c, float2 np, float4 E, float nr)
+UD float2 sf_force(const AgentCtx& A, const SfConst& K, float2 np, float4 E, float nr)
 {
-	const float dtp = c.p[0], V0 = c.p[1], sigma = c.p[2];
 	const float2 R = vsub(A.pos, np);
 	const float magR = vmag(R);
 	if (magR <= A.radius + nr) return V(0, 0);
 	const float vb = E.z;
 	const float2 Eb = V(E.x, E.y);
-	const float2 Vv = vmul(Eb, vb * dtp);
+	const float2 Vv = vmul(Eb, vb * K.dtp);
 	const float magV = vmag(Vv);
 	const float2 R2 = vsub(R, Vv);
 	const float magR2 = vmag(R2);
-	const float bSquared2 = sq_diff_d(magR + magR2, vb * dtp);
+	const float bSquared2 = sq_diff_d(magR + magR2, vb * K.dtp);
 	if (bSquared2 <= 0) return V(0, 0);
 	const float b = 0.5f * sqrtf(bSquared2);
 	if (b < 0.001f) return V(0, 0);
-	const float d_magR2 = 1 / (2 * magR2) * (2 * magR - 2 * magV * vcosangle(R, Vv));
+	// cosAngle(R, Vv): the lengths are magR and magV
+	const float lRV = magR * magV;
+	const float cosRV = lRV == 0 ? 0.0f : vdot(R, Vv) / lRV;
+	const float d_magR2 = 1 / (2 * magR2) * (2 * magR - 2 * magV * cosRV);
 	const float d_bSquared2 = 2 * (magR + magR2) * (1 + d_magR2);
 	const float d_b = (1 / (8 * b)) * d_bSquared2;
-	const float d_V = -V0 / sigma * ref_expf(A.ex, -b / sigma) * d_b;
+	const float d_V = K.nV0s * ref_expf(A.ex, -b / K.sigma) * d_b;
 	const float2 F = vmul(vneg(R), d_V);
-	// viewingAngleHalf = (float)(100 deg in rad); cos of it to 1e-8
+	// viewingAngleHalf = (float)(100 deg in rad); cos of it to 1e-8; |-R| = magR
 	const float viewHalf = (float)(100.0 * REF_PI / 180.0);
-	const float scale = angle_less(A.vel, vneg(R), viewHalf, -0.17364818f) ? 1.0f : 0.5f;
+	const float scale = angle_less_m(A.vel, vneg(R), K.vmag_vel, magR, viewHalf, -0.17364818f) ? 1.0f : 0.5f;
 	return vmul(F, scale);
 }
 

@@ -620,15 +620,21 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 {
 	if (c.kind == K_GOALREACHING) return vdiv(vsub(A.pref, A.vel), fmaxr(A.relax, A.dt));
 	const float rs = c.range * c.range;
-	for (int k = lane; k < N.K; k += 32) {
-		float2 f = V(0, 0);
-		if (N.d2[k] <= rs) {
-			const float2 np = nb_pos(N, k), nv = nb_vel(N, k);
-			if (c.kind == K_SOCIALFORCES) f = sf_force(A, c, np, nb_E(N, k), nb_radius(N, k));
-			else f = pl_force(A, c, np, nv, nb_radius(N, k));
+	if (c.kind == K_SOCIALFORCES) {
+		const SfConst SK = sf_const(A, c);
+		for (int k = lane; k < N.K; k += 32) {
+			float2 f = V(0, 0);
+			if (N.d2[k] <= rs) f = sf_force(A, SK, nb_pos(N, k), nb_E(N, k), nb_radius(N, k));
+			fx[k] = f.x;
+			fy[k] = f.y;
 		}
-		fx[k] = f.x;
-		fy[k] = f.y;
+	} else {
+		for (int k = lane; k < N.K; k += 32) {
+			float2 f = V(0, 0);
+			if (N.d2[k] <= rs) f = pl_force(A, c, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+			fx[k] = f.x;
+			fy[k] = f.y;
+		}
 	}
 	__syncwarp();
 	float acc = 0.0f;
