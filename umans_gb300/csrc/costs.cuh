@@ -172,26 +172,35 @@ UD float karamouzas_maxdev(float ttc)
 }
 
 // Karamouzas::GetCost: Karamouzas.cpp:28-113.  ttcp = TTC at the preferred
-// velocity (sample invariant), maxdev/cosdev from it.
-UD float cost_karamouzas(const AgentCtx& A, const NbView& N, const CostDesc& c, float ttcp, float maxdev,
-                         float cosdev, float2 v)
+// velocity (sample invariant), maxdev/cosdev from it.  Split in three: the
+// sample window (deviation angle, speed range; MAXF outside), the TTC sweep,
+// and the cost terms.
+UD bool karamouzas_window(const AgentCtx& A, float ttcp, float maxdev, float cosdev, float2 v, float speed)
 {
-	const float alpha = c.p[0], beta = c.p[1], gamma = c.p[2], delta = c.p[3], t_max = c.p[4];
 	const float tc_min = 2.5f, tc_max = 8;
-	const float speed = vmag(v);
-	if (angle_greater(v, A.pref, maxdev, cosdev)) return MAXF;
+	if (angle_greater(v, A.pref, maxdev, cosdev)) return false;
 	const float dS = fabsf(A.maxspeed - A.prefspeed), eps = 0.05f;
 	float minS, maxS;
 	if (ttcp <= 0 || ttcp >= tc_max) { minS = A.prefspeed - eps; maxS = A.prefspeed + eps; }
 	else if (ttcp > 0 && ttcp < tc_min) { minS = 0; maxS = A.maxspeed + eps; }
 	else { minS = A.prefspeed - dS - eps; maxS = A.prefspeed + dS + eps; }
-	if (speed < minS || speed > maxS) return MAXF;
-	const float TTC = ttc_first(A, N, v, c.range, true);
+	return !(speed < minS || speed > maxS);
+}
+UD float karamouzas_terms(const AgentCtx& A, const CostDesc& c, float2 v, float speed, float TTC)
+{
+	const float alpha = c.p[0], beta = c.p[1], gamma = c.p[2], delta = c.p[3], t_max = c.p[4];
 	const float a = alpha * (1 - vcosangle(v, A.pref) / 2.0f);
 	const float b = beta * fabsf(speed - vmag(A.vel)) / A.maxspeed;
 	const float cc = gamma * vmag(vsub(v, A.pref)) / (2 * A.maxspeed);
 	const float d = delta * fmaxr(0.0f, t_max - TTC) / t_max;
 	return a + b + cc + d;
+}
+UD float cost_karamouzas(const AgentCtx& A, const NbView& N, const CostDesc& c, float ttcp, float maxdev,
+                         float cosdev, float2 v)
+{
+	const float speed = vmag(v);
+	if (!karamouzas_window(A, ttcp, maxdev, cosdev, v, speed)) return MAXF;
+	return karamouzas_terms(A, c, v, speed, ttc_first(A, N, v, c.range, true));
 }
 
 // Moussaid::GetCost: Moussaid.cpp:28-62

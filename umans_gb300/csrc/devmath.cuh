@@ -188,6 +188,20 @@ UD float ttc_pair(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2
 	return fminr(t1, t2);
 }
 
+// ttc_pair with P = p1 - p2 and c = |P|^2 - (r1 + r2)^2 given (the same
+// values ttc_pair computes; |P|^2 <= RR exactly when c <= 0)
+UD float ttc_pair_pre(float2 v1, float2 P, float c, float2 v2)
+{
+	if (c <= 0) return 0;
+	const float2 Vd = vsub(v1, v2);
+	const float a = vdot(Vd, Vd), b = 2 * vdot(P, Vd);
+	float t1 = MAXF, t2 = MAXF;
+	solve_quadratic(a, b, c, &t1, &t2);
+	if (t1 < 0) t1 = MAXF;
+	if (t2 < 0) t2 = MAXF;
+	return fminr(t1, t2);
+}
+
 UD void ttca_dca(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2, float* ttca_o, float* dca_o)
 {
 	const float2 dpc = vsub(p2, p1), dvc = vsub(v2, v1);

@@ -859,7 +859,7 @@ __device__ __forceinline__ float rng_uniform(uint32_t x, float a, float b)
 // CostFunction::ApproximateGlobalMinimumBySampling: costFunction.cpp:66-164.
 // Samples are spread over lanes; the argmin keeps the first strict minimum.
 __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView& N, const PolicyDesc& pol,
-                             const CostPrep& P, uint32_t rng0, int lane)
+                             const CostPrep& P, uint32_t rng0, int lane, float4* pair4, float* pairv)
 {
 	float2 base = V(0, 0);
 	if (pol.table_base == 1) base = A.vel;
@@ -874,6 +874,85 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 	const int ncost = pol.single_cost ? 1 : pol.ncost;
 	float bestC = MAXF;
 	int bestI = 0x7fffffff;
+	if (ncost == 1 && pol.cost[0].kind == K_KARAMOUZAS && !pol.table_random) {
+		// Karamouzas alone: most samples fall outside its window (cost MAXF);
+		// the lanes test the windows of 32 samples at a time, then the warp
+		// sweeps the neighbours for each sample inside, in sample order.
+		const CostDesc& c = pol.cost[0];
+		const float coeff = pol.single_cost ? 1.0f : c.coeff;
+		const float outside = 0.0f + coeff * MAXF;   // the sum of one term, as below
+		int first_out = 0x7fffffff;
+		// the sample-invariant part of every pair within the cost's range,
+		// compacted into this warp's scratch: ttc_pair's P = p - p_j and
+		// c = |P|^2 - (r + r_j)^2 (c <= 0 exactly when |P|^2 <= (r + r_j)^2),
+		// and the neighbour's velocity
+		int KP = 0;
+		{
+			const float md2 = c.range * c.range;
+			for (int b0 = 0; b0 < N.K; b0 += 32) {
+				const int k = b0 + lane;
+				const bool inr = k < N.K && !(N.d2[k] > md2);
+				const unsigned m = __ballot_sync(0xffffffffu, inr);
+				if (inr) {
+					const float2 Pd = vsub(A.pos, nb_pos(N, k));
+					const float R = A.radius + nb_radius(N, k);
+					const float2 vj = nb_vel(N, k);
+					const int idx = KP + __popc(m & ((1u << lane) - 1u));
+					pair4[idx] = make_float4(Pd.x, Pd.y, vdot(Pd, Pd) - R * R, vj.x);
+					pairv[idx] = vj.y;
+				}
+				KP += __popc(m);
+			}
+			__syncwarp();
+		}
+		for (int i0 = 0; i0 < pol.nsamples; i0 += 32) {
+			const int i = i0 + lane;
+			float2 v = V(0, 0);
+			float speed = 0;
+			bool in = false, valid = i < pol.nsamples;
+			if (valid) {
+				const SampleEntry e = S.table[pol.table_offset + i];
+				v = vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
+				speed = vmag(v);
+				in = karamouzas_window(A, P.ttcp[0], P.maxdev[0], P.cosdev[0], v, speed);
+			}
+			const unsigned out_mask = __ballot_sync(0xffffffffu, valid && !in);
+			if (out_mask && first_out == 0x7fffffff) first_out = i0 + __ffs(out_mask) - 1;
+			unsigned m = __ballot_sync(0xffffffffu, in);
+			while (m) {
+				const int src = __ffs(m) - 1;
+				m &= m - 1;
+				const float2 vs = V(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+				const float ss = __shfl_sync(0xffffffffu, speed, src);
+				// ComputeTimeToFirstCollision over the pairs (ignoring current
+				// collisions): a minimum, split over the lanes
+				float TTC = MAXF;
+				for (int k = lane; k < KP; k += 32) {
+					const float4 q = pair4[k];
+					const float t = ttc_pair_pre(vs, V(q.x, q.y), q.z, V(q.w, pairv[k]));
+					if (t == 0) continue;
+					if (t < TTC) TTC = t;
+				}
+				for (int o = 16; o > 0; o >>= 1) {
+					const float x = __shfl_xor_sync(0xffffffffu, TTC, o);
+					if (x < TTC) TTC = x;
+				}
+				const float tc = 0.0f + coeff * karamouzas_terms(A, c, vs, ss, TTC);
+				if (tc < bestC) { bestC = tc; bestI = i0 + src; }
+			}
+		}
+		// samples outside the window all cost `outside`; like every sample
+		// they count only below the initial best (MAXF), and then the first
+		// of them competes with the best inside on (cost, index)
+		if (first_out != 0x7fffffff && outside < MAXF &&
+		    (outside < bestC || (outside == bestC && first_out < bestI))) {
+			bestC = outside;
+			bestI = first_out;
+		}
+		if (bestI == 0x7fffffff) return V(0, 0);
+		const SampleEntry e = S.table[pol.table_offset + bestI];
+		return vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
+	}
 	for (int i = lane; i < pol.nsamples; i += 32) {
 		float2 v;
 		if (pol.table_random) {
@@ -1081,7 +1160,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				else if (pol.method == M_GLOBAL && pol.ncost == 1 && is_force_based(c0.kind)) best = P.target[0];
 				else {
 					const uint32_t r0 = S.rng[slot];
-					best = sample_min(S, A, N, pol, P, r0, lane);
+					best = sample_min(S, A, N, pol, P, r0, lane, lines, reinterpret_cast<float*>(proj));
 					if (pol.table_random) {
 						rng_used = true;
 						rng_next = mulmod(S.lcgpow[2 * pol.nsamples], r0);
