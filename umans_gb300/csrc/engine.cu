@@ -858,6 +858,12 @@ __device__ __forceinline__ float rng_uniform(uint32_t x, float a, float b)
 
 // CostFunction::ApproximateGlobalMinimumBySampling: costFunction.cpp:66-164.
 // Samples are spread over lanes; the argmin keeps the first strict minimum.
+// samples of the Karamouzas window swept together (independent chains)
+#ifndef UMANS_KS
+#define UMANS_KS 6
+#endif
+constexpr int KS = UMANS_KS;
+
 __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView& N, const PolicyDesc& pol,
                              const CostPrep& P, uint32_t rng0, int lane, float4* pair4, float* pairv)
 {
@@ -918,27 +924,46 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			}
 			const unsigned out_mask = __ballot_sync(0xffffffffu, valid && !in);
 			if (out_mask && first_out == 0x7fffffff) first_out = i0 + __ffs(out_mask) - 1;
+			// KS samples inside the window at a time: their sweeps share the
+			// pair loads and run as independent chains
 			unsigned m = __ballot_sync(0xffffffffu, in);
 			while (m) {
-				const int src = __ffs(m) - 1;
-				m &= m - 1;
-				const float2 vs = V(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-				const float ss = __shfl_sync(0xffffffffu, speed, src);
+				int si[KS];
+				float2 sv[KS];
+				float ssp[KS], T[KS];
+#pragma unroll
+				for (int j = 0; j < KS; ++j) {
+					si[j] = m ? __ffs(m) - 1 : -1;
+					if (m) m &= m - 1;
+					const int src = si[j] < 0 ? si[0] : si[j];
+					sv[j] = V(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+					ssp[j] = __shfl_sync(0xffffffffu, speed, src);
+					T[j] = MAXF;
+				}
 				// ComputeTimeToFirstCollision over the pairs (ignoring current
-				// collisions): a minimum, split over the lanes
-				float TTC = MAXF;
+				// collisions): minima, split over the lanes
 				for (int k = lane; k < KP; k += 32) {
 					const float4 q = pair4[k];
-					const float t = ttc_pair_pre(vs, V(q.x, q.y), q.z, V(q.w, pairv[k]));
-					if (t == 0) continue;
-					if (t < TTC) TTC = t;
+					const float2 P2 = V(q.x, q.y), v2 = V(q.w, pairv[k]);
+#pragma unroll
+					for (int j = 0; j < KS; ++j) {
+						const float t = ttc_pair_pre(sv[j], P2, q.z, v2);
+						if (t != 0 && t < T[j]) T[j] = t;
+					}
 				}
-				for (int o = 16; o > 0; o >>= 1) {
-					const float x = __shfl_xor_sync(0xffffffffu, TTC, o);
-					if (x < TTC) TTC = x;
+#pragma unroll
+				for (int j = 0; j < KS; ++j)
+					for (int o = 16; o > 0; o >>= 1) {
+						const float x = __shfl_xor_sync(0xffffffffu, T[j], o);
+						if (x < T[j]) T[j] = x;
+					}
+				// costs in sample order: the first strict minimum is kept
+#pragma unroll
+				for (int j = 0; j < KS; ++j) {
+					if (si[j] < 0) break;
+					const float tc = 0.0f + coeff * karamouzas_terms(A, c, sv[j], ssp[j], T[j]);
+					if (tc < bestC) { bestC = tc; bestI = i0 + si[j]; }
 				}
-				const float tc = 0.0f + coeff * karamouzas_terms(A, c, vs, ss, TTC);
-				if (tc < bestC) { bestC = tc; bestI = i0 + src; }
 			}
 		}
 		// samples outside the window all cost `outside`; like every sample
