@@ -60,6 +60,8 @@ struct DevState {
 	const uint32_t* lcgpow;
 	float4* scratch;
 	int maxnb, total_warps, max_cells;   // max_cells: capacity of the cell arrays (all scenarios)
+	int t_begin, t_end;   // cell-sorted agents this k_agent launch updates
+	const int* scen_order;   // [nscen]: scenarios in cell-space order (grouped by kernel)
 	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks
 	float cells_per_range;
 	ExpExceptions expx;   // host-expf exception table
@@ -115,7 +117,9 @@ __global__ void k_bbox(DevState S)
 }
 
 // One block: grid parameters of every scenario, then the exclusive scan of
-// their cell counts into cell_base (scenario grids are concatenated).
+// their cell counts into cell_base (scenario grids are concatenated in
+// scen_order, which groups scenarios by the k_agent specialisation they use,
+// so that each group's agents form one range of the cell-sorted arrays).
 __global__ void __launch_bounds__(1024) k_grid(DevState S)
 {
 	const int ns = S.nscen;
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(1024) k_grid(DevState S)
 	const int s0 = threadIdx.x * per;
 	int local = 0;
 	for (int k = 0; k < per && s0 + k < ns; ++k) {
-		const int s = s0 + k;
+		const int s = S.scen_order[s0 + k];
 		const ScenDesc sd = S.scen[s];
 		unsigned* B = S.bbox + 4 * s;
 		float x0, y0, ex, ey;
@@ -163,8 +167,9 @@ __global__ void __launch_bounds__(1024) k_grid(DevState S)
 	}
 	int run = tot[threadIdx.x] - local;
 	for (int k = 0; k < per && s0 + k < ns; ++k) {
-		const int c = S.cell_base[s0 + k];
-		S.cell_base[s0 + k] = run;
+		const int s = S.scen_order[s0 + k];
+		const int c = S.cell_base[s];
+		S.cell_base[s] = run;
 		run += c;
 	}
 	if (threadIdx.x == blockDim.x - 1) S.cell_base[ns] = tot[threadIdx.x];
@@ -1044,9 +1049,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	float4* proj = lines + maxnb;
 	bool overflow = false;
 
-	const int per = (S.n + S.total_warps - 1) / S.total_warps;
-	const int t0 = S.sched ? gw * per : gw, stride = S.sched ? 1 : S.total_warps;
-	const int tend = S.sched ? min(S.n, t0 + per) : S.n;
+	const int span = S.t_end - S.t_begin;
+	const int per = (span + S.total_warps - 1) / S.total_warps;
+	const int t0 = S.t_begin + (S.sched ? gw * per : gw), stride = S.sched ? 1 : S.total_warps;
+	const int tend = S.sched ? min(S.t_end, t0 + per) : S.t_end;
 	for (int t = t0; t < tend; t += stride) {
 		const int slot = S.sSlot[t];
 		const float4 sb = S.sB[t];
@@ -1571,6 +1577,40 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		for (int c = 0; c < p.ncost; ++c)
 			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE;
 	if (need_exp && !exp_exceptions_for_device(&d_->expx, nullptr, err_)) return false;
+	// kernel groups: scenarios whose policies are all gradient + force-based
+	// costs (k_agent<1>), scenarios with an ORCA cost, the others
+	// (k_agent<0>); cell space orders scenarios by group
+	{
+		std::vector<int> cls(scen_.size(), 0);
+		for (size_t k = 0; k < scen_.size(); ++k) {
+			bool force_only = true, orca = false;
+			for (size_t pi = 0; pi < pols_.size(); ++pi) {
+				if (pol_scen_[pi] != (int)k) continue;
+				const PolicyDesc& P = pols_[pi];
+				if (P.method != M_GRADIENT) force_only = false;
+				for (int c = 0; c < P.ncost; ++c) {
+					const int kd = P.cost[c].kind;
+					if (!(kd == K_SOCIALFORCES || kd == K_POWERLAW || kd == K_GOALREACHING)) force_only = false;
+					if (kd == K_ORCA) orca = true;
+				}
+			}
+			cls[k] = force_only ? 0 : (orca ? 1 : 2);
+		}
+		scen_order_.clear();
+		groups_.clear();
+		for (int c = 0; c < 3; ++c) {
+			const int j0 = (int)scen_order_.size();
+			for (size_t k = 0; k < scen_.size(); ++k)
+				if (cls[k] == c) scen_order_.push_back((int)k);
+			if ((int)scen_order_.size() > j0) groups_.push_back(KGroup{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0 });
+		}
+		if (!dalloc(scen_order_dev_, scen_order_.size(), err_)) return false;
+		CK(cudaMemcpy(scen_order_dev_, scen_order_.data(), sizeof(int) * scen_order_.size(), cudaMemcpyHostToDevice));
+		d_->scen_order = scen_order_dev_;
+		for (size_t k = 1; k < groups_.size(); ++k) CK(cudaStreamCreateWithFlags(&aux_[k - 1], cudaStreamNonBlocking));
+		CK(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+		for (cudaEvent_t& e : join_ev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+	}
 	if (!build_tables()) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;
@@ -1854,18 +1894,21 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	}
 	mode_ = 1;
-	for (const auto& p : pols_) {
-		if (p.method != M_GRADIENT) mode_ = 0;
-		for (int c = 0; c < p.ncost; ++c)
-			if (!(p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_GOALREACHING))
-				mode_ = 0;
+	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
+	// one launch shape per kernel group, each with its own line scratch
+	// (groups of a batch run concurrently)
+	size_t scr = 0;
+	for (auto& g : groups_) {
+		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode);
+		if (opt_.occupancy < 1.0f) g.blocks = std::max(num_sms_, (int)(g.blocks * opt_.occupancy));
+		g.scratch_off = scr;
+		scr += (size_t)g.blocks * wpb * 2 * maxnb_;
 	}
-	agent_blocks_ = agent_blocks_for(num_sms_, wpb, smem, mode_);
-	if (opt_.occupancy < 1.0f) agent_blocks_ = std::max(num_sms_, (int)(agent_blocks_ * opt_.occupancy));
+	agent_blocks_ = groups_.empty() ? num_sms_ : groups_[0].blocks;
 	S.total_warps = agent_blocks_ * wpb;
 	S.sched = opt_.schedule;
 	S.cells_per_range = opt_.cells_per_range;
-	if (!dalloc(S.scratch, (size_t)S.total_warps * 2 * maxnb_, err_)) return false;
+	if (!dalloc(S.scratch, std::max<size_t>(scr, 1), err_)) return false;
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
 	return true;
@@ -1889,15 +1932,47 @@ void Engine::enqueue_step()
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
-	if (S.tape_list) {
-		if (mode_ == 1) k_agent<1, true><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
-		else k_agent<0, true><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
-	} else if (mode_ == 1) k_agent<1><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
-	else k_agent<0><<<agent_blocks_, wpb * 32, smem, stream_>>>(S, 0);
+	// the agents of each kernel group form one range of the cell-sorted
+	// arrays (scenarios are ordered by group in cell space)
+	int t = 0;
+	std::vector<int> tb(groups_.size()), te(groups_.size());
+	for (size_t k = 0; k < groups_.size(); ++k) {
+		const KGroup& g = groups_[k];
+		int cnt = 0;
+		if (scen_.size() == 1) cnt = n_;
+		else for (int j = g.j0; j < g.j1; ++j) cnt += scen_[scen_order_[j]].n;
+		tb[k] = t; te[k] = t + cnt; t += cnt;
+	}
+	auto launch = [&](size_t k, cudaStream_t st) {
+		const KGroup& g = groups_[k];
+		if (te[k] <= tb[k]) return;
+		DevState A = S;
+		A.t_begin = tb[k]; A.t_end = te[k];
+		A.total_warps = g.blocks * wpb;
+		A.scratch = S.scratch + g.scratch_off;
+		if (S.tape_list) {
+			if (g.mode == 1) k_agent<1, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
+			else k_agent<0, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
+		} else if (g.mode == 1) k_agent<1><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
+		else k_agent<0><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
+	};
+	if (groups_.size() == 1 || S.tape_list) {
+		for (size_t k = 0; k < groups_.size(); ++k) launch(k, stream_);
+	} else {
+		// fork: groups 1.. on auxiliary streams, group 0 on the engine's
+		cudaEventRecord(fork_ev_, stream_);
+		for (size_t k = 1; k < groups_.size(); ++k) {
+			cudaStreamWaitEvent(aux_[k - 1], fork_ev_, 0);
+			launch(k, aux_[k - 1]);
+			cudaEventRecord(join_ev_[k - 1], aux_[k - 1]);
+		}
+		launch(0, stream_);
+		for (size_t k = 1; k < groups_.size(); ++k) cudaStreamWaitEvent(stream_, join_ev_[k - 1], 0);
+	}
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
 
-int Engine::kernels_per_step() const { return 8; }
+int Engine::kernels_per_step() const { return 7 + (int)groups_.size(); }
 
 bool Engine::capture_graph()
 {
@@ -2177,6 +2252,7 @@ bool Engine::add_agent(float x, float y, float radius, float pref, float maxs, f
                        int desired_id, int* out_id)
 {
 	// AddAgent (APIFunctions.cpp:139-171) -> WorldBase::AddAgent (worldBase.cpp:161-186)
+	if (scen_.size() > 1) { err_ = "agents cannot be added to a batch"; return false; }
 	int pidx = -1;
 	for (size_t k = 0; k < sc_.policy_ids.size(); ++k)
 		if (sc_.policy_ids[k] == policy_id) pidx = (int)k;
@@ -2203,6 +2279,7 @@ bool Engine::add_agent(float x, float y, float radius, float pref, float maxs, f
 bool Engine::remove_agent(int id)
 {
 	// WorldBase::RemoveAgent (worldBase.cpp:198-235): the last agent moves into the gap
+	if (scen_.size() > 1) { err_ = "agents cannot be removed from a batch"; return false; }
 	auto it = slot_of_.find(id);
 	if (it == slot_of_.end()) { err_ = "no agent with id " + std::to_string(id); return false; }
 	if (!download_mutable()) return false;
@@ -2253,6 +2330,8 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	k_scan_top<<<1, 1024, 0, stream_>>>(T);
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
 	k_scatter<<<nb, threads, 0, stream_>>>(T);
+	T.t_begin = 0;
+	T.t_end = n_;
 	k_agent<0><<<blocks, wpb * 32, smem, stream_>>>(T, 1);
 	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(stream_));
@@ -2613,8 +2692,11 @@ Engine::~Engine()
 			if (p) cudaFree(p);
 		delete d_;
 	}
-	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_ })
+	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_, fork_ev_, join_ev_[0], join_ev_[1] })
 		if (e) cudaEventDestroy(e);
+	for (cudaStream_t st : aux_)
+		if (st) cudaStreamDestroy(st);
+	if (scen_order_dev_) cudaFree(scen_order_dev_);
 	if (ev0_) cudaEventDestroy(ev0_);
 	if (ev1_) cudaEventDestroy(ev1_);
 	if (stream_) cudaStreamDestroy(stream_);
