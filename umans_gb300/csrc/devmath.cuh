@@ -51,15 +51,43 @@ UD float2 vclamp(float2 v, float maxLength)   // clampVector: vector2D.h:241-247
 UD float fminr(float a, float b) { return (b < a) ? b : a; }   // std::min
 UD float fmaxr(float a, float b) { return (a < b) ? b : a; }   // std::max
 
+// (float)((double)a * (double)b - (double)c * (double)d).  The products are
+// exact in double; their difference D is formed exactly as a float expansion
+// (FMA products and TwoSum) and rounded to float.  That equals the
+// double-then-float rounding unless D lies within 2^-10 half-ulp of a float
+// rounding boundary or the subtraction cancels badly; those rare cases take
+// the FP64 path.
+UD float prod_diff_d(float a, float b, float c, float d)
+{
+	const float sh = a * b, sl = fmaf(a, b, -sh);
+	const float th = c * d, tl = fmaf(c, d, -th);
+	const float ah = sh - th;
+	const float bb = ah - sh;
+	const float al = (sh - (ah - bb)) + (-th - bb);
+	const float lo = (sl - tl) + al;
+	const float aah = fabsf(ah);
+	if (aah > 0.0f && fabsf(lo) <= 0x1p-20f * aah && fmaxf(fabsf(sh), fabsf(th)) <= 1024.0f * aah) {
+		const float rh = ah + lo;
+		const float rl = lo - (rh - ah);
+		const uint32_t e = __float_as_uint(rh) & 0x7f800000u;
+		if (e > (25u << 23) && e < (254u << 23)) {
+			const float half_ulp = __uint_as_float(e - (24u << 23));
+			if (fabsf(rl) < half_ulp * 0.9990234375f) return rh;
+		}
+	}
+	return (float)__dsub_rn(__dmul_rn((double)a, (double)b), __dmul_rn((double)c, (double)d));
+}
+
+// pow(x,2) - pow(y,2) of floats in double, then to float
+// (SocialForcesAvoidance.cpp:86)
+UD float sq_diff_d(float x, float y) { return prod_diff_d(x, x, y, y); }
+
 // rotateCounterClockwise with cosf/sinf already evaluated (a float pair):
-// the products are exact in double, the sum is rounded once in double and
-// then to float, exactly as vector2D.h:166-170.
+// each component is a double sum of two exact double products rounded to
+// float, exactly as vector2D.h:166-170 (c*x - s*y and s*x + c*y = s*x - (-c)*y)
 UD float2 vrot_cs(float2 v, float c, float s)
 {
-	const double C = (double)c, S = (double)s;
-	const double x = __dsub_rn(__dmul_rn(C, (double)v.x), __dmul_rn(S, (double)v.y));
-	const double y = __dadd_rn(__dmul_rn(S, (double)v.x), __dmul_rn(C, (double)v.y));
-	return V((float)x, (float)y);
+	return V(prod_diff_d(c, v.x, s, v.y), prod_diff_d(s, v.x, -c, v.y));
 }
 
 // angle(): vector2D.h:172-186, computed exactly in double
@@ -130,33 +158,6 @@ UD bool line_intersection(float2 a, float2 b, float2 c, float2 d, float2* res)
 	res->x = (float)__ddiv_rn(__dsub_rn(__dmul_rn(b2, c1), __dmul_rn(b1, c2)), det);
 	res->y = (float)__ddiv_rn(__dsub_rn(__dmul_rn(a1, c2), __dmul_rn(a2, c1)), det);
 	return true;
-}
-
-// (float)((double)x * (double)x - (double)y * (double)y): pow(x,2) - pow(y,2)
-// of floats (SocialForcesAvoidance.cpp:86).  x^2 and y^2 are exact in double;
-// the difference D is formed exactly as a float expansion (FMA products and
-// TwoSum) and rounded to float.  That equals the double-then-float rounding
-// unless D lies within 2^-10 half-ulp of a float rounding boundary or the
-// subtraction cancels badly; those rare cases take the FP64 path.
-UD float sq_diff_d(float x, float y)
-{
-	const float sh = x * x, sl = fmaf(x, x, -sh);
-	const float th = y * y, tl = fmaf(y, y, -th);
-	const float ah = sh - th;
-	const float bb = ah - sh;
-	const float al = (sh - (ah - bb)) + (-th - bb);
-	const float lo = (sl - tl) + al;
-	const float aah = fabsf(ah);
-	if (aah > 0.0f && fabsf(lo) <= 0x1p-20f * aah && fmaxf(sh, th) <= 1024.0f * aah) {
-		const float rh = ah + lo;
-		const float rl = lo - (rh - ah);
-		const uint32_t e = __float_as_uint(rh) & 0x7f800000u;
-		if (e > (25u << 23) && e < (254u << 23)) {
-			const float half_ulp = __uint_as_float(e - (24u << 23));
-			if (fabsf(rl) < half_ulp * 0.9990234375f) return rh;
-		}
-	}
-	return (float)__dsub_rn(__dmul_rn((double)x, (double)x), __dmul_rn((double)y, (double)y));
 }
 
 // ---------------------------------------------------------------------
