@@ -718,7 +718,7 @@ __device__ float2 orca_solve(const AgentCtx& A, const NbView& N, const CostDesc&
 	}
 	__syncwarp();
 	float2 res;
-	const int fail = lp2(lines, nl, A.maxspeed, A.pref, false, &res);
+	const int fail = lp2(lines, nl, A.maxspeed, A.pref, false, &res, lane);
 	if (fail < nl) lp3(lines, nl, fail, A.maxspeed, &res, proj, lane);
 	*nlines_out = nl;
 	return res;

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(128) k_orca_noalloc(
 			}
 			__syncwarp();
 			float2 best;
-			const int fail = lp2(lines, nl, ms, pv, false, &best);
+			const int fail = lp2(lines, nl, ms, pv, false, &best, lane);
 			if (fail < nl) lp3(lines, nl, fail, ms, &best, proj, lane);
 			float2 acc = vdiv(vsub(best, v), fmaxr(relax, dt));
 			acc = vclamp(acc, ma);

@@ -13,7 +13,12 @@ __device__ __forceinline__ float det2(float2 a, float2 b) { return a.x * b.y - a
 __device__ __forceinline__ float2 lp_point(float4 l) { return V(l.x, l.y); }
 __device__ __forceinline__ float2 lp_dir(float4 l) { return V(l.z, l.w); }
 
-static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res)
+// linearProgram1 (ORCASolver.cpp:173-226), the warp splitting the earlier
+// lines.  tl only grows and tr only shrinks along the reference's loop, so
+// its early exits (a parallel line excluding the whole line, or tl > tr at
+// some prefix) give the same answer as testing the whole set at once; the
+// bounds are the maximum / minimum of the same values.
+static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt, bool dirOpt, float2* res, int lane)
 {
 	const float4 ln = L[lineNo];
 	const float2 P = lp_point(ln), D = lp_dir(ln);
@@ -22,19 +27,28 @@ static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt
 	if (disc < 0.0f) return false;
 	const float sd = sqrtf(disc);
 	float tl = -dp - sd, tr = -dp + sd;
-	for (int i = 0; i < lineNo; ++i) {
+	bool bad = false;
+	for (int i = lane; i < lineNo; i += 32) {
 		const float4 li = L[i];
 		const float den = det2(D, lp_dir(li));
 		const float num = det2(lp_dir(li), vsub(P, lp_point(li)));
 		if (fabsf(den) <= 0.00001f) {
-			if (num < 0.0f) return false;
+			if (num < 0.0f) bad = true;
 			continue;
 		}
 		const float t = num / den;
 		if (den >= 0.0f) tr = fminr(tr, t);
 		else tl = fmaxr(tl, t);
-		if (tl > tr) return false;
 	}
+	for (int o = 16; o > 0; o >>= 1) {
+		tr = fminr(tr, __shfl_xor_sync(0xffffffffu, tr, o));
+		tl = fmaxr(tl, __shfl_xor_sync(0xffffffffu, tl, o));
+	}
+	// one representative for every lane (equal values may differ in the sign
+	// of zero between lanes)
+	tr = __shfl_sync(0xffffffffu, tr, 0);
+	tl = __shfl_sync(0xffffffffu, tl, 0);
+	if (__any_sync(0xffffffffu, bad) || tl > tr) return false;
 	if (dirOpt) {
 		if (vdot(opt, D) > 0.0f) *res = vadd(P, vmul(D, tr));
 		else *res = vadd(P, vmul(D, tl));
@@ -47,17 +61,31 @@ static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt
 	return true;
 }
 
-static __device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res)
+// linearProgram2 (ORCASolver.cpp:228-267): the warp looks for the next line
+// the current result violates 32 lines at a time; lines it satisfies leave
+// the reference's loop unchanged.
+static __device__ int lp2(const float4* L, int n, float radius, float2 opt, bool dirOpt, float2* res, int lane)
 {
 	if (dirOpt) *res = vmul(opt, radius);
 	else if (vsq(opt) > radius * radius) *res = vmul(vnorm(opt), radius);
 	else *res = opt;
-	for (int i = 0; i < n; ++i) {
-		const float4 li = L[i];
-		if (det2(lp_dir(li), vsub(lp_point(li), *res)) > 0.0f) {
-			const float2 tmp = *res;
-			if (!lp1(L, i, radius, opt, dirOpt, res)) { *res = tmp; return i; }
+	int i = 0;
+	while (i < n) {
+		int viol = n;
+		for (int base = i; base < n; base += 32) {
+			const int j = base + lane;
+			bool v = false;
+			if (j < n) {
+				const float4 lj = L[j];
+				v = det2(lp_dir(lj), vsub(lp_point(lj), *res)) > 0.0f;
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, v);
+			if (m) { viol = base + __ffs(m) - 1; break; }
 		}
+		if (viol == n) return n;
+		const float2 tmp = *res;
+		if (!lp1(L, viol, radius, opt, dirOpt, res, lane)) { *res = tmp; return viol; }
+		i = viol + 1;
 	}
 	return n;
 }
@@ -98,7 +126,7 @@ static __device__ void lp3(const float4* L, int n, int begin, float radius, floa
 			}
 			__syncwarp();
 			const float2 tmp = *res;
-			if (lp2(proj, np, radius, V(-Di.y, Di.x), true, res) < np) *res = tmp;
+			if (lp2(proj, np, radius, V(-Di.y, Di.x), true, res, lane) < np) *res = tmp;
 			distance = det2(Di, vsub(Pi, *res));
 			__syncwarp();
 		}
