@@ -1607,9 +1607,6 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		if (!dalloc(scen_order_dev_, scen_order_.size(), err_)) return false;
 		CK(cudaMemcpy(scen_order_dev_, scen_order_.data(), sizeof(int) * scen_order_.size(), cudaMemcpyHostToDevice));
 		d_->scen_order = scen_order_dev_;
-		for (size_t k = 1; k < groups_.size(); ++k) CK(cudaStreamCreateWithFlags(&aux_[k - 1], cudaStreamNonBlocking));
-		CK(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
-		for (cudaEvent_t& e : join_ev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 	}
 	if (!build_tables()) return false;
 	if (!alloc(std::max(n_, 16))) return false;
@@ -1896,7 +1893,6 @@ bool Engine::configure()
 	mode_ = 1;
 	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
 	// one launch shape per kernel group, each with its own line scratch
-	// (groups of a batch run concurrently)
 	size_t scr = 0;
 	for (auto& g : groups_) {
 		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode);
@@ -1956,19 +1952,9 @@ void Engine::enqueue_step()
 		} else if (g.mode == 1) k_agent<1><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
 		else k_agent<0><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
 	};
-	if (groups_.size() == 1 || S.tape_list) {
-		for (size_t k = 0; k < groups_.size(); ++k) launch(k, stream_);
-	} else {
-		// fork: groups 1.. on auxiliary streams, group 0 on the engine's
-		cudaEventRecord(fork_ev_, stream_);
-		for (size_t k = 1; k < groups_.size(); ++k) {
-			cudaStreamWaitEvent(aux_[k - 1], fork_ev_, 0);
-			launch(k, aux_[k - 1]);
-			cudaEventRecord(join_ev_[k - 1], aux_[k - 1]);
-		}
-		launch(0, stream_);
-		for (size_t k = 1; k < groups_.size(); ++k) cudaStreamWaitEvent(stream_, join_ev_[k - 1], 0);
-	}
+	// one after the other: each launch fills the GPU (measured: running the
+	// groups on concurrent streams was no faster)
+	for (size_t k = 0; k < groups_.size(); ++k) launch(k, stream_);
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
 
@@ -2692,10 +2678,8 @@ Engine::~Engine()
 			if (p) cudaFree(p);
 		delete d_;
 	}
-	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_, fork_ev_, join_ev_[0], join_ev_[1] })
+	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_ })
 		if (e) cudaEventDestroy(e);
-	for (cudaStream_t st : aux_)
-		if (st) cudaStreamDestroy(st);
 	if (scen_order_dev_) cudaFree(scen_order_dev_);
 	if (ev0_) cudaEventDestroy(ev0_);
 	if (ev1_) cudaEventDestroy(ev1_);

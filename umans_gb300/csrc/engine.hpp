@@ -175,7 +175,7 @@ private:
 	int prof_steps_ = 0;
 	std::vector<int> pol_scen_;   // scenario of each policy
 	// k_agent launches: one per kernel group (scenarios ordered by group in
-	// cell space); groups after the first run on auxiliary streams
+	// cell space)
 	struct KGroup {
 		int mode;          // k_agent specialisation
 		int j0, j1;        // positions in scen_order_
@@ -185,8 +185,6 @@ private:
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
 	int* scen_order_dev_ = nullptr;
-	cudaStream_t aux_[2] = { nullptr, nullptr };
-	cudaEvent_t fork_ev_ = nullptr, join_ev_[2] = { nullptr, nullptr };
 	AgentRecord* io_host_ = nullptr;   // page-locked staging for AgentData exchange
 	size_t io_host_cap_ = 0;
 	bool stage(size_t records);
