@@ -259,15 +259,22 @@ def cpu_baseline(path: str, n_agents: int, seconds: float = 12.0, threads: int |
                 sample=f"{steps} steps of the full {n_agents}-agent workload after 1 warm-up step")
 
 
-def dist_setup(args):
+def dist_setup(args=None, backend: str | None = None):
+    """One process per GPU under torchrun: every rank runs an independent
+    replica of the workload (the step has no exchange between replicas);
+    the process group only carries the barrier and the max over ranks.
+    NCCL on GPUs; gloo where there is no GPU (the CPU tests)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return rank, world, local, dist
     return rank, world, local, None
 
@@ -281,9 +288,16 @@ def max_over_ranks(dist, x: float) -> float:
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(world: int, agents: int, steps: int, seconds: float) -> float:
+    """Whole-job agent-steps/s of `world` replicas of `agents` agents that
+    all finished `steps` steps within `seconds` (the slowest rank's time)."""
+    return world * agents * steps / seconds
 
 
 def run_reference(args):
@@ -342,7 +356,7 @@ def run_ours(args):
         barrier(dist)
         t_ms = sum(a.elapsed_time(b) for a, b in evs)
         t_ms = max_over_ranks(dist, t_ms)
-        value = world * n * args.steps / (t_ms / 1e3)
+        value = replica_rate(world, n, args.steps, t_ms / 1e3)
         # --- back-to-back steps (L2 warm), for reference ------------------
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -396,7 +410,7 @@ def run_ours(args):
         te = time.perf_counter() - te
         te = max_over_ranks(dist, te)
         u.cleanUp()
-        e2e_value = world * n * args.steps / te
+        e2e_value = replica_rate(world, n, args.steps, te)
         cpu = cpu_baseline(path, n) if (rank == 0 and world == 1 and not args.no_cpu) else None
         batched = None if args.no_batch else batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
         diff = None if args.no_diff else diff_leg(tmp, sets=args.diff_sets)
