@@ -172,6 +172,10 @@ int umans_get_force_params(umans_sim* sim, int scenario, float* params4);
  * values and reports the size of the exception table.  Errors are reported
  * through umans_last_error(NULL). */
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions);
+/* Test hook: the device's (float)((double)a*b - (double)c*d) on n quadruples
+ * abcd[4*i .. 4*i+3] (the promoted products of SocialForcesAvoidance.cpp:86
+ * and vector2D.h:166-170).  Errors: umans_last_error(NULL). */
+int umans_debug_prod_diff(const float* abcd, float* y, int n);
 /* ORCA velocities without allocation.  No counterpart in the reference.
  *
  * For callers that cannot allocate GPU memory at the moment they need a

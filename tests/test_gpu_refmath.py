@@ -43,3 +43,49 @@ def test_ref_expf_random_and_edges():
     ref = libm_expf(x)
     bad = np.nonzero(y.view(np.uint32) != ref.view(np.uint32))[0]
     assert bad.size == 0, f"{bad.size} mismatches, e.g. x={x[bad[:5]]} got {y[bad[:5]]} want {ref[bad[:5]]}"
+
+
+def device_prod_diff(a, b, c, d):
+    lib = _lib.load()
+    q = np.ascontiguousarray(np.stack([a, b, c, d], 1), np.float32)
+    y = np.empty(q.shape[0], np.float32)
+    rc = lib.umans_debug_prod_diff(q.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p), q.shape[0])
+    assert rc == 0, lib.umans_last_error(None)
+    return y
+
+
+def host_prod_diff(a, b, c, d):
+    f64 = np.float64
+    return (f64(a) * f64(b) - f64(c) * f64(d)).astype(np.float32)
+
+
+def test_prod_diff_matches_double_then_float():
+    """(float)((double)a*b - (double)c*d): random operands over many scales,
+    squared differences, rotations of unit vectors, heavy cancellation, and
+    results placed next to float rounding midpoints."""
+    rng = np.random.default_rng(7)
+    n = 4_000_000
+    cases = []
+    f32 = np.float32
+    sc = np.exp2(rng.integers(-20, 20, n)).astype(f32)
+    cases.append((rng.standard_normal(n).astype(f32) * sc, rng.standard_normal(n).astype(f32),
+                  rng.standard_normal(n).astype(f32) * sc, rng.standard_normal(n).astype(f32)))
+    x = rng.uniform(0, 20, n).astype(f32)
+    y = (x + rng.standard_normal(n).astype(f32) * np.float32(1e-3)).astype(f32)
+    cases.append((x, x, y, y))                                   # x^2 - y^2, cancelling
+    ang = rng.uniform(-np.pi, np.pi, n)
+    cs, sn = np.cos(ang).astype(f32), np.sin(ang).astype(f32)
+    v = rng.standard_normal((n, 2)).astype(f32)
+    cases.append((cs, v[:, 0], sn, v[:, 1]))                     # rotation, x
+    cases.append((sn, v[:, 0], -cs, v[:, 1]))                    # rotation, y
+    # a - c*d with c*d about half an ulp of a: results next to midpoints
+    a = rng.uniform(1, 2, n).astype(f32)
+    ulp = np.spacing(a)
+    c = rng.uniform(0.5, 1, n).astype(f32)
+    d = (ulp * rng.uniform(0.45, 0.55, n) / c).astype(f32)
+    cases.append((a, np.ones(n, f32), c, d))
+    for k, (a, b, c, d) in enumerate(cases):
+        got = device_prod_diff(a, b, c, d)
+        want = host_prod_diff(a, b, c, d)
+        bad = np.flatnonzero(got.view(np.uint32) != want.view(np.uint32))
+        assert bad.size == 0, (k, bad[:5], a[bad[:5]], b[bad[:5]], c[bad[:5]], d[bad[:5]], got[bad[:5]], want[bad[:5]])

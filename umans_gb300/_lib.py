@@ -70,6 +70,7 @@ _SIGS = {
     "umans_set_force_params": (C.c_int, [P, C.c_int, P]),
     "umans_get_force_params": (C.c_int, [P, C.c_int, P]),
     "umans_debug_ref_expf": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_size_t)]),
+    "umans_debug_prod_diff": (C.c_int, [P, P, C.c_int]),
     "umans_orca_velocities_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, C.c_float,
                                                 C.c_float, C.c_float, C.c_float, P, P]),
     "umans_last_error": (C.c_char_p, [P]),

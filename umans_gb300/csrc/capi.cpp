@@ -323,6 +323,14 @@ int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 	return UMANS_OK;
 }
 
+int umans_debug_prod_diff(const float* abcd, float* y, int n)
+{
+	if ((n > 0 && (!abcd || !y)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	std::string err;
+	if (!umans::debug_prod_diff(abcd, y, n, err)) return fail(nullptr, UMANS_ERR_CUDA, err);
+	return UMANS_OK;
+}
+
 int umans_orca_velocities_noalloc(int n, const float* pos, const float* vel, const float* pref, const float* radius,
                                   const float* max_speed, const float* max_accel, const int* nbr_index,
                                   const float* nbr_dist2, const int* nbr_count, int nbr_cap, float range,

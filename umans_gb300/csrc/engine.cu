@@ -542,19 +542,19 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 				const int v = __shfl_up_sync(0xffffffffu, incl, o);
 				if (lane >= o) incl += v;
 			}
-			int rbeg[ROWS], rst[ROWS];
-#pragma unroll
-			for (int k = 0; k < ROWS; ++k) {
-				rst[k] = __shfl_sync(0xffffffffu, rs, k);
-				rbeg[k] = __shfl_sync(0xffffffffu, incl - len, k);
-			}
+			// lane k < ROWS holds row k's start in the concatenation (rows past
+			// nr are empty and start at the total)
+			const int beg = incl - len;
 			const int total = __shfl_sync(0xffffffffu, incl, ROWS - 1);
 			for (int base = 0; base < total; base += 32) {
 				const int c = base + lane;
-				int tt = -1;
+				// the last row starting at or before c (binary search over the
+				// ROWS starts, held by lanes 0..ROWS-1)
+				int r = 0;
 #pragma unroll
-				for (int k = 0; k < ROWS; ++k)
-					if (k < nr && c >= rbeg[k]) tt = rst[k] + (c - rbeg[k]);
+				for (int step = ROWS / 2; step > 0; step >>= 1)
+					if (__shfl_sync(0xffffffffu, beg, r + step) <= c) r += step;
+				const int tt = __shfl_sync(0xffffffffu, rs, r) + (c - __shfl_sync(0xffffffffu, beg, r));
 				bool ok = false;
 				float d2f = 0;
 				if (c < total && tt != t) {
@@ -1239,6 +1239,32 @@ __global__ void k_ref_expf(ExpExceptions T, const float* x, float* y, int n)
 }
 
 // Evaluates the device's reference-exact expf on n host values (tests).
+__global__ void k_prod_diff(const float4* abcd, float* y, int n)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) {
+		const float4 q = abcd[i];
+		y[i] = prod_diff_d(q.x, q.y, q.z, q.w);
+	}
+}
+
+// Evaluates the device's (float)((double)a*b - (double)c*d) on n host
+// quadruples (tests).
+bool debug_prod_diff(const float* abcd, float* y, int n, std::string& err)
+{
+	float4* dq = nullptr;
+	float* dy = nullptr;
+	if (cudaMalloc(&dq, sizeof(float4) * std::max(n, 1)) != cudaSuccess ||
+	    cudaMalloc(&dy, sizeof(float) * std::max(n, 1)) != cudaSuccess) { err = "cudaMalloc"; return false; }
+	cudaMemcpy(dq, abcd, sizeof(float4) * n, cudaMemcpyHostToDevice);
+	if (n > 0) k_prod_diff<<<(n + 255) / 256, 256>>>(dq, dy, n);
+	cudaError_t e = cudaMemcpy(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost);
+	cudaFree(dq);
+	cudaFree(dy);
+	if (e != cudaSuccess) { err = cudaGetErrorString(e); return false; }
+	return true;
+}
+
 bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err)
 {
 	ExpExceptions T;

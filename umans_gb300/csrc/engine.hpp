@@ -18,6 +18,8 @@ struct DevState;   // device pointers (engine.cu)
 
 // device evaluation of the reference-exact expf (refmath.hpp), for tests
 bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err);
+// device evaluation of (float)((double)a*b - (double)c*d) (devmath.cuh), for tests
+bool debug_prod_diff(const float* abcd, float* y, int n, std::string& err);
 
 struct EngineOptions {
 	int max_neighbours = 0;        // 0: chosen from the initial state
