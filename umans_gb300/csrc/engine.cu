@@ -1551,6 +1551,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	CK(cudaGetDevice(&dev));
 	CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
 	CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+	CK(cudaMallocHost(&status_host_, sizeof(int)));
 	for (cudaEvent_t* e : { &ev0_, &ev1_, &pa0_, &pa1_, &ps0_, &ps1_ }) CK(cudaEventCreate(e));
 	d_ = new DevState();
 	std::memset(d_, 0, sizeof(DevState));
@@ -2090,6 +2091,16 @@ bool Engine::run_steps(int nsteps)
 // The mutable per-agent state at the start of a batch of steps, kept so that
 // a batch in which some neighbour list outgrew the capacity can be re-run
 // with a larger capacity (every step is then computed with complete lists).
+// the mutable state copied in one launch (position, velocity, view,
+// velocity without forces, random state)
+__global__ void k_copy_state(int n, const float2* p, const float2* v, const float2* w, const float2* f,
+                             const uint32_t* r, float2* P, float2* Vv, float2* W, float2* F, uint32_t* R)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	P[i] = p[i]; Vv[i] = v[i]; W[i] = w[i]; F[i] = f[i]; R[i] = r[i];
+}
+
 bool Engine::take_snapshot()
 {
 	DevState& S = *d_;
@@ -2101,11 +2112,9 @@ bool Engine::take_snapshot()
 			return false;
 	}
 	if (n_ > 0) {
-		CK(cudaMemcpyAsync(snap_pos_, S.pos, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
-		CK(cudaMemcpyAsync(snap_vel_, S.vel, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
-		CK(cudaMemcpyAsync(snap_view_, S.view, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
-		CK(cudaMemcpyAsync(snap_vwf_, S.vwf, sizeof(float2) * n_, cudaMemcpyDeviceToDevice, stream_));
-		CK(cudaMemcpyAsync(snap_rng_, S.rng, sizeof(uint32_t) * n_, cudaMemcpyDeviceToDevice, stream_));
+		k_copy_state<<<(n_ + 255) / 256, 256, 0, stream_>>>(n_, S.pos, S.vel, S.view, S.vwf, S.rng, snap_pos_, snap_vel_,
+		                                                    snap_view_, snap_vwf_, snap_rng_);
+		CK(cudaGetLastError());
 	}
 	snap_valid_ = true;
 	snap_time_ = time_;
@@ -2167,9 +2176,11 @@ bool Engine::sync()
 {
 	if (!steps_pending_) return true;   // nothing enqueued since the last check
 	for (;;) {
+		// the status word follows the steps on the stream into page-locked
+		// host memory: one synchronisation
+		CK(cudaMemcpyAsync(status_host_, d_->status, sizeof(int), cudaMemcpyDeviceToHost, stream_));
 		CK(cudaStreamSynchronize(stream_));
-		int st = 0;
-		CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
+		const int st = *status_host_;
 		if (st == 0) {
 			snap_valid_ = false;
 			steps_pending_ = false;
@@ -2693,6 +2704,7 @@ Engine::~Engine()
 	invalidate_graph();
 	diff_free();
 	if (io_host_) cudaFreeHost(io_host_);
+	if (status_host_) cudaFreeHost(status_host_);
 	if (d_) {
 		DevState& S = *d_;
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,

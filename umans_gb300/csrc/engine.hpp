@@ -188,6 +188,7 @@ private:
 	std::vector<int> scen_order_;
 	int* scen_order_dev_ = nullptr;
 	AgentRecord* io_host_ = nullptr;   // page-locked staging for AgentData exchange
+	int* status_host_ = nullptr;       // page-locked copy of the device status word
 	size_t io_host_cap_ = 0;
 	bool stage(size_t records);
 
