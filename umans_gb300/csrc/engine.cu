@@ -449,43 +449,72 @@ __device__ __forceinline__ double exact_key(float2 q, float2 c)
 // 2.5e-7 (one rounding of each difference, square and sum), so two keys more
 // than 1e-6 apart order as the exact ones do; closer pairs are compared on the
 // reference's double distance, then the id.
+// insertion sort of the run [r0, r1] (lane 0) in the reference's order
+__device__ void sort_run(const DevState& S, const WarpLists& L, int r0, int r1, float2 q)
+{
+	for (int x = r0 + 1; x <= r1; ++x) {
+		const uint32_t rx = L.ref[x];
+		const float kx = L.key[x];
+		int y = x - 1;
+		while (y >= r0) {
+			const uint32_t ry = L.ref[y];
+			const float ky = L.key[y];
+			bool after;   // entry y belongs after entry x
+			if (ky - kx > 1e-6f * ky) after = true;
+			else if (kx - ky > 1e-6f * kx) after = false;
+			else {
+				const double dx = exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
+				const double dy = exact_key(q, S.sP[ry & 0x0FFFFFFFu]);
+				after = dy > dx || (dy == dx && S.sId[ry & 0x0FFFFFFFu] > S.sId[rx & 0x0FFFFFFFu]);
+			}
+			if (!after) break;
+			L.ref[y + 1] = ry; L.key[y + 1] = ky;
+			--y;
+		}
+		L.ref[y + 1] = rx; L.key[y + 1] = kx;
+	}
+}
+
 __device__ void fix_near_ties(const DevState& S, const WarpLists& L, int s, int e, float2 q, int lane, float win)
 {
-	bool close = false;
-	for (int k = s + lane; k + 1 < e; k += 32) {
-		const float a = L.key[k], b = L.key[k + 1];
-		if (b - a <= win * b) close = true;
+	// flags of the adjacent pairs (k, k+1) whose keys are within the window,
+	// one bit per pair, 32 pairs per word in the (free) aux list.  Runs are
+	// the maximal sequences of flagged pairs; re-sorting a run only permutes
+	// keys inside it, so all flags can be taken from the keys as sorted.
+	unsigned* words = reinterpret_cast<unsigned*>(L.aux);
+	const int npairs = e - 1 - s;
+	unsigned any = 0;
+	for (int w = 0; 32 * w < npairs; ++w) {
+		const int k = s + 32 * w + lane;
+		bool close = false;
+		if (k + 1 < e) {
+			const float a = L.key[k], b = L.key[k + 1];
+			close = b - a <= win * b;
+		}
+		const unsigned m = __ballot_sync(0xffffffffu, close);
+		if (lane == 0) words[w] = m;
+		any |= m;
 	}
-	if (!__any_sync(0xffffffffu, close)) return;
+	if (!any) return;
+	__syncwarp();
 	if (lane == 0) {
-		int k = s;
-		while (k + 1 < e) {
-			if (!(L.key[k + 1] - L.key[k] <= win * L.key[k + 1])) { ++k; continue; }
-			const int r0 = k;
-			while (k + 1 < e && L.key[k + 1] - L.key[k] <= win * L.key[k + 1]) ++k;
-			const int r1 = k;   // inclusive
-			for (int x = r0 + 1; x <= r1; ++x) {
-				const uint32_t rx = L.ref[x];
-				const float kx = L.key[x];
-				int y = x - 1;
-				while (y >= r0) {
-					const uint32_t ry = L.ref[y];
-					const float ky = L.key[y];
-					bool after;   // entry y belongs after entry x
-					if (ky - kx > 1e-6f * ky) after = true;
-					else if (kx - ky > 1e-6f * kx) after = false;
-					else {
-						const double dx = exact_key(q, S.sP[rx & 0x0FFFFFFFu]);
-						const double dy = exact_key(q, S.sP[ry & 0x0FFFFFFFu]);
-						after = dy > dx || (dy == dx && S.sId[ry & 0x0FFFFFFFu] > S.sId[rx & 0x0FFFFFFFu]);
-					}
-					if (!after) break;
-					L.ref[y + 1] = ry; L.key[y + 1] = ky;
-					--y;
-				}
-				L.ref[y + 1] = rx; L.key[y + 1] = kx;
-			}
-			++k;
+		const int nw = (npairs + 31) / 32;
+		int p = 0;   // next pair to look at
+		while (p < npairs) {
+			// first flagged pair at or after p
+			int w = p >> 5;
+			unsigned m = words[w] & (~0u << (p & 31));
+			while (!m && ++w < nw) m = words[w];
+			if (!m) break;
+			const int r0 = 32 * w + __ffs(m) - 1;
+			// first unflagged pair after it (or the end)
+			int u = r0 >> 5;
+			unsigned z = ~words[u] & (~0u << (r0 & 31));
+			while (!z && ++u < nw) z = ~words[u];
+			const int r1 = z ? min(32 * u + __ffs(z) - 1, npairs) : npairs;
+			// pairs r0 .. r1-1 flagged: entries r0 .. r1 form the run
+			sort_run(S, L, s + r0, s + r1, q);
+			p = r1 + 1;
 		}
 	}
 	__syncwarp();
