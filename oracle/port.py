@@ -245,8 +245,20 @@ def read_scenario(path: str) -> dict:
             g = (_f32(ge.get("x")), _f32(ge.get("y"))) if ge is not None else p
             ids.append(aid); pos.append(p); goal.append(g); rad.append(r); pref.append(ps)
             maxs.append(ms); maxa.append(ma); pidx.append(policy_ids.index(_int(pol.get("id"))))
+    # obstacles (crowdSimulator.cpp:496-514, 633-645): every polygon's
+    # closed outline, polygons in file order (Polygon2D.cpp:27-35)
+    edges = []
+    oblock = world.find("Obstacles")
+    if oblock is not None:
+        oblock = _load_block(oblock, folder, "Obstacles")
+        for oe in _children_from_first(oblock, "Obstacle"):
+            pts = [(_f32(pe.get("x", "0")), _f32(pe.get("y", "0"))) for pe in oe.findall("Point")]
+            for k in range(len(pts)):
+                a, b = pts[k], pts[(k + 1) % len(pts)]
+                edges.append((a[0], a[1], b[0], b[1]))
     f = np.float32
     return dict(world=1 if toric else 0, width=width, height=height, dt=dt, end_time=end_time,
+                edges=np.array(edges, f).reshape(-1, 4),
                 policies=policies, ids=np.array(ids, np.int64),
                 pos=np.array(pos, f).reshape(-1, 2), goal=np.array(goal, f).reshape(-1, 2),
                 radius=np.array(rad, f), pref_speed=np.array(pref, f), max_speed=np.array(maxs, f),
@@ -284,6 +296,7 @@ def _load():
         lib.up_set_state.argtypes = [P, P, P, P]
         lib.up_neighbors.argtypes = [P, C.c_int, P, P, P, P, C.c_int]
         lib.up_libm_expf.argtypes = [P, P, C.c_long]
+        lib.up_set_obstacles.argtypes = [P, C.c_int, P]
         _lib = lib
     return _lib
 
@@ -313,6 +326,10 @@ class PortSim:
                       ("ids", "pos", "goal", "radius", "pref_speed", "max_speed", "max_accel", "policy_index")]
         self._h = lib.up_create(len(s["ids"]), s["world"], s["width"], s["height"], s["dt"],
                                 C.cast(pols, C.c_void_p), len(s["policies"]), *(_p(a) for a in self._keep))
+        edges = np.ascontiguousarray(s.get("edges", np.zeros((0, 4), np.float32)), np.float32)
+        if edges.shape[0]:
+            self._keep.append(edges)
+            lib.up_set_obstacles(self._h, edges.shape[0], _p(edges))
 
     def close(self):
         if self._h:

@@ -116,6 +116,8 @@ typedef struct {
 } nbr;
 
 typedef struct { nbr* v; int n, cap; } nbrlist;
+typedef struct { v2 a, b; } seg;
+typedef struct { seg* v; int n, cap; } seglist;
 
 struct up_world {
 	int n, type;
@@ -129,6 +131,10 @@ struct up_world {
 	int* policy;
 	uint32_t* rng;
 	nbrlist* nb;
+	/* obstacle edges (Polygon2D edges in file order) and each agent's list */
+	seg* edges;
+	int ne;
+	seglist* ob;
 	/* grid */
 	int *cell_start, *cell_items, gnx, gny, gcells_cap;
 	float gx0, gy0, gcs;
@@ -268,20 +274,72 @@ static void query_group(const up_world* w, int self, v2 q0, v2 q, float r, v2 of
 	nb_sort(L->v + start, L->n - start, w->id);
 }
 
+/* nearestPointOnLine(pt, la, lb, onSegment = true): vector2D.h:274-296 */
+static inline v2 nearest_on_segment(v2 pt, v2 la, v2 lb)
+{
+	if (la.x == lb.x && la.y == lb.y) return la;
+	const v2 line = vsub(la, lb);
+	float k = vdot(vsub(pt, lb), line) / vsq(line);
+	if (k > 1) k = 1;
+	else if (k < 0) k = 0;
+	return vadd(vmul(la, k), vmul(lb, 1 - k));
+}
+/* distanceToLineSquared(pt, la, lb, true): vector2D.h:303-306 */
+static inline float dist2_to_segment(v2 pt, v2 la, v2 lb) { return vsq(vsub(pt, nearest_on_segment(pt, la, lb))); }
+
+static void seg_push(seglist* L, seg e)
+{
+	if (L->n == L->cap) {
+		L->cap = L->cap ? 2 * L->cap : 16;
+		L->v = (seg*)realloc(L->v, sizeof(seg) * (size_t)L->cap);
+	}
+	L->v[L->n++] = e;
+}
+
+/* computeNeighboringObstacles_Flat (worldBase.cpp:62-77) at the displaced
+ * query point q, edges shifted by -displacement (worldToric.cpp:50-58) */
+static void query_obstacles(const up_world* w, v2 q, float r, v2 disp, int displaced, seglist* L)
+{
+	const float r2 = r * r;
+	for (int k = 0; k < w->ne; ++k) {
+		const seg e = w->edges[k];
+		if (dist2_to_segment(q, e.a, e.b) <= r2) {
+			seg o = e;
+			if (displaced) { o.a = vsub(e.a, disp); o.b = vsub(e.b, disp); }
+			seg_push(L, o);
+		}
+	}
+}
+
 static void compute_neighbors(up_world* w, int i)
 {
 	nbrlist* L = &w->nb[i];
+	seglist* O = &w->ob[i];
 	L->n = 0;
+	O->n = 0;
 	const float r = policy_range(&w->pol[w->policy[i]]);
 	const v2 p = w->pos[i];
 	query_group(w, i, p, p, r, V(0, 0), L);
+	query_obstacles(w, p, r, V(0, 0), 0, O);
 	if (w->type == UP_TORIC) {
 		const float W = w->width, H = w->height;
 		/* worldToric.cpp:61-79: four axis displacements, no diagonals */
-		if (p.x - r < -0.5 * W) query_group(w, i, p, vadd(p, V(W, 0)), r, V(-W, -0.0f), L);
-		if (p.x + r > 0.5 * W) query_group(w, i, p, vadd(p, V(-W, 0)), r, V(W, -0.0f), L);
-		if (p.y - r < -0.5 * H) query_group(w, i, p, vadd(p, V(0, H)), r, V(-0.0f, -H), L);
-		if (p.y + r > 0.5 * H) query_group(w, i, p, vadd(p, V(0, -H)), r, V(-0.0f, H), L);
+		if (p.x - r < -0.5 * W) {
+			query_group(w, i, p, vadd(p, V(W, 0)), r, V(-W, -0.0f), L);
+			query_obstacles(w, vadd(p, V(W, 0)), r, V(W, 0), 1, O);
+		}
+		if (p.x + r > 0.5 * W) {
+			query_group(w, i, p, vadd(p, V(-W, 0)), r, V(W, -0.0f), L);
+			query_obstacles(w, vadd(p, V(-W, 0)), r, V(-W, 0), 1, O);
+		}
+		if (p.y - r < -0.5 * H) {
+			query_group(w, i, p, vadd(p, V(0, H)), r, V(-0.0f, -H), L);
+			query_obstacles(w, vadd(p, V(0, H)), r, V(0, H), 1, O);
+		}
+		if (p.y + r > 0.5 * H) {
+			query_group(w, i, p, vadd(p, V(0, -H)), r, V(-0.0f, H), L);
+			query_obstacles(w, vadd(p, V(0, -H)), r, V(0, -H), 1, O);
+		}
 	}
 }
 
@@ -314,10 +372,41 @@ static inline float ttc_pair(v2 p1, v2 v1, float r1, v2 p2, v2 v2_, float r2)
 	return fminr(t1, t2);
 }
 
+/* ComputeTimeToCollision_LineSegmentInterior: costFunction.cpp:293-325 */
+static float ttc_segment_interior(v2 p, v2 v, float r, v2 a, v2 b)
+{
+	if (dist2_to_segment(p, a, b) <= r * r) return 0;
+	v2 X;
+	if (!line_intersection(p, vadd(p, v), a, b, &X)) return MAXF;
+	if (vdot(v, vsub(X, p)) < 0) return MAXF;
+	const v2 line = vsub(a, b);
+	const float k = vdot(vsub(X, b), line) / vsq(line);
+	if (!(k >= 0 && k <= 1)) return MAXF;
+	const float speed = vmag(v);
+	const float t = vmag(vsub(X, p)) / speed;
+	const float ang = vangle(v, vsub(b, a));
+	const float sub = r / sinf(ang);
+	const float tsub = sub / speed;
+	return fmaxr(0.0f, t - tsub);
+}
+
+/* ComputeTimeToCollision_LineSegment: costFunction.cpp:270-291 */
+static float ttc_segment(v2 p, v2 v, float r, v2 a, v2 b)
+{
+	const float t1 = ttc_pair(p, v, r, a, V(0, 0), 0);
+	if (t1 == 0) return 0;
+	if (a.x == b.x && a.y == b.y) return t1;
+	const float t2 = ttc_pair(p, v, r, b, V(0, 0), 0);
+	if (t2 == 0) return 0;
+	const float ti = ttc_segment_interior(p, v, r, a, b);
+	return fminr(fminr(t1, t2), ti);
+}
+
 typedef struct {
 	const up_world* w;
 	int i;
 	const nbrlist* L;
+	const seglist* O;
 	v2 pos, vel, pref, goal;
 	float radius, prefspeed, maxspeed, maxacc, dt, relax;
 } actx;
@@ -330,6 +419,14 @@ static inline float ttc_first(const actx* A, v2 pos, v2 vel, float radius, float
 		const nbr* e = &A->L->v[k];
 		if (e->d2 > md2) continue;
 		float t = ttc_pair(pos, vel, radius, e->pos, A->w->vel[e->j], A->w->radius[e->j]);
+		if (ignoreCurrent && t == 0) continue;
+		if (t < minT) minT = t;
+	}
+	/* neighbouring obstacles: costFunction.cpp:251-265 */
+	for (int k = 0; k < A->O->n; ++k) {
+		const seg e = A->O->v[k];
+		if (dist2_to_segment(pos, e.a, e.b) > md2) continue;
+		float t = ttc_segment(pos, vel, radius, e.a, e.b);
 		if (ignoreCurrent && t == 0) continue;
 		if (t < minT) minT = t;
 	}
@@ -424,7 +521,25 @@ static v2 compute_force(const actx* A, const up_cost* c)
 			F.x += f.x; F.y += f.y;
 		}
 	}
-	return vadd(F, V(0, 0));
+	v2 O = V(0, 0);
+	for (int k = 0; k < A->O->n; ++k) {
+		const seg e = A->O->v[k];
+		if (dist2_to_segment(A->pos, e.a, e.b) <= rs) {
+			v2 f = V(0, 0);   /* PowerLaw: no obstacle force (PowerLaw.cpp:68-72) */
+			if (c->kind == UP_SOCIALFORCES) {
+				/* SocialForcesAvoidance::ComputeObstacleInteractionForce: .cpp:112-140 */
+				const v2 diff = vsub(A->pos, nearest_on_segment(A->pos, e.a, e.b));
+				const float dist = vmag(diff);
+				if (!(dist < 0.001f)) {
+					const float U0 = c->p[3], R = c->p[4];
+					const float dU = -U0 / R * expf(-dist / R);
+					f = vmul(V(-diff.x, -diff.y), dU);
+				}
+			}
+			O.x += f.x; O.y += f.y;
+		}
+	}
+	return vadd(F, O);
 }
 
 static v2 target_velocity(const actx* A, const up_cost* c)
@@ -1037,13 +1152,20 @@ static v2 contact_forces(const actx* A, const up_policy* pol)
 			const float inter = A->radius + A->w->radius[e->j] - vmag(diff);
 			if (inter > 0) total = vadd(total, vmul(vnorm(diff), pol->contact_scale * inter));
 		}
+		/* colliding obstacles: policy.cpp:126-137 */
+		for (int k = 0; k < A->O->n; ++k) {
+			const seg e = A->O->v[k];
+			const v2 diff = vsub(A->pos, nearest_on_segment(A->pos, e.a, e.b));
+			const float inter = A->radius - vmag(diff);
+			if (inter > 0) total = vadd(total, vmul(vnorm(diff), pol->contact_scale * inter));
+		}
 	}
 	return total;
 }
 
 static void make_ctx(up_world* w, int i, actx* A)
 {
-	A->w = w; A->i = i; A->L = &w->nb[i];
+	A->w = w; A->i = i; A->L = &w->nb[i]; A->O = &w->ob[i];
 	A->pos = w->pos[i]; A->vel = w->vel[i]; A->pref = w->pref[i]; A->goal = w->goal[i];
 	A->radius = w->radius[i]; A->prefspeed = w->prefspeed[i]; A->maxspeed = w->maxspeed[i];
 	A->maxacc = w->maxacc[i]; A->dt = w->dt; A->relax = w->pol[w->policy[i]].relax_time;
@@ -1117,6 +1239,7 @@ up_world* up_create(int n, int world_type, float width, float height, float dt,
 	w->policy = (int*)calloc(N, sizeof(int));
 	w->rng = (uint32_t*)calloc(N, sizeof(uint32_t));
 	w->nb = (nbrlist*)calloc(N, sizeof(nbrlist));
+	w->ob = (seglist*)calloc(N, sizeof(seglist));
 	for (int i = 0; i < n; ++i) {
 		w->id[i] = ids[i];
 		w->pos[i] = V(pos[2 * i], pos[2 * i + 1]);
@@ -1135,12 +1258,23 @@ up_world* up_create(int n, int world_type, float width, float height, float dt,
 void up_free(up_world* w)
 {
 	if (!w) return;
-	for (int i = 0; i < w->n; ++i) free(w->nb[i].v);
-	free(w->nb); free(w->pol); free(w->id);
+	for (int i = 0; i < w->n; ++i) { free(w->nb[i].v); free(w->ob[i].v); }
+	free(w->nb); free(w->ob); free(w->edges); free(w->pol); free(w->id);
 	free(w->pos); free(w->vel); free(w->goal); free(w->pref); free(w->next); free(w->vwf);
 	free(w->view); free(w->contact); free(w->radius); free(w->prefspeed); free(w->maxspeed);
 	free(w->maxacc); free(w->policy); free(w->rng); free(w->cell_start); free(w->cell_items);
 	free(w);
+}
+
+void up_set_obstacles(up_world* w, int ne, const float* edges)
+{   /* WorldBase::AddObstacle (worldBase.cpp:239-242): edges (ax, ay, bx, by) */
+	free(w->edges);
+	w->ne = ne;
+	w->edges = (seg*)malloc(sizeof(seg) * (size_t)(ne > 0 ? ne : 1));
+	for (int k = 0; k < ne; ++k) {
+		w->edges[k].a = V(edges[4 * k], edges[4 * k + 1]);
+		w->edges[k].b = V(edges[4 * k + 2], edges[4 * k + 3]);
+	}
 }
 
 int up_num_agents(const up_world* w) { return w->n; }

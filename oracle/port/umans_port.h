@@ -70,6 +70,8 @@ up_world* up_create(int n, int world_type, float width, float height, float dt,
                     const float* radius, const float* pref_speed, const float* max_speed,
                     const float* max_accel, const int* policy_index);
 void up_free(up_world* w);
+/* static obstacle edges (ax, ay, bx, by), in file order */
+void up_set_obstacles(up_world* w, int ne, const float* edges);
 int up_num_agents(const up_world* w);
 double up_time(const up_world* w);
 /* runs n steps with `threads` OpenMP threads; returns wall seconds */

@@ -73,6 +73,10 @@ def main():
         run(f"circle24_{m}", S.model_circle(m), 100, every=5)
         run(f"crossing40_{m}", S.model_crossing(m), 100, every=5)
         run(f"toric60_{m}", S.model_toric(m, side=8.0), 100, every=5, nb_steps=(1,))
+    for m in S.MODEL_POLICIES:
+        run(f"obstacle_crossing40_{m}", S.model_obstacle_crossing(m), 100, every=5)
+        run(f"corridor_walls40_{m}", S.model_corridor_walls(m), 100, every=5)
+        run(f"toric_obstacle60_{m}", S.model_toric_obstacle(m), 100, every=5)
     run("orca_circle50", S.circle_orca(50), 100, every=5, nb_steps=(1, 50))
     run("socialforces_toric1500", S.socialforces_toric(n=1500, density=0.625), 100, every=10,
         nb_steps=(1, 100), nb_agents=150)

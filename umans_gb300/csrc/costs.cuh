@@ -24,6 +24,10 @@ struct NbView {
 	const float4* sB;        // cell-sorted (pref.x, pref.y, radius, -)
 	const float4* sE;        // cell-sorted (normalised pref.x, pref.y, speed, -)
 	float W, H;              // toric world size (PhantomAgent offsets)
+	// obstacle edges within range: (displacement group << 28) | edge index
+	const float4* edges;
+	const uint32_t* obs;
+	int KO;
 };
 
 // PhantomAgent position offset of displacement group g (worldToric.cpp:61-79):
@@ -34,6 +38,31 @@ UD float2 group_offset(uint32_t g, float W, float H)
 	const float ox = g == 1 ? -W : (g == 2 ? W : (g == 0 ? 0.0f : -0.0f));
 	const float oy = g == 3 ? -H : (g == 4 ? H : (g == 0 ? 0.0f : -0.0f));
 	return V(ox, oy);
+}
+
+// displacement of group g (worldToric.cpp:65-76): 1 (W, 0), 2 (-W, 0),
+// 3 (0, H), 4 (0, -H)
+UD float2 group_disp(uint32_t g, float W, float H)
+{
+	const float dx = g == 1 ? W : (g == 2 ? -W : 0.0f);
+	const float dy = g == 3 ? H : (g == 4 ? -H : 0.0f);
+	return V(dx, dy);
+}
+
+// obstacle entry k: the edge, shifted by -displacement for displaced
+// queries (worldToric.cpp:55-58)
+UD void nb_seg(const NbView& N, int k, float2* a, float2* b)
+{
+	const uint32_t e = N.obs[k];
+	const float4 E = N.edges[e & 0x0FFFFFFFu];
+	*a = V(E.x, E.y);
+	*b = V(E.z, E.w);
+	const uint32_t g = e >> 28;
+	if (g != 0) {
+		const float2 d = group_disp(g, N.W, N.H);
+		*a = vsub(*a, d);
+		*b = vsub(*b, d);
+	}
 }
 
 UD float2 nb_pos(const NbView& N, int k)
@@ -57,7 +86,7 @@ struct AgentCtx {
 	ExpExceptions ex;    // host-expf exceptions (refmath.hpp)
 };
 
-// ComputeTimeToFirstCollision: costFunction.cpp:229-268 (agents only)
+// ComputeTimeToFirstCollision: costFunction.cpp:229-268
 UD float ttc_first(const AgentCtx& A, const NbView& N, float2 vel, float maxDist, bool ignoreCurrent)
 {
 	float minT = MAXF;
@@ -65,6 +94,14 @@ UD float ttc_first(const AgentCtx& A, const NbView& N, float2 vel, float maxDist
 	for (int k = 0; k < N.K; ++k) {
 		if (N.d2[k] > md2) continue;
 		const float t = ttc_pair(A.pos, vel, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+		if (ignoreCurrent && t == 0) continue;
+		if (t < minT) minT = t;
+	}
+	for (int k = 0; k < N.KO; ++k) {
+		float2 a, b;
+		nb_seg(N, k, &a, &b);
+		if (dist2_to_segment(A.pos, a, b) > md2) continue;
+		const float t = ttc_segment(A.pos, vel, A.radius, a, b);
 		if (ignoreCurrent && t == 0) continue;
 		if (t < minT) minT = t;
 	}
@@ -130,6 +167,18 @@ UD float2 sf_force(const AgentCtx& A, const SfConst& K, float2 np, float4 E, flo
 	const float viewHalf = (float)(100.0 * REF_PI / 180.0);
 	const float scale = angle_less_m(A.vel, vneg(R), K.vmag_vel, magR, viewHalf, -0.17364818f) ? 1.0f : 0.5f;
 	return vmul(F, scale);
+}
+
+// SocialForcesAvoidance::ComputeObstacleInteractionForce:
+// SocialForcesAvoidance.cpp:112-140 (U0 = p[3], R = p[4])
+UD float2 sf_obstacle_force(const AgentCtx& A, const CostDesc& c, float2 a, float2 b)
+{
+	const float2 diff = vsub(A.pos, nearest_on_segment(A.pos, a, b));
+	const float dist = vmag(diff);
+	if (dist < 0.001f) return V(0, 0);
+	const float U0 = c.p[3], R = c.p[4];
+	const float d_U = -U0 / R * ref_expf(A.ex, -dist / R);
+	return vmul(vneg(diff), d_U);
 }
 
 // PowerLaw::ComputeAgentInteractionForce: PowerLaw.cpp:28-66

@@ -189,6 +189,52 @@ UD float ttc_pair(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2
 	return fminr(t1, t2);
 }
 
+// nearestPointOnLine(pt, la, lb, onSegment = true): vector2D.h:274-296
+UD float2 nearest_on_segment(float2 pt, float2 la, float2 lb)
+{
+	if (la.x == lb.x && la.y == lb.y) return la;
+	const float2 line = vsub(la, lb);
+	float k = vdot(vsub(pt, lb), line) / vsq(line);
+	if (k > 1) k = 1;
+	else if (k < 0) k = 0;
+	return vadd(vmul(la, k), vmul(lb, 1 - k));
+}
+// distanceToLineSquared(pt, la, lb, true): vector2D.h:303-306
+UD float dist2_to_segment(float2 pt, float2 la, float2 lb) { return vsq(vsub(pt, nearest_on_segment(pt, la, lb))); }
+
+// ComputeTimeToCollision_LineSegmentInterior: costFunction.cpp:293-325.
+// sinf of the reference is the host C library's; here the double sine
+// rounded to float (equal wherever the library rounds correctly).
+UD float ttc_segment_interior(float2 p, float2 v, float r, float2 a, float2 b)
+{
+	if (dist2_to_segment(p, a, b) <= r * r) return 0;
+	float2 X;
+	if (!line_intersection(p, vadd(p, v), a, b, &X)) return MAXF;
+	if (vdot(v, vsub(X, p)) < 0) return MAXF;
+	// nearestPointOnLine(X, a, b, false, &onSegment): k in [0, 1]
+	const float2 line = vsub(a, b);
+	const float k = vdot(vsub(X, b), line) / vsq(line);
+	if (!(k >= 0 && k <= 1)) return MAXF;
+	const float speed = vmag(v);
+	const float t = vmag(vsub(X, p)) / speed;
+	const float ang = vangle_exact(v, vsub(b, a));
+	const float sub = r / (float)sin((double)ang);
+	const float tsub = sub / speed;
+	return fmaxr(0.0f, t - tsub);
+}
+
+// ComputeTimeToCollision_LineSegment: costFunction.cpp:270-291
+UD float ttc_segment(float2 p, float2 v, float r, float2 a, float2 b)
+{
+	const float t1 = ttc_pair(p, v, r, a, V(0, 0), 0);
+	if (t1 == 0) return 0;
+	if (a.x == b.x && a.y == b.y) return t1;
+	const float t2 = ttc_pair(p, v, r, b, V(0, 0), 0);
+	if (t2 == 0) return 0;
+	const float ti = ttc_segment_interior(p, v, r, a, b);
+	return fminr(fminr(t1, t2), ti);
+}
+
 // ttc_pair with P = p1 - p2 and c = |P|^2 - (r1 + r2)^2 given (the same
 // values ttc_pair computes; |P|^2 <= RR exactly when c <= 0)
 UD float ttc_pair_pre(float2 v1, float2 P, float c, float2 v2)

@@ -61,6 +61,9 @@ struct DevState {
 	float4* scratch;
 	int maxnb, total_warps, max_cells;   // max_cells: capacity of the cell arrays (all scenarios)
 	int t_begin, t_end;   // cell-sorted agents this k_agent launch updates
+	const float4* edges;  // obstacle edges of all scenarios (ScenDesc::edge_off)
+	uint32_t* obs_list;   // per warp: max_obs entries of the agent's obstacle list
+	int max_obs;
 	const int* scen_order;   // [nscen]: scenarios in cell-space order (grouped by kernel)
 	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks
 	float cells_per_range;
@@ -626,6 +629,42 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 	return K;
 }
 
+// Obstacle edges within range of the agent (worldBase.cpp:62-77), per
+// displacement group as the agents (worldToric.cpp:32-79): edges in file
+// order, each group's appended after the previous one.  Returns the count.
+__device__ int gather_obstacles(const DevState& S, const ScenDesc& sd, float2 p, float r, int lane, uint32_t* out)
+{
+	int K = 0;
+	const float r2 = r * r;
+	const unsigned lt = (1u << lane) - 1u;
+	for (int g = 0; g < 5; ++g) {
+		float2 disp = V(0, 0);
+		if (g > 0) {
+			if (sd.world != W_TORIC) break;
+			bool active;
+			if (g == 1) { active = (p.x - r) < -0.5f * sd.width; disp = V(sd.width, 0); }
+			else if (g == 2) { active = (p.x + r) > 0.5f * sd.width; disp = V(-sd.width, 0); }
+			else if (g == 3) { active = (p.y - r) < -0.5f * sd.height; disp = V(0, sd.height); }
+			else { active = (p.y + r) > 0.5f * sd.height; disp = V(0, -sd.height); }
+			if (!active) continue;
+		}
+		const float2 q = vadd(p, disp);
+		for (int b0 = 0; b0 < sd.nedges; b0 += 32) {
+			const int k = b0 + lane;
+			bool ok = false;
+			if (k < sd.nedges) {
+				const float4 E = S.edges[sd.edge_off + k];
+				ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, ok);
+			if (ok) out[K + __popc(m & lt)] = ((uint32_t)g << 28) | (uint32_t)(sd.edge_off + k);
+			K += __popc(m);
+		}
+	}
+	__syncwarp();
+	return K;
+}
+
 // ------------------------------------------------------------------------
 // warp helpers
 // ------------------------------------------------------------------------
@@ -680,7 +719,23 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 	const float ax = __shfl_sync(0xffffffffu, acc, 0);
 	const float ay = __shfl_sync(0xffffffffu, acc, 1);
 	__syncwarp();
-	return vadd(V(ax, ay), V(0, 0));
+	// obstacle edges within the cost's range, summed in list order; PowerLaw
+	// has no obstacle force (PowerLaw.cpp:68-72: a zero vector each)
+	float2 obs = V(0, 0);
+	if (c.kind == K_SOCIALFORCES) {
+		for (int b0 = 0; b0 < N.KO; b0 += 32) {
+			const int k = b0 + lane;
+			bool take = false;
+			float2 f = V(0, 0);
+			if (k < N.KO) {
+				float2 a, b;
+				nb_seg(N, k, &a, &b);
+				if (dist2_to_segment(A.pos, a, b) <= rs) { take = true; f = sf_obstacle_force(A, c, a, b); }
+			}
+			obs = ordered_accumulate(obs, f, take);
+		}
+	}
+	return vadd(V(ax, ay), obs);
 }
 
 // ForceBasedFunction::ComputeTargetVelocity: ForceBasedFunction.cpp:48-52
@@ -985,6 +1040,16 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 						if (t != 0 && t < T[j]) T[j] = t;
 					}
 				}
+				// obstacle edges within the cost's range
+				for (int k = lane; k < N.KO; k += 32) {
+					float2 a, b;
+					nb_seg(N, k, &a, &b);
+					if (dist2_to_segment(A.pos, a, b) > c.range * c.range) continue;
+					for (int j = 0; j < KS; ++j) {
+						const float t = ttc_segment(A.pos, sv[j], A.radius, a, b);
+						if (t != 0 && t < T[j]) T[j] = t;
+					}
+				}
 #pragma unroll
 				for (int j = 0; j < KS; ++j)
 					for (int o = 16; o > 0; o >>= 1) {
@@ -1100,6 +1165,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		NbView N;
 		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB; N.sE = S.sE;
 		N.W = sd.width; N.H = sd.height;
+		N.edges = S.edges; N.obs = nullptr; N.KO = 0;
 
 		if (dump) {
 			const int cap = S.dump_cap;
@@ -1117,6 +1183,11 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				S.tape_list[(size_t)slot * maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
 			}
 			if (lane == 0) S.tape_cnt[slot] = K;
+		}
+		if (sd.nedges > 0) {
+			uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
+			N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
+			N.obs = ol;
 		}
 
 		// phase 5: contact forces (policy.cpp:107-141), independent of phase 4
@@ -1136,6 +1207,20 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 						const float inter = rsum - vmag(diff);
 						if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
 					}
+				}
+				contact = ordered_accumulate(contact, f, take);
+			}
+			// colliding obstacle edges, after the agents (policy.cpp:126-137)
+			for (int b0 = 0; b0 < N.KO; b0 += 32) {
+				const int k = b0 + lane;
+				bool take = false;
+				float2 f = V(0, 0);
+				if (k < N.KO) {
+					float2 a, b;
+					nb_seg(N, k, &a, &b);
+					const float2 diff = vsub(A.pos, nearest_on_segment(A.pos, a, b));
+					const float inter = A.radius - vmag(diff);
+					if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
 				}
 				contact = ordered_accumulate(contact, f, take);
 			}
@@ -1170,6 +1255,14 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					for (int k = lane; k < K; k += 32) {
 						if (N.d2[k] > md2) continue;
 						const float tt = ttc_pair(A.pos, A.pref, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+						if (tt == 0) continue;
+						if (tt < m) m = tt;
+					}
+					for (int k = lane; k < N.KO; k += 32) {
+						float2 a, b;
+						nb_seg(N, k, &a, &b);
+						if (dist2_to_segment(A.pos, a, b) > md2) continue;
+						const float tt = ttc_segment(A.pos, A.pref, A.radius, a, b);
 						if (tt == 0) continue;
 						if (tt < m) m = tt;
 					}
@@ -1596,6 +1689,9 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		for (const auto& p : sc.policies) { pols_.push_back(p); pol_scen_.push_back((int)k); }
 		ScenDesc& D = scen_[k];
 		D.world = sc.world; D.width = sc.width; D.height = sc.height; D.dt = sc.dt;
+		D.edge_off = (int)edges_.size();
+		D.nedges = (int)sc.edges.size();
+		edges_.insert(edges_.end(), sc.edges.begin(), sc.edges.end());
 		float mr = 0;
 		for (const auto& p : sc.policies) mr = std::max(mr, p.range);
 		D.max_range = mr;
@@ -1658,12 +1754,17 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			const int j0 = (int)scen_order_.size();
 			for (size_t k = 0; k < scen_.size(); ++k)
 				if (cls[k] == c) scen_order_.push_back((int)k);
-			if ((int)scen_order_.size() > j0) groups_.push_back(KGroup{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0 });
+			if ((int)scen_order_.size() > j0) groups_.push_back(KGroup{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 });
 		}
 		if (!dalloc(scen_order_dev_, scen_order_.size(), err_)) return false;
 		CK(cudaMemcpy(scen_order_dev_, scen_order_.data(), sizeof(int) * scen_order_.size(), cudaMemcpyHostToDevice));
 		d_->scen_order = scen_order_dev_;
 	}
+	if (!edges_.empty()) {
+		if (!dalloc(edges_dev_, edges_.size(), err_)) return false;
+		CK(cudaMemcpy(edges_dev_, edges_.data(), sizeof(float4) * edges_.size(), cudaMemcpyHostToDevice));
+	}
+	d_->edges = edges_dev_;
 	if (!build_tables()) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;
@@ -1949,13 +2050,19 @@ bool Engine::configure()
 	mode_ = 1;
 	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
 	// one launch shape per kernel group, each with its own line scratch
-	size_t scr = 0;
+	size_t scr = 0, obs = 0;
+	int maxe = 0;
+	for (const auto& D : scen_) maxe = std::max(maxe, D.nedges);
+	S.max_obs = 5 * maxe;   // every edge, once per displacement group
 	for (auto& g : groups_) {
 		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode);
 		if (opt_.occupancy < 1.0f) g.blocks = std::max(num_sms_, (int)(g.blocks * opt_.occupancy));
 		g.scratch_off = scr;
 		scr += (size_t)g.blocks * wpb * 2 * maxnb_;
+		g.obs_off = obs;
+		obs += (size_t)g.blocks * wpb * S.max_obs;
 	}
+	if (!dalloc(S.obs_list, std::max<size_t>(obs, 1), err_)) return false;
 	agent_blocks_ = groups_.empty() ? num_sms_ : groups_[0].blocks;
 	S.total_warps = agent_blocks_ * wpb;
 	S.sched = opt_.schedule;
@@ -2002,6 +2109,7 @@ void Engine::enqueue_step()
 		A.t_begin = tb[k]; A.t_end = te[k];
 		A.total_warps = g.blocks * wpb;
 		A.scratch = S.scratch + g.scratch_off;
+		A.obs_list = S.obs_list + g.obs_off;
 		if (S.tape_list) {
 			if (g.mode == 1) k_agent<1, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
 			else k_agent<0, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
@@ -2518,6 +2626,7 @@ bool Engine::diff_begin(int steps, int every, const float* targets, float weight
 		err_ = "the differentiable form needs a fixed agent set (no delayed starts, no removal at the goal)";
 		return false;
 	}
+	if (!edges_.empty()) { err_ = "the differentiable form does not support static obstacles"; return false; }
 	for (size_t pi = 0; pi < pols_.size(); ++pi) {
 		const PolicyDesc& P = pols_[pi];
 		bool ok = P.method == M_GRADIENT;
@@ -2739,7 +2848,7 @@ Engine::~Engine()
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,
 		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.fill, S.blocksum, S.grid, S.bbox, S.status,
 		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io,
-		                 S.agent_scen, S.cell_base, scen_dev_,
+		                 S.agent_scen, S.cell_base, scen_dev_, S.obs_list,
 		                 snap_pos_, snap_vel_, snap_view_, snap_vwf_, snap_rng_ };
 		for (void* p : ptrs)
 			if (p) cudaFree(p);
@@ -2748,6 +2857,7 @@ Engine::~Engine()
 	for (cudaEvent_t e : { pa0_, pa1_, ps0_, ps1_ })
 		if (e) cudaEventDestroy(e);
 	if (scen_order_dev_) cudaFree(scen_order_dev_);
+	if (edges_dev_) cudaFree(edges_dev_);
 	if (ev0_) cudaEventDestroy(ev0_);
 	if (ev1_) cudaEventDestroy(ev1_);
 	if (stream_) cudaStreamDestroy(stream_);

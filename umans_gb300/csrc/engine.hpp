@@ -182,11 +182,13 @@ private:
 		int mode;          // k_agent specialisation
 		int j0, j1;        // positions in scen_order_
 		int blocks;
-		size_t scratch_off;
+		size_t scratch_off, obs_off;
 	};
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
 	int* scen_order_dev_ = nullptr;
+	std::vector<float4> edges_;      // obstacle edges of all scenarios
+	float4* edges_dev_ = nullptr;
 	AgentRecord* io_host_ = nullptr;   // page-locked staging for AgentData exchange
 	int* status_host_ = nullptr;       // page-locked copy of the device status word
 	size_t io_host_cap_ = 0;

@@ -79,6 +79,7 @@ struct ScenDesc {
 	float max_range;      // largest interaction range of its policies
 	int agent_off, n;     // its agents occupy list slots [agent_off, agent_off + n)
 	int max_cells;        // cap on its grid's cell count
+	int edge_off, nedges; // its obstacle edges in the concatenated edge array
 };
 
 // Grid parameters written by the device each step.

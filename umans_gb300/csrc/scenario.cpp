@@ -166,6 +166,24 @@ struct Loader {
 		return true;
 	}
 
+	bool obstacle(const XmlElement* oe)
+	{   // FromConfigFile_loadSingleObstacle: crowdSimulator.cpp:496-514, then
+		// WorldBase::AddObstacle (worldBase.cpp:239-242): the polygon's edges
+		std::vector<float2> pts;
+		for (const XmlElement* pe = oe->first_child("Point"); pe; pe = oe->next_sibling(pe, "Point")) {
+			float x = 0, y = 0;
+			pe->query_float("x", &x);
+			pe->query_float("y", &y);
+			pts.push_back(float2{ x, y });
+		}
+		const size_t n = pts.size();
+		for (size_t i = 0; i < n; ++i) {
+			const float2 a = pts[i], b = pts[(i + 1) % n];
+			s.edges.push_back(float4{ a.x, a.y, b.x, b.y });
+		}
+		return true;
+	}
+
 	bool agent(const XmlElement* ae)
 	{   // FromConfigFile_loadSingleAgent: crowdSimulator.cpp:424-494
 		int want = -1;
@@ -277,9 +295,11 @@ bool load_scenario(const std::string& path, Scenario& s, std::string& err)
 	if (const XmlElement* ab = sim->first_child("Agents")) {
 		if (!L.block(ab, folder, "Agents", "Agent", [&](const XmlElement* e) { return L.agent(e); }, ext2)) return false;
 	}
-	if (world->first_child("Obstacles")) {
-		err = "static obstacles are not supported by this engine";
-		return false;
+	// FromConfigFile: obstacles after the agents (crowdSimulator.cpp:633-645)
+	XmlDocument ext3;
+	if (const XmlElement* ob = world->first_child("Obstacles")) {
+		if (!L.block(ob, folder, "Obstacles", "Obstacle", [&](const XmlElement* e) { return L.obstacle(e); }, ext3))
+			return false;
 	}
 	return true;
 }

@@ -4,6 +4,8 @@
 #include <string>
 #include <vector>
 
+#include <vector_types.h>
+
 #include "model.hpp"
 
 namespace umans {
@@ -25,6 +27,9 @@ struct Scenario {
 	std::vector<PolicyDesc> policies;
 	std::vector<int> policy_ids;
 	std::vector<AgentInit> agents;   // in the order the reference adds them
+	// obstacle edges (a.x, a.y, b.x, b.y): every polygon's closed outline,
+	// polygons in file order (Polygon2D::Polygon2D, tools/Polygon2D.cpp:27-35)
+	std::vector<float4> edges;
 	int next_unused_id = 0;
 	std::vector<std::string> warnings;
 };

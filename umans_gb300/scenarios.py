@@ -82,14 +82,20 @@ class Scenario:
     pref_speed: np.ndarray = None   # (n,) float32
     max_speed: np.ndarray = None    # (n,) float32
     policy_id: np.ndarray = None    # (n,) int
+    obstacles: list = field(default_factory=list)   # polygons: (k, 2) vertex arrays
 
     @property
     def n(self) -> int:
         return int(self.pos.shape[0])
 
     def to_xml(self) -> str:
-        w = (f'<World type="Toric" width="{_f(self.width)}" height="{_f(self.height)}"/>'
-             if self.world == "Toric" else '<World type="Infinite"/>')
+        obs = ""
+        if self.obstacles:
+            obs = "<Obstacles>" + "".join(
+                "<Obstacle>" + "".join(f'<Point x="{_f(x)}" y="{_f(y)}"/>' for x, y in np.asarray(poly, np.float32))
+                + "</Obstacle>" for poly in self.obstacles) + "</Obstacles>"
+        w = (f'<World type="Toric" width="{_f(self.width)}" height="{_f(self.height)}">{obs}</World>'
+             if self.world == "Toric" else f'<World type="Infinite">{obs}</World>')
         end = f' end_time="{_f(self.end_time)}"' if self.end_time is not None else ""
         out = ['<?xml version="1.0" encoding="utf-8"?>',
                f'<Simulation delta_time="{_f(self.dt)}"{end}>', w,
@@ -290,6 +296,41 @@ def model_crossing(model: str, n: int = 40, seed: int = 11) -> Scenario:
     goal = np.concatenate([a + [20, 0], b + [0, 20]])
     return Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
                     **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+
+
+BLOCK = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], np.float32)
+
+
+def model_obstacle_crossing(model: str, n: int = 40, seed: int = 13) -> Scenario:
+    """The crossing layout with a 2 x 2 m block at the crossing point."""
+    sc = model_crossing(model, n, seed)
+    sc.obstacles = [BLOCK.copy()]
+    return sc
+
+
+def model_corridor_walls(model: str, n: int = 40, seed: int = 14) -> Scenario:
+    """Two groups walking in opposite directions along a 4 m wide corridor
+    between two wall polygons (agents start close to the walls)."""
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    a = np.stack([rng.uniform(-10, -4, h), rng.uniform(-1.6, 1.6, h)], 1)
+    b = np.stack([rng.uniform(4, 10, n - h), rng.uniform(-1.6, 1.6, n - h)], 1)
+    pos = np.concatenate([a, b])
+    goal = np.concatenate([a + [16, 0], b - [16, 0]])
+    top = np.array([[-16, 2], [16, 2], [16, 2.5], [-16, 2.5]], np.float32)
+    bottom = np.array([[-16, -2.5], [16, -2.5], [16, -2], [-16, -2]], np.float32)
+    sc = Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
+                  **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+    sc.obstacles = [top, bottom]
+    return sc
+
+
+def model_toric_obstacle(model: str, n: int = 60, side: float = 8.0, seed: int = 15) -> Scenario:
+    """The toric layout with a block next to the world's edge (displaced
+    obstacle queries)."""
+    sc = model_toric(model, n, side, seed)
+    sc.obstacles = [BLOCK * 0.5 + np.array([side / 2 - 0.75, 0.0], np.float32)]
+    return sc
 
 
 def model_toric(model: str, n: int = 60, side: float = 12.0, seed: int = 12) -> Scenario:
