@@ -56,3 +56,18 @@ def test_batch_of_golden_scenarios_matches_reference(golden_xml):
             if len(idx):
                 dev = float(np.abs(pos[off[k]:off[k + 1]] - g["pos"][idx[0]]).max()) if off[k + 1] > off[k] else 0.0
                 assert dev <= 1e-4, f"{name} step {s}: {dev}"
+
+
+def test_batch_with_obstacles_equals_individual_simulations(tmp_path):
+    """Scenarios with static obstacles (each its own edges) in one batch."""
+    scs = [S.model_obstacle_crossing("SocialForces"), S.model_corridor_walls("Karamouzas"),
+           S.model_toric_obstacle("ORCA"), S.model_crossing("PowerLaw")]
+    paths = [sc.write(str(tmp_path / f"o{k}.xml")) for k, sc in enumerate(scs)]
+    b = Batch(paths)
+    off = b.offsets
+    b.step(30)
+    pos = b.positions()
+    for k, p in enumerate(paths):
+        s = Simulation(p)
+        s.step(30)
+        assert np.array_equal(pos[off[k]:off[k + 1]], s.positions()), f"scenario {k}"

@@ -221,3 +221,10 @@ def test_unsupported_policies_are_rejected(tmp_path):
     s = Simulation(path)
     with pytest.raises(UmansError, match="gradient-method"):
         s.diff_begin(np.zeros((3, s.n, 2), np.float32))
+
+
+def test_obstacles_are_rejected(tmp_path):
+    path = S.model_obstacle_crossing("SocialForces", n=10).write(str(tmp_path / "obst.xml"))
+    s = Simulation(path)
+    with pytest.raises(UmansError, match="obstacles"):
+        s.diff_begin(np.zeros((3, s.n, 2), np.float32))
