@@ -35,7 +35,7 @@ LIB_PATH = os.path.join(PORT_DIR, "libumans_port.so")
 
 KINDS = ["ORCA", "RVO", "SocialForcesAvoidance", "PowerLaw", "GoalReachingForce",
          "Karamouzas", "Moussaid", "Paris", "VanToll", "TtcaDca", "FOEAvoidance",
-         "PLEdestrians"]
+         "PLEdestrians", "RandomFunction", "Generic"]
 # (attribute name, slot, default) per kind; defaults from the reference headers
 PARAMS = {
     "ORCA": [("timeHorizon", 0, 5.0)],                                   # ORCA.h:54
@@ -53,10 +53,12 @@ PARAMS = {
                 ("sigmaTtca", 2, 1.0), ("sigmaDca", 3, 0.3)],
     "FOEAvoidance": [],
     "PLEdestrians": [("w_a", 0, 2.23), ("w_b", 1, 1.26), ("t_min", 2, 0.5), ("t_max", 3, 3.0)],
+    "RandomFunction": [],
+    "Generic": [],
 }
 # the U0 attribute is read into V0 (SocialForcesAvoidance.cpp:148); U0 itself
 # keeps its default 10 in slot 3 and is only used by obstacle forces.
-DEFAULT_RANGE = {"GoalReachingForce": 0.0}
+DEFAULT_RANGE = {"GoalReachingForce": 0.0, "RandomFunction": 0.0}   # RandomFunction.h: range_ = 0
 
 
 class CostT(C.Structure):

@@ -916,6 +916,9 @@ static float cost_eval(const actx* A, const up_cost* c, cprep* P, v2 v)
 	case UP_PARIS: return cost_paris(A, c, v);
 	case UP_TTCADCA: return cost_ttcadca(A, c, v);
 	case UP_FOE: return cost_foe(A, c, v);
+	/* RandomFunction::GetCost: RandomFunction.cpp:25-28 (the agent's stream) */
+	case UP_RANDOM: return rng_uniform(&((up_world*)A->w)->rng[A->i], -1, 1);
+	case UP_GENERIC: return 0;   /* GenericCost::GetCost: GenericCost.cpp:27-31 */
 	}
 	return 0;
 }
@@ -1037,6 +1040,14 @@ static v2 cost_gradient(const actx* A, const up_cost* c, cprep* P, v2 v)
 		return vdiv(vsub(v, P->target), A->dt);
 	case UP_TTCADCA: return grad_ttcadca(A, c, v);
 	case UP_FOE: return grad_foe(A, c, v);
+	case UP_RANDOM: {
+		/* RandomFunction::GetGradient: RandomFunction.cpp:30-33; the reference
+		 * build evaluates the constructor's second argument first */
+		uint32_t* st = &((up_world*)A->w)->rng[A->i];
+		const float gy = rng_uniform(st, -1, 1);
+		const float gx = rng_uniform(st, -1, 1);
+		return V(gx, gy);
+	}
 	default: {
 		/* CostFunction::GetGradient default: costFunction.cpp:36-54 */
 		const float d = 0.1f;

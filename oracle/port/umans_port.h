@@ -20,7 +20,7 @@ extern "C" {
 enum up_cost_kind {
 	UP_ORCA = 0, UP_RVO, UP_SOCIALFORCES, UP_POWERLAW, UP_GOALREACHING,
 	UP_KARAMOUZAS, UP_MOUSSAID, UP_PARIS, UP_VANTOLL, UP_TTCADCA,
-	UP_FOE, UP_PLEDESTRIANS, UP_NUM_KINDS
+	UP_FOE, UP_PLEDESTRIANS, UP_RANDOM, UP_GENERIC, UP_NUM_KINDS
 };
 enum up_method { UP_GRADIENT = 0, UP_SAMPLING = 1, UP_GLOBAL = 2 };
 enum up_world_type { UP_INFINITE = 0, UP_TORIC = 1 };

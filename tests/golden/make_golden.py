@@ -77,6 +77,8 @@ def main():
         run(f"obstacle_crossing40_{m}", S.model_obstacle_crossing(m), 100, every=5)
         run(f"corridor_walls40_{m}", S.model_corridor_walls(m), 100, every=5)
         run(f"toric_obstacle60_{m}", S.model_toric_obstacle(m), 100, every=5)
+    for name in S.REGISTRY_POLICIES:
+        run(f"registry40_{name}", S.registry_crossing(name), 100, every=5)
     run("orca_circle50", S.circle_orca(50), 100, every=5, nb_steps=(1, 50))
     run("socialforces_toric1500", S.socialforces_toric(n=1500, density=0.625), 100, every=10,
         nb_steps=(1, 100), nb_agents=150)

@@ -928,6 +928,7 @@ __device__ float eval_cost(const AgentCtx& A, const NbView& N, const CostDesc& c
 	case K_PARIS: return cost_paris(A, N, c, v);
 	case K_TTCADCA: return cost_ttcadca(A, N, c, v);
 	case K_FOE: return cost_foe(A, N, c, v);
+	case K_GENERIC: return 0;   // GenericCost::GetCost: GenericCost.cpp:27-31
 	}
 	return 0;
 }
@@ -1079,10 +1080,11 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 	}
 	for (int i = lane; i < pol.nsamples; i += 32) {
 		float2 v;
+		const int d0 = i * pol.draws;   // draws before this sample
 		if (pol.table_random) {
 			const float ma = pol.max_angle;
-			const uint32_t x1 = mulmod(S.lcgpow[2 * i + 1], rng0);
-			const uint32_t x2 = mulmod(S.lcgpow[2 * i + 2], rng0);
+			const uint32_t x1 = mulmod(S.lcgpow[d0 + 1], rng0);
+			const uint32_t x2 = mulmod(S.lcgpow[d0 + 2], rng0);
 			const float ra = rng_uniform(x1, -ma, ma);
 			const float rl = rng_uniform(x2, 0, radius);
 			v = vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
@@ -1091,9 +1093,15 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			v = vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
 		}
 		float tc = 0;
+		int jr = d0 + (pol.table_random ? 2 : 0);
 		for (int ci = 0; ci < ncost; ++ci) {
 			const float coeff = pol.single_cost ? 1.0f : pol.cost[ci].coeff;
-			tc += coeff * eval_cost(A, N, pol.cost[ci], P, ci, v);
+			float cv;
+			if (pol.cost[ci].kind == K_RANDOM)   // RandomFunction::GetCost: RandomFunction.cpp:25-28
+				cv = rng_uniform(mulmod(S.lcgpow[++jr], rng0), -1, 1);
+			else
+				cv = eval_cost(A, N, pol.cost[ci], P, ci, v);
+			tc += coeff * cv;
 		}
 		if (tc < bestC) { bestC = tc; bestI = i; }
 	}
@@ -1107,8 +1115,8 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 	const int i = bestI;
 	if (pol.table_random) {
 		const float ma = pol.max_angle;
-		const uint32_t x1 = mulmod(S.lcgpow[2 * i + 1], rng0);
-		const uint32_t x2 = mulmod(S.lcgpow[2 * i + 2], rng0);
+		const uint32_t x1 = mulmod(S.lcgpow[i * pol.draws + 1], rng0);
+		const uint32_t x2 = mulmod(S.lcgpow[i * pol.draws + 2], rng0);
 		const float ra = rng_uniform(x1, -ma, ma);
 		const float rl = rng_uniform(x2, 0, radius);
 		return vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
@@ -1281,10 +1289,21 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 			if (pol.method == M_GRADIENT) {
 				// Policy::getAccelerationFromGradient: policy.cpp:78-89
 				float2 T = V(0, 0);
+				int grad_draws = 0;
 				for (int ci = 0; ci < pol.ncost; ++ci) {
 					const CostDesc& c = pol.cost[ci];
 					float2 g;
 					if (MODE == 1 || is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
+					else if (c.kind == K_RANDOM) {
+						// RandomFunction::GetGradient (RandomFunction.cpp:30-33): two
+						// numbers in [-1, 1]; the reference build evaluates the
+						// constructor's second argument first
+						const uint32_t r0 = S.rng[slot];
+						const float gy = rng_uniform(mulmod(S.lcgpow[grad_draws + 1], r0), -1, 1);
+						const float gx = rng_uniform(mulmod(S.lcgpow[grad_draws + 2], r0), -1, 1);
+						grad_draws += 2;
+						g = V(gx, gy);
+					} else if (c.kind == K_GENERIC) g = V(0, 0);   // FD of a zero cost
 					else if (c.kind == K_TTCADCA) g = grad_ttcadca(A, N, c, A.vel);
 					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel);
 					else {
@@ -1306,6 +1325,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				}
 				acc = vmul(T, -1);
 				if (TAPE && lane == 0) S.tape_acc[slot] = acc;
+				if (grad_draws > 0) {
+					rng_used = true;
+					rng_next = mulmod(S.lcgpow[grad_draws], S.rng[slot]);
+				}
 			} else if (MODE == 0) {
 				float2 best;
 				const CostDesc& c0 = pol.cost[0];
@@ -1314,9 +1337,9 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				else {
 					const uint32_t r0 = S.rng[slot];
 					best = sample_min(S, A, N, pol, P, r0, lane, lines, reinterpret_cast<float*>(proj));
-					if (pol.table_random) {
+					if (pol.draws > 0) {
 						rng_used = true;
-						rng_next = mulmod(S.lcgpow[2 * pol.nsamples], r0);
+						rng_next = mulmod(S.lcgpow[pol.nsamples * pol.draws], r0);
 					}
 				}
 				acc = vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt));
@@ -1776,10 +1799,14 @@ bool Engine::build_tables()
 {
 	std::vector<PolicyDesc> pols = pols_;
 	std::vector<SampleEntry> table;
-	int maxrandom = 0;
+	size_t maxdraws = 0;   // random numbers an agent draws in one step, over all policies
 	for (auto& p : pols) {
 		p.use_sampling = 0; p.table_random = 0; p.single_cost = 0;
 		p.table_offset = 0; p.nsamples = 0; p.len_divisor = 1;
+		p.nrand = 0; p.draws = 0;
+		for (int c = 0; c < p.ncost; ++c) p.nrand += p.cost[c].kind == K_RANDOM;
+		// RandomFunction::GetGradient draws two numbers per cost (RandomFunction.cpp:30-33)
+		if (p.method == M_GRADIENT) maxdraws = std::max(maxdraws, (size_t)(2 * p.nrand));
 		bool sampling = p.method == M_SAMPLING;
 		int type = p.s_type, base = p.s_base, dir = p.s_dir, rad = p.s_radius, ns = p.speed_samples, na = p.angle_samples,
 		    incl = p.include_base;
@@ -1795,13 +1822,17 @@ bool Engine::build_tables()
 			}
 		}
 		if (!sampling) continue;
+		if (p.single_cost) p.nrand = p.cost[0].kind == K_RANDOM ? 1 : 0;
 		p.use_sampling = 1;
 		p.table_base = base; p.table_dir = dir; p.table_radius = rad;
 		p.max_angle = (float)(angle / 360.0 * 3.1415926535897);
 		if (type == 1) {
+			// random sampling (costFunction.cpp:99-119): angle, then length, then
+			// one number per RandomFunction cost, sample after sample
 			p.table_random = 1;
 			p.nsamples = std::max(p.random_samples, 0);
-			maxrandom = std::max(maxrandom, p.nsamples);
+			p.draws = 2 + p.nrand;
+			maxdraws = std::max(maxdraws, (size_t)p.nsamples * p.draws);
 			continue;
 		}
 		// regular schedule: costFunction.cpp:122-158 (float angle accumulation)
@@ -1822,9 +1853,11 @@ bool Engine::build_tables()
 			}
 		}
 		p.nsamples = (int)table.size() - p.table_offset;
+		p.draws = p.nrand;
+		maxdraws = std::max(maxdraws, (size_t)p.nsamples * p.draws);
 	}
 	if (table.empty()) table.push_back(SampleEntry{ 0, 0, 0, 0 });
-	std::vector<uint32_t> pw(2 * (size_t)maxrandom + 3);
+	std::vector<uint32_t> pw(maxdraws + 3);
 	pw[0] = 1;
 	for (size_t k = 1; k < pw.size(); ++k) pw[k] = (uint32_t)(((uint64_t)pw[k - 1] * LCG_A) % LCG_M);
 	PolicyDesc* dp = nullptr;

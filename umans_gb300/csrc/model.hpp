@@ -13,7 +13,7 @@ namespace umans {
 
 enum CostKind : int {
 	K_ORCA = 0, K_RVO, K_SOCIALFORCES, K_POWERLAW, K_GOALREACHING, K_KARAMOUZAS,
-	K_MOUSSAID, K_PARIS, K_VANTOLL, K_TTCADCA, K_FOE, K_PLEDESTRIANS, K_NUM_KINDS
+	K_MOUSSAID, K_PARIS, K_VANTOLL, K_TTCADCA, K_FOE, K_PLEDESTRIANS, K_RANDOM, K_GENERIC, K_NUM_KINDS
 };
 enum Method : int { M_GRADIENT = 0, M_SAMPLING = 1, M_GLOBAL = 2 };
 enum WorldType : int { W_INFINITE = 0, W_TORIC = 1 };
@@ -64,6 +64,8 @@ struct PolicyDesc {
 	int table_base;      // base rule of the table actually used
 	int table_random;    // 1 when random sampling is used
 	int single_cost;     // GLOBAL with one non-closed-form cost: sample only cost[0] with coeff 1
+	int nrand;           // RandomFunction costs among the ones evaluated per sample / gradient
+	int draws;           // random numbers drawn per sample (random sampling: 2, + nrand)
 };
 
 // Same layout as the C ABI's struct AgentData (28 bytes).

@@ -13,7 +13,7 @@ static const double REF_PI = 3.1415926535897;   // vector2D.h:27
 
 static const char* KIND_NAMES[K_NUM_KINDS] = {
 	"ORCA", "RVO", "SocialForcesAvoidance", "PowerLaw", "GoalReachingForce", "Karamouzas",
-	"Moussaid", "Paris", "VanToll", "TtcaDca", "FOEAvoidance", "PLEdestrians"};
+	"Moussaid", "Paris", "VanToll", "TtcaDca", "FOEAvoidance", "PLEdestrians", "RandomFunction", "Generic"};
 
 const char* cost_kind_name(int kind) { return (kind >= 0 && kind < K_NUM_KINDS) ? KIND_NAMES[kind] : "?"; }
 
@@ -21,7 +21,6 @@ int cost_kind_from_name(const std::string& name)
 {
 	for (int k = 0; k < K_NUM_KINDS; ++k)
 		if (name == KIND_NAMES[k]) return k;
-	if (name == "RandomFunction" || name == "Generic") return -2;
 	return -1;
 }
 
@@ -44,6 +43,7 @@ void cost_defaults(int kind, CostDesc& c)
 	case K_VANTOLL: c.p[0] = 8; break;
 	case K_TTCADCA: c.p[0] = 2; c.p[1] = 2; c.p[2] = 1; c.p[3] = 0.3f; break;
 	case K_PLEDESTRIANS: c.p[0] = 2.23f; c.p[1] = 1.26f; c.p[2] = 0.5f; c.p[3] = 3; break;
+	case K_RANDOM: c.range = 0; break;                                 // RandomFunction.h: range_ = 0
 	default: break;
 	}
 }

@@ -298,6 +298,40 @@ def model_crossing(model: str, n: int = 40, seed: int = 11) -> Scenario:
                     **_agents(n, pos, goal, pref=1.3, maxs=1.6))
 
 
+# Policies with the RandomFunction and Generic cost functions (the per-agent
+# random stream consumed by sampling and by the costs themselves)
+REGISTRY_POLICIES = {
+    "RandomGradient": '<Policy id="0" OptimizationMethod="gradient" RelaxationTime="0.5">'
+                      '<costfunction range="5" name="SocialForcesAvoidance"/>'
+                      '<costfunction name="RandomFunction" coeff="0.5"/>'
+                      '<costfunction name="GoalReachingForce"/></Policy>',
+    "RandomSampling": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+                      'SamplingBaseDirection="unit" SamplingAngle="360" SpeedSamples="4" AngleSamples="36" '
+                      'SamplingRadius="maximum speed" RelaxationTime="0.5">'
+                      '<costfunction range="5" name="PowerLaw"/><costfunction name="RandomFunction" coeff="0.2"/>'
+                      '<costfunction name="GoalReachingForce"/></Policy>',
+    "RandomRVO": '<Policy id="0" OptimizationMethod="sampling" SamplingType="random" SamplingBase="current velocity" '
+                 'SamplingBaseDirection="unit" SamplingAngle="360" RandomSamples="100" '
+                 'SamplingRadius="maximum acceleration" RelaxationTime="0">'
+                 '<costfunction range="5" name="RVO"/><costfunction name="RandomFunction" coeff="0.1"/></Policy>',
+    "RandomGlobal": '<Policy id="0" OptimizationMethod="global" RelaxationTime="0.5">'
+                    '<costfunction name="RandomFunction"/></Policy>',
+    "GenericGlobal": '<Policy id="0" OptimizationMethod="global" RelaxationTime="0.5">'
+                     '<costfunction name="Generic"/></Policy>',
+    "GenericSampling": '<Policy id="0" OptimizationMethod="sampling" SamplingType="regular" SamplingBase="zero" '
+                       'SamplingBaseDirection="preferred velocity" SamplingAngle="180" SpeedSamples="5" '
+                       'AngleSamples="19" SamplingRadius="preferred speed" RelaxationTime="0.5">'
+                       '<costfunction range="5" name="Moussaid"/><costfunction name="Generic"/></Policy>',
+}
+
+
+def registry_crossing(name: str, n: int = 40, seed: int = 16) -> Scenario:
+    """The crossing layout with one of the RandomFunction / Generic policies."""
+    sc = model_crossing("ORCA", n, seed)
+    sc.policies = [REGISTRY_POLICIES[name]]
+    return sc
+
+
 BLOCK = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], np.float32)
 
 
