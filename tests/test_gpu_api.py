@@ -41,9 +41,14 @@ def test_reference_api_roundtrip(tmp_path):
 def test_bad_scenarios_fail_loudly(tmp_path):
     p = tmp_path / "bad.xml"
     p.write_text('<Simulation delta_time="0.1"><World type="Infinite"/><Policies>'
-                 '<Policy id="0" OptimizationMethod="gradient"><costfunction name="RandomFunction"/>'
-                 '</Policy></Policies></Simulation>')
+                 '<Policy id="0" OptimizationMethod="global"><costfunction name="ORCA"/>'
+                 '<costfunction name="ORCA"/></Policy></Policies></Simulation>')
     with pytest.raises(UmansError, match="not supported"):
+        Simulation(str(p))
+    p.write_text('<Simulation delta_time="0.1"><World type="Infinite"/><Policies>'
+                 '<Policy id="0" OptimizationMethod="gradient"><costfunction name="NoSuchCost"/>'
+                 '</Policy></Policies></Simulation>')
+    with pytest.raises(UmansError, match="cost function"):
         Simulation(str(p))
     p.write_text('<Simulation delta_time="-1"><World type="Infinite"/></Simulation>')
     with pytest.raises(UmansError, match="delta_time"):
