@@ -167,6 +167,21 @@ int umans_diff_end(umans_sim* sim);
  * are left unchanged.  get: NaN where the scenario has no such cost. */
 int umans_set_force_params(umans_sim* sim, int scenario, const float* params4);
 int umans_get_force_params(umans_sim* sim, int scenario, float* params4);
+/* Trajectory output, the reference's CSVWriter (src/Engine/tools/csvwriter.cpp,
+ * fed after every step by CrowdSimulator::RunSimulationSteps,
+ * crowdSimulator.cpp:77-95).  After every step the positions go to a device
+ * ring of ring_steps steps; a full ring is copied to page-locked host memory
+ * and written by a background thread while the GPU keeps stepping.  binary = 0:
+ * the reference's layout, one file output_<id>.csv per agent with "t,x,y"
+ * lines appended, at full float precision (9 significant digits; the
+ * reference writes 6); binary = 1: one file trajectory.bin of chunks (see
+ * umans_gb300.read_trajectory).  Changes of the agent list flush the ring
+ * first.  Single simulations only.  umans_record_flush writes everything
+ * recorded so far and waits; umans_record_stop flushes and ends recording
+ * (also done by umans_destroy). */
+int umans_record_start(umans_sim* sim, const char* directory, int ring_steps, int binary);
+int umans_record_flush(umans_sim* sim);
+int umans_record_stop(umans_sim* sim);
 /* Test hook: the device's exponential used by the force models, which
  * returns exactly the host C library's expf for x in [-87, 0]; evaluates n
  * values and reports the size of the exception table.  Errors are reported

@@ -186,6 +186,19 @@ class Simulation:
         self._check(self._lib.umans_neighbours(self._h, int(cap), _p(ids), _p(d2), _p(cnt)))
         return ids, d2, cnt
 
+    # --- trajectory output ------------------------------------------------
+    def record_start(self, directory: str, ring_steps: int = 64, binary: bool = False):
+        """Write every step's positions to `directory`: output_<id>.csv per
+        agent (the reference's CSVWriter layout, full float precision), or
+        trajectory.bin with `binary` (read it with read_trajectory)."""
+        self._check(self._lib.umans_record_start(self._h, os.fsencode(directory), int(ring_steps), int(bool(binary))))
+
+    def record_flush(self):
+        self._check(self._lib.umans_record_flush(self._h))
+
+    def record_stop(self):
+        self._check(self._lib.umans_record_stop(self._h))
+
     @property
     def num_scenarios(self) -> int:
         ns = C.c_int()
@@ -232,6 +245,29 @@ class Simulation:
 
     def diff_end(self):
         self._check(self._lib.umans_diff_end(self._h))
+
+
+def read_trajectory(path: str):
+    """Chunks of a trajectory.bin written by Simulation.record_start(binary=True):
+    a list of (ids[n], times[steps], xy[steps, n, 2])."""
+    import struct
+    out = []
+    with open(path, "rb") as fh:
+        data = fh.read()
+    off = 0
+    while off < len(data):
+        if data[off:off + 4] != b"UMTR":
+            raise ValueError("not a trajectory chunk at byte %d" % off)
+        n, steps = struct.unpack_from("<ii", data, off + 4)
+        off += 12
+        ids = np.frombuffer(data, np.int32, n, off).copy()
+        off += 4 * n
+        times = np.frombuffer(data, np.float64, steps, off).copy()
+        off += 8 * steps
+        xy = np.frombuffer(data, np.float32, steps * n * 2, off).reshape(steps, n, 2).copy()
+        off += 4 * steps * n * 2
+        out.append((ids, times, xy))
+    return out
 
 
 class Batch(Simulation):

@@ -315,6 +315,28 @@ int umans_get_force_params(umans_sim* s, int scenario, float* params4)
 	return UMANS_OK;
 }
 
+int umans_record_start(umans_sim* s, const char* directory, int ring_steps, int binary)
+{
+	if (!s || !directory) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->record_start(directory, ring_steps, binary ? umans::TrajWriter::BINARY : umans::TrajWriter::CSV))
+		return fail(s, UMANS_ERR_ARGUMENT, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_record_flush(umans_sim* s)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->record_flush()) return fail(s, UMANS_ERR_DEVICE, s->eng->error());
+	return UMANS_OK;
+}
+
+int umans_record_stop(umans_sim* s)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->record_stop()) return fail(s, UMANS_ERR_DEVICE, s->eng->error());
+	return UMANS_OK;
+}
+
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 {
 	if ((n > 0 && (!x || !y)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");

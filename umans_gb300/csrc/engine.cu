@@ -2210,6 +2210,7 @@ bool Engine::remove_at_goal()
 		const float dx = goal_[i].x - pos_[i].x, dy = goal_[i].y - pos_[i].y;
 		const float r = prm_[i].x;
 		if (dx * dx + dy * dy <= r * r) {
+			if (!changed && !rec_flush_async()) return false;   // the ring's agents are the old list
 			const int last = n_ - 1;
 			slot_of_.erase(id_[i]);
 			if (i != last) {
@@ -2229,10 +2230,17 @@ bool Engine::remove_at_goal()
 }
 
 // Enqueues n steps (no host work in between).
-bool Engine::run_steps(int nsteps)
+bool Engine::run_steps(int nsteps, bool record)
 {
 	if (configured_maxnb_ != maxnb_ && !configure()) return false;
 	steps_pending_ = true;
+	record = record && rec_ != nullptr;
+	if (record && n_ > rec_cap_n_) {
+		// the population grew since the ring was sized (it was flushed then)
+		CK(cudaStreamSynchronize(stream_));
+		rec_cap_n_ = n_;
+		if (!dalloc(rec_ring_, (size_t)rec_R_ * rec_cap_n_, err_)) return false;
+	}
 	for (int s = 0; s < nsteps; ++s) {
 		if (opt_.use_graph && !profile_) {
 			if (!graph_valid_ && !capture_graph()) return false;
@@ -2254,8 +2262,111 @@ bool Engine::run_steps(int nsteps)
 		}
 		time_ += sc_.dt;
 		for (size_t k = 0; k < times_.size(); ++k) times_[k] += scen_[k].dt;
+		if (record && n_ > 0) {
+			// RunSimulationSteps hands the writer every agent's position after
+			// each step with the world's time (crowdSimulator.cpp:81-93)
+			if (rec_head_ == 0) rec_ids_ = id_;
+			CK(cudaMemcpyAsync(rec_ring_ + (size_t)rec_head_ * n_, d_->pos, sizeof(float2) * n_,
+			                   cudaMemcpyDeviceToDevice, stream_));
+			rec_times_.push_back(time_);
+			++rec_head_;
+		}
 	}
 	return true;
+}
+
+// ------------------------------------------------------------------------
+// trajectory output
+// ------------------------------------------------------------------------
+bool Engine::record_start(const std::string& dir, int ring_steps, int format)
+{
+	if (!sync()) return false;
+	if (rec_ && !record_stop()) return false;
+	if (ring_steps < 1) { err_ = "ring_steps must be positive"; return false; }
+	if (scen_.size() > 1) { err_ = "trajectory output is for single simulations"; return false; }
+	rec_ = new TrajWriter(dir, format);
+	const std::string e = rec_->error();
+	if (!e.empty()) { err_ = e; rec_free(); return false; }
+	rec_R_ = ring_steps;
+	rec_cap_n_ = std::max(n_, 1);
+	if (!dalloc(rec_ring_, (size_t)rec_R_ * rec_cap_n_, err_)) { rec_free(); return false; }
+	for (int b = 0; b < 2; ++b) {
+		rec_busy_[b].store(0);
+		if (!rec_ev_[b]) CK(cudaEventCreateWithFlags(&rec_ev_[b], cudaEventDisableTiming));
+	}
+	rec_head_ = rec_snap_head_ = 0;
+	rec_times_.clear();
+	return true;
+}
+
+bool Engine::rec_flush_async()
+{
+	if (!rec_ || rec_head_ == 0) return true;
+	const int b = rec_next_;
+	if (rec_busy_[b].load()) rec_->drain();
+	const size_t floats = (size_t)rec_head_ * n_ * 2;
+	if (rec_host_cap_[b] < floats) {
+		if (rec_host_[b]) cudaFreeHost(rec_host_[b]);
+		rec_host_[b] = nullptr;
+		rec_host_cap_[b] = 0;
+		CK(cudaMallocHost(&rec_host_[b], sizeof(float) * floats));
+		rec_host_cap_[b] = floats;
+	}
+	CK(cudaMemcpyAsync(rec_host_[b], rec_ring_, sizeof(float) * floats, cudaMemcpyDeviceToHost, stream_));
+	CK(cudaEventRecord(rec_ev_[b], stream_));
+	rec_busy_[b].store(1);
+	rec_->push(n_, rec_head_, rec_ids_, rec_times_, rec_host_[b], rec_ev_[b], &rec_busy_[b]);
+	rec_head_ = rec_snap_head_ = 0;
+	rec_times_.clear();
+	rec_next_ ^= 1;
+	// a grown population needs a larger ring before the next step is recorded
+	if (n_ > rec_cap_n_) {
+		CK(cudaStreamSynchronize(stream_));
+		rec_cap_n_ = n_;
+		if (!dalloc(rec_ring_, (size_t)rec_R_ * rec_cap_n_, err_)) return false;
+	}
+	return true;
+}
+
+bool Engine::rec_before_change()
+{
+	if (!rec_ || rec_head_ == 0) return true;
+	if (!sync()) return false;
+	return rec_flush_async();
+}
+
+bool Engine::record_flush()
+{
+	if (!rec_) return true;
+	if (!sync()) return false;
+	if (!rec_flush_async()) return false;
+	rec_->drain();
+	const std::string e = rec_->error();
+	if (!e.empty()) { err_ = e; return false; }
+	return true;
+}
+
+bool Engine::record_stop()
+{
+	if (!rec_) return true;
+	const bool ok = record_flush();
+	rec_free();
+	return ok;
+}
+
+void Engine::rec_free()
+{
+	delete rec_;   // drains and joins the writer
+	rec_ = nullptr;
+	if (rec_ring_) cudaFree(rec_ring_);
+	rec_ring_ = nullptr;
+	for (int b = 0; b < 2; ++b) {
+		if (rec_host_[b]) cudaFreeHost(rec_host_[b]);
+		rec_host_[b] = nullptr;
+		rec_host_cap_[b] = 0;
+	}
+	rec_head_ = rec_snap_head_ = 0;
+	rec_times_.clear();
 }
 
 // The mutable per-agent state at the start of a batch of steps, kept so that
@@ -2287,6 +2398,7 @@ bool Engine::take_snapshot()
 		CK(cudaGetLastError());
 	}
 	snap_valid_ = true;
+	rec_snap_head_ = rec_head_;
 	snap_time_ = time_;
 	snap_times_ = times_;
 	snap_steps_ = 0;
@@ -2305,6 +2417,8 @@ bool Engine::restore_snapshot()
 	}
 	time_ = snap_time_;
 	times_ = snap_times_;
+	rec_head_ = rec_snap_head_;
+	rec_times_.resize(rec_head_);
 	return true;
 }
 
@@ -2314,16 +2428,29 @@ bool Engine::step(int nsteps)
 	const bool dynamic = !pending_.empty() || any_remove_at_goal_;
 	if (time_kernels) CK(cudaEventRecord(ev0_, stream_));
 	if (!dynamic) {
-		if (!snap_valid_ && !take_snapshot()) return false;
-		if (!run_steps(nsteps)) return false;
-		snap_steps_ += nsteps;
+		// with trajectory output, batches stop where the ring is full; the
+		// ring is handed over once its steps are committed
+		int left = nsteps;
+		while (left > 0) {
+			int k = left;
+			if (rec_) {
+				if (rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
+				k = std::min(left, rec_R_ - rec_head_);
+			}
+			if (!snap_valid_ && !take_snapshot()) return false;
+			if (!run_steps(k, true)) return false;
+			snap_steps_ += k;
+			left -= k;
+		}
 	} else {
 		// insertions and removals change the agent list between steps: settle
 		// every step before the host-side changes
 		for (int s = 0; s < nsteps; ++s) {
+			if (rec_ && rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
+			if (!pending_.empty() && (double)pending_.front().start_time <= time_ && !rec_before_change()) return false;
 			if (!pending_.empty() && !apply_pending_agents()) return false;
 			if (!take_snapshot()) return false;
-			if (!run_steps(1)) return false;
+			if (!run_steps(1, true)) return false;
 			snap_steps_ = 1;
 			if (!sync()) return false;
 			if (any_remove_at_goal_ && !remove_at_goal()) return false;
@@ -2362,7 +2489,7 @@ bool Engine::sync()
 			if (!restore_snapshot()) return false;
 			maxnb_ = std::min(3072, maxnb_ * 2);
 			invalidate_graph();
-			if (!run_steps(steps)) return false;
+			if (!run_steps(steps, true)) return false;
 			continue;
 		}
 		snap_valid_ = false;
@@ -2446,6 +2573,7 @@ bool Engine::add_agent(float x, float y, float radius, float pref, float maxs, f
 {
 	// AddAgent (APIFunctions.cpp:139-171) -> WorldBase::AddAgent (worldBase.cpp:161-186)
 	if (scen_.size() > 1) { err_ = "agents cannot be added to a batch"; return false; }
+	if (!rec_before_change()) return false;
 	int pidx = -1;
 	for (size_t k = 0; k < sc_.policy_ids.size(); ++k)
 		if (sc_.policy_ids[k] == policy_id) pidx = (int)k;
@@ -2473,6 +2601,7 @@ bool Engine::remove_agent(int id)
 {
 	// WorldBase::RemoveAgent (worldBase.cpp:198-235): the last agent moves into the gap
 	if (scen_.size() > 1) { err_ = "agents cannot be removed from a batch"; return false; }
+	if (!rec_before_change()) return false;
 	auto it = slot_of_.find(id);
 	if (it == slot_of_.end()) { err_ = "no agent with id " + std::to_string(id); return false; }
 	if (!download_mutable()) return false;
@@ -2873,6 +3002,9 @@ Engine::~Engine()
 {
 	if (stream_) cudaStreamSynchronize(stream_);
 	invalidate_graph();
+	record_stop();
+	for (cudaEvent_t e : rec_ev_)
+		if (e) cudaEventDestroy(e);
 	diff_free();
 	if (io_host_) cudaFreeHost(io_host_);
 	if (status_host_) cudaFreeHost(status_host_);

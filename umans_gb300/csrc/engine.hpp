@@ -2,6 +2,7 @@
 // (src/Engine/core/worldBase.cpp:79-128) behind the reference's simulation
 // interface (CrowdSimulator / WorldBase / Agent, src/Engine/core/).
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -10,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "model.hpp"
+#include "recorder.hpp"
 #include "scenario.hpp"
 
 namespace umans {
@@ -112,6 +114,14 @@ public:
 	// entries are left unchanged.  get: NaN where the scenario has no such cost.
 	bool set_force_params(int scen, const float* p4);
 	bool get_force_params(int scen, float* p4);
+
+	// ---- trajectory output -------------------------------------------
+	// Positions of every step are kept in a device ring of `ring_steps`
+	// steps and written (TrajWriter formats) when the ring is full, on
+	// flush and on stop; population changes flush first.
+	bool record_start(const std::string& dir, int ring_steps, int format);
+	bool record_flush();   // everything recorded so far written to disk
+	bool record_stop();
 	int diff_kernels_forward_per_step() const { return kernels_per_step() + 1; }
 
 private:
@@ -122,7 +132,7 @@ private:
 	bool build_tables();
 	bool choose_maxnb();
 	bool configure();
-	bool run_steps(int n);
+	bool run_steps(int n, bool record = false);
 	bool take_snapshot();
 	bool restore_snapshot();
 	void enqueue_step();
@@ -217,6 +227,20 @@ private:
 	bool diff_alloc_tape();
 	bool diff_check_status();
 	void diff_free();
+
+	// trajectory output state
+	TrajWriter* rec_ = nullptr;
+	int rec_R_ = 0, rec_head_ = 0, rec_snap_head_ = 0, rec_cap_n_ = 0, rec_next_ = 0;
+	float2* rec_ring_ = nullptr;
+	std::vector<double> rec_times_;
+	std::vector<int> rec_ids_;
+	float* rec_host_[2] = { nullptr, nullptr };
+	size_t rec_host_cap_[2] = { 0, 0 };
+	std::atomic<int> rec_busy_[2];
+	cudaEvent_t rec_ev_[2] = { nullptr, nullptr };
+	bool rec_flush_async();         // after a committed sync: hand the ring to the writer
+	bool rec_before_change();       // sync and flush before the agent list changes
+	void rec_free();
 };
 
 }  // namespace umans
