@@ -187,6 +187,12 @@ int umans_record_stop(umans_sim* sim);
  * values and reports the size of the exception table.  Errors are reported
  * through umans_last_error(NULL). */
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions);
+/* Test hook: the device's sinf/cosf, which return exactly the host C
+ * library's sinf/cosf for |x| <= 64 (the float sin/cos of
+ * costFunction.cpp:33, :104, :321 and FOEAvoidance.cpp:142); evaluates n
+ * values and reports the size of the exception tables.  Errors:
+ * umans_last_error(NULL). */
+int umans_debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions);
 /* Test hook: the device's (float)((double)a*b - (double)c*d) on n quadruples
  * abcd[4*i .. 4*i+3] (the promoted products of SocialForcesAvoidance.cpp:86
  * and vector2D.h:166-170).  Errors: umans_last_error(NULL). */

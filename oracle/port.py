@@ -298,6 +298,7 @@ def _load():
         lib.up_set_state.argtypes = [P, P, P, P]
         lib.up_neighbors.argtypes = [P, C.c_int, P, P, P, P, C.c_int]
         lib.up_libm_expf.argtypes = [P, P, C.c_long]
+        lib.up_libm_sincosf.argtypes = [P, P, P, C.c_long]
         lib.up_set_obstacles.argtypes = [P, C.c_int, P]
         _lib = lib
     return _lib
@@ -313,6 +314,14 @@ def libm_expf(x: np.ndarray) -> np.ndarray:
     y = np.empty_like(x)
     _load().up_libm_expf(_p(x), _p(y), x.size)
     return y
+
+
+def libm_sincosf(x: np.ndarray):
+    """The host C library's sinf and cosf, elementwise (float32)."""
+    x = np.ascontiguousarray(x, np.float32)
+    s, c = np.empty_like(x), np.empty_like(x)
+    _load().up_libm_sincosf(_p(x), _p(s), _p(c), x.size)
+    return s, c
 
 
 class PortSim:

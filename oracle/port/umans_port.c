@@ -1327,6 +1327,11 @@ void up_libm_expf(const float* x, float* y, long n)
 	for (long i = 0; i < n; ++i) y[i] = expf(x[i]);
 }
 
+void up_libm_sincosf(const float* x, float* s, float* c, long n)
+{
+	for (long i = 0; i < n; ++i) { s[i] = sinf(x[i]); c[i] = cosf(x[i]); }
+}
+
 int up_neighbors(const up_world* w, int i, long long* ids, float* dist2, float* px, float* py, int cap)
 {
 	const nbrlist* L = &w->nb[i];

@@ -84,6 +84,8 @@ int up_neighbors(const up_world* w, int i, long long* ids, float* dist2,
                  float* px, float* py, int cap);
 
 void up_libm_expf(const float* x, float* y, long n);
+/* the host C library's sinf / cosf (test reference of the device's) */
+void up_libm_sincosf(const float* x, float* s, float* c, long n);
 
 #ifdef __cplusplus
 }

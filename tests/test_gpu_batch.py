@@ -41,11 +41,11 @@ def test_autotune_keeps_results(tmp_path):
 
 
 def test_batch_of_golden_scenarios_matches_reference(golden_xml):
-    names = [n for n in golden_names() if not n.endswith("_Dutra")]
+    names = golden_names()
     items = [golden_xml(n) for n in names]
     b = Batch([p for p, _ in items])
     off = b.offsets
-    snaps = sorted({int(s) for _, g in items for s in g["steps"] if s <= 60})
+    snaps = sorted({int(s) for _, g in items for s in g["steps"] if s <= 100})
     done = 0
     for s in snaps:
         b.step(s - done)
@@ -55,7 +55,7 @@ def test_batch_of_golden_scenarios_matches_reference(golden_xml):
             idx = np.nonzero(g["steps"] == s)[0]
             if len(idx):
                 dev = float(np.abs(pos[off[k]:off[k + 1]] - g["pos"][idx[0]]).max()) if off[k + 1] > off[k] else 0.0
-                assert dev <= 1e-4, f"{name} step {s}: {dev}"
+                assert dev == 0.0, f"{name} step {s}: {dev}"
 
 
 def test_batch_with_obstacles_equals_individual_simulations(tmp_path):

@@ -22,12 +22,10 @@ TOL = 1e-4   # m over the first 100 steps (spec bound)
 THREADS = os.cpu_count() or 4
 
 
-# TtcaDca (the Dutra policy) rotates its gradient with the host sinf/cosf
-# (TtcaDca.cpp:255-260 via costFunction.cpp:30-34) of an unbounded angle; the
-# device does not reproduce the host library's sinf/cosf bit for bit, and the
-# dense crowds amplify the last-bit differences.  Its bound is asserted over
-# the first 10 steps and the 100-step deviation is printed.
-BOUNDED_STEPS = {"Dutra": 10}
+# every fixture is asserted over its first 100 steps (the host sinf/cosf of
+# the TtcaDca and FOEAvoidance gradient rotations, the random-sample rotations
+# and the segment collision times are reproduced exactly on the device)
+BOUNDED_STEPS = {}
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -50,6 +48,7 @@ def test_trajectory_matches_reference(name, golden_xml):
     print(f"{name}: max deviation over the first {min(done, horizon)} steps = {worst:.3g} m; "
           f"over {min(done, 100)} steps = {worst_all:.3g} m")
     assert worst <= TOL, f"{name}: max deviation {worst} m"
+    assert worst_all == 0.0, f"{name}: not bit-identical ({worst_all} m)"
 
 
 @pytest.mark.parametrize("name", [n for n in golden_names() if n.startswith(("toric60", "orca_circle50",

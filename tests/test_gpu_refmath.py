@@ -1,11 +1,12 @@
 """The device exponential of the force models equals the host C library's
-expf bit for bit on [-87, 0] (float-float evaluation + exception table)."""
+expf bit for bit on [-87, 0], and the device sine and cosine equal the host
+sinf/cosf on [-64, 64] (float-float evaluation + exception tables)."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
-from oracle.port import libm_expf
+from oracle.port import libm_expf, libm_sincosf
 from umans_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
@@ -89,3 +90,50 @@ def test_prod_diff_matches_double_then_float():
         want = host_prod_diff(a, b, c, d)
         bad = np.flatnonzero(got.view(np.uint32) != want.view(np.uint32))
         assert bad.size == 0, (k, bad[:5], a[bad[:5]], b[bad[:5]], c[bad[:5]], d[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def device_sincosf(x):
+    lib = _lib.load()
+    x = np.ascontiguousarray(x, np.float32)
+    s, c = np.empty_like(x), np.empty_like(x)
+    cnt = C.c_size_t()
+    P = C.c_void_p
+    rc = lib.umans_debug_ref_sincosf(x.ctypes.data_as(P), s.ctypes.data_as(P), c.ctypes.data_as(P), x.size,
+                                     C.byref(cnt))
+    assert rc == 0, lib.umans_last_error(None)
+    return s, c, cnt.value
+
+
+def _check_sincos(x):
+    s, c, nexc = device_sincosf(x)
+    rs, rc = libm_sincosf(x)
+    for name, got, want in (("sin", s, rs), ("cos", c, rc)):
+        bad = np.nonzero(got.view(np.uint32) != want.view(np.uint32))[0]
+        assert bad.size == 0, f"{name}: {bad.size} mismatches, e.g. x={x[bad[:5]]} got {got[bad[:5]]} want {want[bad[:5]]}"
+    return nexc
+
+
+def test_ref_sincosf_random_sample_angles():
+    # the random-sample rotation angles: uniform in [-pi, pi]
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-np.pi, np.pi, 16_000_000).astype(np.float32)
+    assert _check_sincos(x) > 0
+
+
+def test_ref_sincosf_dense_ranges_and_magnitudes():
+    for start in (0.1, 0.7853, 1.0, 1.5707, 3.1415, 40.0, -2.5):
+        bits = np.float32(start).view(np.uint32) + np.arange(4_000_000, dtype=np.uint32)
+        _check_sincos(bits.view(np.float32))
+    rng = np.random.default_rng(6)
+    mag = np.exp2(rng.uniform(-20, 6, 8_000_000)).astype(np.float32)
+    x = np.where(rng.random(mag.size) < 0.5, -mag, mag).astype(np.float32)
+    _check_sincos(x[np.abs(x) <= 64])
+
+
+def test_ref_sincosf_edges():
+    k = np.arange(-40, 41, dtype=np.float64)
+    near = (k * np.pi / 2).astype(np.float32)               # floats nearest multiples of pi/2
+    near = np.concatenate([near, np.nextafter(near, np.float32(np.inf)), np.nextafter(near, np.float32(-np.inf))])
+    x = np.concatenate([near, np.float32([0.0, -0.0, 1e-45, -1e-45, 1e-30, 2.0 ** -12, -(2.0 ** -12), 64.0, -64.0,
+                                          np.nextafter(np.float32(2.0 ** -12), np.float32(0))])]).astype(np.float32)
+    _check_sincos(x[np.abs(x) <= 64])

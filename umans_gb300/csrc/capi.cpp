@@ -345,6 +345,14 @@ int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 	return UMANS_OK;
 }
 
+int umans_debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions)
+{
+	if ((n > 0 && (!x || !s || !c)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	std::string err;
+	if (!umans::debug_ref_sincosf(x, s, c, n, exceptions, err)) return fail(nullptr, UMANS_ERR_CUDA, err);
+	return UMANS_OK;
+}
+
 int umans_debug_prod_diff(const float* abcd, float* y, int n)
 {
 	if ((n > 0 && (!abcd || !y)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");

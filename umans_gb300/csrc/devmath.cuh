@@ -19,9 +19,18 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "refmath.hpp"
+
 namespace umans {
 
 #define UD __device__ __forceinline__
+
+// The host C library's sinf/cosf (refmath.hpp): exception tables of the
+// device, set once per device by the engine before the first step that needs
+// them.
+static __constant__ SinCosExceptions c_sincos;
+UD void host_sincosf(float x, float* s, float* c) { ref_sincosf(c_sincos, x, s, c); }
+UD float host_sinf(float x) { return ref_sinf(c_sincos, x); }
 
 constexpr float MAXF = FLT_MAX;
 constexpr double REF_PI = 3.1415926535897;   // vector2D.h:27
@@ -202,9 +211,8 @@ UD float2 nearest_on_segment(float2 pt, float2 la, float2 lb)
 // distanceToLineSquared(pt, la, lb, true): vector2D.h:303-306
 UD float dist2_to_segment(float2 pt, float2 la, float2 lb) { return vsq(vsub(pt, nearest_on_segment(pt, la, lb))); }
 
-// ComputeTimeToCollision_LineSegmentInterior: costFunction.cpp:293-325.
-// sinf of the reference is the host C library's; here the double sine
-// rounded to float (equal wherever the library rounds correctly).
+// ComputeTimeToCollision_LineSegmentInterior: costFunction.cpp:293-325
+// (sinf: the host C library's, host_sinf).
 UD float ttc_segment_interior(float2 p, float2 v, float r, float2 a, float2 b)
 {
 	if (dist2_to_segment(p, a, b) <= r * r) return 0;
@@ -218,7 +226,7 @@ UD float ttc_segment_interior(float2 p, float2 v, float r, float2 a, float2 b)
 	const float speed = vmag(v);
 	const float t = vmag(vsub(X, p)) / speed;
 	const float ang = vangle_exact(v, vsub(b, a));
-	const float sub = r / (float)sin((double)ang);
+	const float sub = r / host_sinf(ang);
 	const float tsub = sub / speed;
 	return fmaxr(0.0f, t - tsub);
 }
@@ -267,7 +275,9 @@ UD void ttca_dca(float2 p1, float2 v1, float r1, float2 p2, float2 v2, float r2,
 // RotateGradientToEuclideanCoordinates: costFunction.cpp:30-34
 UD float2 rotate_gradient(float gth, float gs, float2 dir, float speed)
 {
-	const float2 w = vadd(vmul(V(sinf(gth), 1 - cosf(gth)), speed), V(0, gs));
+	float sn, cs;
+	host_sincosf(gth, &sn, &cs);
+	const float2 w = vadd(vmul(V(sn, 1 - cs), speed), V(0, gs));
 	return V(dir.y * w.x + dir.x * w.y, -dir.x * w.x + dir.y * w.y);
 }
 

@@ -26,6 +26,8 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
 
 #include "costs.cuh"
 #include "orca.cuh"
@@ -898,7 +900,9 @@ __device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c
 	}
 	if (gt < -0.1f) gt = -0.1f;
 	else if (gt > 0.1f) gt = 0.1f;
-	const float2 w = vadd(vmul(V(sinf(gt), 1 - cosf(gt)), vmag(v)), V(0, gv));
+	float sn, cs;
+	host_sincosf(gt, &sn, &cs);
+	const float2 w = vadd(vmul(V(sn, 1 - cs), vmag(v)), V(0, gv));
 	return V(-Vn.y * w.x + -Vn.x * w.y, -(-Vn.x) * w.x + -Vn.y * w.y);
 }
 
@@ -1087,7 +1091,9 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			const uint32_t x2 = mulmod(S.lcgpow[d0 + 2], rng0);
 			const float ra = rng_uniform(x1, -ma, ma);
 			const float rl = rng_uniform(x2, 0, radius);
-			v = vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
+			float sn, cs;
+			host_sincosf(ra, &sn, &cs);
+			v = vadd(base, vmul(vrot_cs(dir, cs, sn), rl));
 		} else {
 			const SampleEntry e = S.table[pol.table_offset + i];
 			v = vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
@@ -1119,7 +1125,9 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 		const uint32_t x2 = mulmod(S.lcgpow[i * pol.draws + 2], rng0);
 		const float ra = rng_uniform(x1, -ma, ma);
 		const float rl = rng_uniform(x2, 0, radius);
-		return vadd(base, vmul(vrot_cs(dir, cosf(ra), sinf(ra)), rl));
+		float sn, cs;
+		host_sincosf(ra, &sn, &cs);
+		return vadd(base, vmul(vrot_cs(dir, cs, sn), rl));
 	}
 	const SampleEntry e = S.table[pol.table_offset + i];
 	return vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
@@ -1375,6 +1383,54 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		__syncwarp();
 	}
 	if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
+}
+
+// Sets this module's sinf/cosf exception tables on the current device (once).
+bool set_device_sincos(std::string& err)
+{
+	static std::mutex mu;
+	static std::set<int> done;
+	std::lock_guard<std::mutex> lk(mu);
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) { err = "cudaGetDevice failed"; return false; }
+	if (done.count(dev)) return true;
+	SinCosExceptions T;
+	if (!sincos_exceptions_for_device(&T, nullptr, err)) return false;
+	const cudaError_t e = cudaMemcpyToSymbol(c_sincos, &T, sizeof(T));
+	if (e != cudaSuccess) { err = std::string("sincos table: ") + cudaGetErrorString(e); return false; }
+	done.insert(dev);
+	return true;
+}
+
+__global__ void k_ref_sincosf(const float* x, float* s, float* c, int n)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) host_sincosf(x[i], &s[i], &c[i]);
+}
+
+// Evaluates the device's reference-exact sinf/cosf on n host values (tests).
+bool debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions, std::string& err)
+{
+	if (!set_device_sincos(err)) return false;
+	if (exceptions) {
+		SinCosExceptions T;
+		if (!sincos_exceptions_for_device(&T, exceptions, err)) return false;
+	}
+	float *dx = nullptr, *ds = nullptr, *dc = nullptr;
+	const size_t b = sizeof(float) * std::max(n, 1);
+	if (cudaMalloc(&dx, b) != cudaSuccess || cudaMalloc(&ds, b) != cudaSuccess || cudaMalloc(&dc, b) != cudaSuccess) {
+		err = "cudaMalloc";
+		return false;
+	}
+	cudaMemcpy(dx, x, sizeof(float) * n, cudaMemcpyHostToDevice);
+	if (n > 0) k_ref_sincosf<<<(n + 255) / 256, 256>>>(dx, ds, dc, n);
+	cudaError_t e = cudaMemcpy(s, ds, sizeof(float) * n, cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) e = cudaMemcpy(c, dc, sizeof(float) * n, cudaMemcpyDeviceToHost);
+	cudaFree(dx);
+	cudaFree(ds);
+	cudaFree(dc);
+	if (e != cudaSuccess) { err = cudaGetErrorString(e); return false; }
+	return true;
 }
 
 __global__ void k_ref_expf(ExpExceptions T, const float* x, float* y, int n)
@@ -1789,6 +1845,14 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	}
 	d_->edges = edges_dev_;
 	if (!build_tables()) return false;
+	// the host sinf/cosf: random-sample rotations, the gradient rotations of
+	// TtcaDca and FOEAvoidance, the segment collision times
+	bool need_trig = !edges_.empty();
+	for (const auto& p : pols_) {
+		need_trig |= p.table_random != 0;
+		for (int c = 0; c < p.ncost; ++c) need_trig |= p.cost[c].kind == K_TTCADCA || p.cost[c].kind == K_FOE;
+	}
+	if (need_trig && !set_device_sincos(err_)) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;
 	if (!choose_maxnb()) return false;

@@ -20,6 +20,8 @@ struct DevState;   // device pointers (engine.cu)
 
 // device evaluation of the reference-exact expf (refmath.hpp), for tests
 bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err);
+bool debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions, std::string& err);
+bool set_device_sincos(std::string& err);
 // device evaluation of (float)((double)a*b - (double)c*d) (devmath.cuh), for tests
 bool debug_prod_diff(const float* abcd, float* y, int n, std::string& err);
 

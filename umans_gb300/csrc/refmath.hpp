@@ -310,4 +310,296 @@ __device__ __forceinline__ float ref_expf(const ExpExceptions& T, float x)
 // host side (refmath.cpp): table shared by all simulations on a device
 bool exp_exceptions_for_device(ExpExceptions* out, size_t* count, std::string& err);
 
+// ---------------------------------------------------------------------------
+// Reference-exact float sine and cosine.
+//
+// The reference takes sin/cos of float arguments, which resolve to the host C
+// library's sinf/cosf: the gradient rotation (costFunction.cpp:30-34,
+// FOEAvoidance.cpp:142), the random-sample rotation (costFunction.cpp:104 via
+// rotateCounterClockwise, vector2D.h:166-170) and the segment collision time
+// (costFunction.cpp:321).  The host sinf/cosf round ~1-3% of the arguments
+// above 2^-5 the other way from the correctly rounded value (always within
+// 0.061 ulp of a rounding midpoint), which the crowd dynamics amplify.  Same
+// scheme as the exponential:
+//  * ff_sincos_core: Cody-Waite reduction x = k pi/2 + r with pi/2 in four
+//    floats (k * P1 exact for |k| < 2^12, |x| <= SC_LIMIT), then
+//    r = j/64 + d, |d| <= 1/128, and
+//      sin r = sin(j/64) cos d + cos(j/64) sin d,
+//      cos r = cos(j/64) cos d - sin(j/64) sin d
+//    with sin, cos(j/64) as float pairs (gen_sincos_table.py, 2^-48) and
+//    cos d = 1 - d^2/2 + d^4/24, sin d = d - d^3/6 + d^5/120, all in
+//    float-float (~2^-40 relative before the final rounding; only IEEE float
+//    +,-,* and exact products, so host and device agree bit for bit);
+//  * the host enumerates every float of |x| <= SC_LIMIT, records the
+//    arguments where the C library differs, and the smallest distance of
+//    such an argument's value from the rounding point (the "near" bound);
+//  * the device looks the argument up only when its value lies that close
+//    to a rounding midpoint (~1/8 of the calls), and returns the host
+//    library's bits.
+// Beyond SC_LIMIT the value is (float)sin((double)x), (float)cos((double)x).
+constexpr float SC_LIMIT = 64.0f;
+constexpr float SC_TINY = 0x1p-12f;     // below: sin x = x, cos x = 1 (correctly rounded)
+constexpr float SC_P1 = 0x1.9220000000000p+0f;
+constexpr float SC_P2 = -0x1.2aeef40000000p-18f;
+constexpr float SC_P3 = -0x1.73dcb40000000p-43f;
+constexpr float SC_P4 = 0x1.3198a20000000p-69f;
+constexpr float SC_TWO_OVER_PI = 0x1.45f3060000000p-1f;
+
+// { sin hi, sin lo, cos hi, cos lo } of j/64, j = 0..52
+#if defined(__CUDACC__)
+static __device__ const float SC_TAB_D[53][4] = {
+	{ 0.0f, 0.0f, 0x1.0000000000000p+0f, 0.0f },
+	{ 0x1.fffaaa0000000p-7f, 0x1.5dddda0000000p-32f, 0x1.fff0000000000p-1f, 0x1.5554a00000000p-29f },
+	{ 0x1.ffeaaa0000000p-6f, 0x1.dddd0e0000000p-31f, 0x1.ffc0020000000p-1f, -0x1.555b060000000p-26f },
+	{ 0x1.7fdc020000000p-5f, -0x1.f9a08a0000000p-30f, 0x1.ff70060000000p-1f, 0x1.7fbf340000000p-26f },
+	{ 0x1.ffaaae0000000p-5f, 0x1.dda9dc0000000p-30f, 0x1.ff00160000000p-1f, -0x1.56c1660000000p-26f },
+	{ 0x1.3facb20000000p-4f, -0x1.a5d1540000000p-29f, 0x1.fe70340000000p-1f, 0x1.29ef6e0000000p-29f },
+	{ 0x1.7f70100000000p-4f, 0x1.92a8720000000p-31f, 0x1.fdc06c0000000p-1f, -0x1.0328ca0000000p-30f },
+	{ 0x1.bf1b780000000p-4f, 0x1.5a0e480000000p-30f, 0x1.fcf0c80000000p-1f, 0x1.d336240000000p-34f },
+	{ 0x1.feaaee0000000p-4f, 0x1.d0ddc60000000p-29f, 0x1.fc01560000000p-1f, -0x1.b054860000000p-26f },
+	{ 0x1.1f0d3e0000000p-3f, -0x1.0a062a0000000p-28f, 0x1.faf2220000000p-1f, 0x1.8f12f40000000p-27f },
+	{ 0x1.3eb3120000000p-3f, 0x1.8bacda0000000p-28f, 0x1.f9c3400000000p-1f, 0x1.4f98860000000p-26f },
+	{ 0x1.5e44fc0000000p-3f, 0x1.f424de0000000p-28f, 0x1.f874c20000000p-1f, 0x1.c3dd9e0000000p-26f },
+	{ 0x1.7dc1020000000p-3f, 0x1.f75e560000000p-28f, 0x1.f706be0000000p-1f, -0x1.84c7920000000p-31f },
+	{ 0x1.9d252e0000000p-3f, -0x1.e6279e0000000p-28f, 0x1.f579480000000p-1f, 0x1.9fecf20000000p-26f },
+	{ 0x1.bc6f840000000p-3f, 0x1.db8c340000000p-28f, 0x1.f3cc7c0000000p-1f, 0x1.d9e8b60000000p-28f },
+	{ 0x1.db9e160000000p-3f, -0x1.2968c20000000p-33f, 0x1.f200740000000p-1f, -0x1.ef336c0000000p-26f },
+	{ 0x1.faaeee0000000p-3f, -0x1.619d520000000p-28f, 0x1.f0154a0000000p-1f, -0x1.0422be0000000p-30f },
+	{ 0x1.0cd00c0000000p-2f, 0x1.de6c860000000p-27f, 0x1.ee0b200000000p-1f, -0x1.0fc3ba0000000p-27f },
+	{ 0x1.1c37d60000000p-2f, 0x1.31ae1e0000000p-28f, 0x1.ebe2140000000p-1f, 0x1.eeddf40000000p-26f },
+	{ 0x1.2b8ddc0000000p-2f, 0x1.0fad280000000p-28f, 0x1.e99a4c0000000p-1f, 0x1.d3e6c20000000p-28f },
+	{ 0x1.3ad12a0000000p-2f, -0x1.12c5840000000p-27f, 0x1.e733ea0000000p-1f, 0x1.93d3fa0000000p-33f },
+	{ 0x1.4a00ca0000000p-2f, -0x1.3c30b80000000p-28f, 0x1.e4af140000000p-1f, 0x1.6548940000000p-26f },
+	{ 0x1.591bca0000000p-2f, -0x1.7429a40000000p-32f, 0x1.e20bf40000000p-1f, 0x1.359ad80000000p-26f },
+	{ 0x1.6821380000000p-2f, 0x1.471afe0000000p-27f, 0x1.df4ab40000000p-1f, -0x1.4278a20000000p-29f },
+	{ 0x1.7710260000000p-2f, -0x1.5137be0000000p-27f, 0x1.dc6b7e0000000p-1f, 0x1.732b220000000p-26f },
+	{ 0x1.85e7a20000000p-2f, -0x1.afb2d60000000p-27f, 0x1.d96e820000000p-1f, 0x1.ee353c0000000p-26f },
+	{ 0x1.94a6be0000000p-2f, 0x1.3ea8d80000000p-27f, 0x1.d653f00000000p-1f, 0x1.cf90100000000p-27f },
+	{ 0x1.a34c920000000p-2f, -0x1.9d799c0000000p-29f, 0x1.d31bf80000000p-1f, 0x1.b1af800000000p-26f },
+	{ 0x1.b1d8300000000p-2f, 0x1.4c85860000000p-28f, 0x1.cfc6d00000000p-1f, -0x1.6b54980000000p-27f },
+	{ 0x1.c048b20000000p-2f, -0x1.09d7ec0000000p-27f, 0x1.cc54aa0000000p-1f, 0x1.594b980000000p-28f },
+	{ 0x1.ce9d2e0000000p-2f, 0x1.ea52900000000p-29f, 0x1.c8c5c00000000p-1f, -0x1.cc795e0000000p-27f },
+	{ 0x1.dcd4c20000000p-2f, -0x1.59ac6c0000000p-27f, 0x1.c51a480000000p-1f, 0x1.7162ec0000000p-26f },
+	{ 0x1.eaee880000000p-2f, -0x1.769f420000000p-27f, 0x1.c152800000000p-1f, 0x1.96df540000000p-27f },
+	{ 0x1.f8e99e0000000p-2f, 0x1.daaf260000000p-28f, 0x1.bd6ea40000000p-1f, -0x1.dfad620000000p-26f },
+	{ 0x1.0362940000000p-1f, -0x1.8e59aa0000000p-27f, 0x1.b96eee0000000p-1f, 0x1.eb10820000000p-26f },
+	{ 0x1.0a40220000000p-1f, -0x1.61f0000000000p-29f, 0x1.b553a40000000p-1f, 0x1.0c104e0000000p-29f },
+	{ 0x1.110d0c0000000p-1f, 0x1.2da70e0000000p-27f, 0x1.b11d040000000p-1f, 0x1.62a4c60000000p-29f },
+	{ 0x1.17c8e60000000p-1f, -0x1.a224a00000000p-30f, 0x1.accb520000000p-1f, 0x1.bda77a0000000p-27f },
+	{ 0x1.1e73440000000p-1f, -0x1.b935160000000p-26f, 0x1.a85ed40000000p-1f, 0x1.b9f0160000000p-28f },
+	{ 0x1.250bba0000000p-1f, -0x1.90ee880000000p-26f, 0x1.a3d7d00000000p-1f, 0x1.a95ee80000000p-28f },
+	{ 0x1.2b91de0000000p-1f, 0x1.5108440000000p-26f, 0x1.9f368e0000000p-1f, 0x1.b225f00000000p-26f },
+	{ 0x1.32054c0000000p-1f, -0x1.d6e8760000000p-26f, 0x1.9a7b5a0000000p-1f, 0x1.b5328a0000000p-28f },
+	{ 0x1.3865980000000p-1f, -0x1.753afa0000000p-26f, 0x1.95a67e0000000p-1f, 0x1.963f980000000p-34f },
+	{ 0x1.3eb25e0000000p-1f, -0x1.9265580000000p-26f, 0x1.90b8480000000p-1f, -0x1.ec89420000000p-27f },
+	{ 0x1.44eb380000000p-1f, 0x1.cf386a0000000p-29f, 0x1.8bb1060000000p-1f, -0x1.688dc00000000p-27f },
+	{ 0x1.4b0fc40000000p-1f, 0x1.aaadd80000000p-27f, 0x1.8691080000000p-1f, 0x1.aef4d80000000p-26f },
+	{ 0x1.511fa00000000p-1f, -0x1.4265720000000p-28f, 0x1.8158a40000000p-1f, -0x1.cdd2540000000p-26f },
+	{ 0x1.571a6a0000000p-1f, -0x1.3254ca0000000p-26f, 0x1.7c08280000000p-1f, -0x1.ec35620000000p-30f },
+	{ 0x1.5cffc20000000p-1f, -0x1.280e1e0000000p-26f, 0x1.769fec0000000p-1f, 0x1.9548480000000p-27f },
+	{ 0x1.62cf4a0000000p-1f, -0x1.b794e20000000p-27f, 0x1.7120460000000p-1f, 0x1.f4eed00000000p-26f },
+	{ 0x1.6888a40000000p-1f, 0x1.c269660000000p-26f, 0x1.6b89900000000p-1f, -0x1.5841280000000p-27f },
+	{ 0x1.6e2b780000000p-1f, -0x1.dfa1100000000p-28f, 0x1.65dc200000000p-1f, -0x1.0a39a40000000p-28f },
+	{ 0x1.73b7680000000p-1f, 0x1.bd4af00000000p-30f, 0x1.6018520000000p-1f, 0x1.bd58f80000000p-27f },
+};
+#endif
+static const float SC_TAB_H[53][4] = {
+	{ 0.0f, 0.0f, 0x1.0000000000000p+0f, 0.0f },
+	{ 0x1.fffaaa0000000p-7f, 0x1.5dddda0000000p-32f, 0x1.fff0000000000p-1f, 0x1.5554a00000000p-29f },
+	{ 0x1.ffeaaa0000000p-6f, 0x1.dddd0e0000000p-31f, 0x1.ffc0020000000p-1f, -0x1.555b060000000p-26f },
+	{ 0x1.7fdc020000000p-5f, -0x1.f9a08a0000000p-30f, 0x1.ff70060000000p-1f, 0x1.7fbf340000000p-26f },
+	{ 0x1.ffaaae0000000p-5f, 0x1.dda9dc0000000p-30f, 0x1.ff00160000000p-1f, -0x1.56c1660000000p-26f },
+	{ 0x1.3facb20000000p-4f, -0x1.a5d1540000000p-29f, 0x1.fe70340000000p-1f, 0x1.29ef6e0000000p-29f },
+	{ 0x1.7f70100000000p-4f, 0x1.92a8720000000p-31f, 0x1.fdc06c0000000p-1f, -0x1.0328ca0000000p-30f },
+	{ 0x1.bf1b780000000p-4f, 0x1.5a0e480000000p-30f, 0x1.fcf0c80000000p-1f, 0x1.d336240000000p-34f },
+	{ 0x1.feaaee0000000p-4f, 0x1.d0ddc60000000p-29f, 0x1.fc01560000000p-1f, -0x1.b054860000000p-26f },
+	{ 0x1.1f0d3e0000000p-3f, -0x1.0a062a0000000p-28f, 0x1.faf2220000000p-1f, 0x1.8f12f40000000p-27f },
+	{ 0x1.3eb3120000000p-3f, 0x1.8bacda0000000p-28f, 0x1.f9c3400000000p-1f, 0x1.4f98860000000p-26f },
+	{ 0x1.5e44fc0000000p-3f, 0x1.f424de0000000p-28f, 0x1.f874c20000000p-1f, 0x1.c3dd9e0000000p-26f },
+	{ 0x1.7dc1020000000p-3f, 0x1.f75e560000000p-28f, 0x1.f706be0000000p-1f, -0x1.84c7920000000p-31f },
+	{ 0x1.9d252e0000000p-3f, -0x1.e6279e0000000p-28f, 0x1.f579480000000p-1f, 0x1.9fecf20000000p-26f },
+	{ 0x1.bc6f840000000p-3f, 0x1.db8c340000000p-28f, 0x1.f3cc7c0000000p-1f, 0x1.d9e8b60000000p-28f },
+	{ 0x1.db9e160000000p-3f, -0x1.2968c20000000p-33f, 0x1.f200740000000p-1f, -0x1.ef336c0000000p-26f },
+	{ 0x1.faaeee0000000p-3f, -0x1.619d520000000p-28f, 0x1.f0154a0000000p-1f, -0x1.0422be0000000p-30f },
+	{ 0x1.0cd00c0000000p-2f, 0x1.de6c860000000p-27f, 0x1.ee0b200000000p-1f, -0x1.0fc3ba0000000p-27f },
+	{ 0x1.1c37d60000000p-2f, 0x1.31ae1e0000000p-28f, 0x1.ebe2140000000p-1f, 0x1.eeddf40000000p-26f },
+	{ 0x1.2b8ddc0000000p-2f, 0x1.0fad280000000p-28f, 0x1.e99a4c0000000p-1f, 0x1.d3e6c20000000p-28f },
+	{ 0x1.3ad12a0000000p-2f, -0x1.12c5840000000p-27f, 0x1.e733ea0000000p-1f, 0x1.93d3fa0000000p-33f },
+	{ 0x1.4a00ca0000000p-2f, -0x1.3c30b80000000p-28f, 0x1.e4af140000000p-1f, 0x1.6548940000000p-26f },
+	{ 0x1.591bca0000000p-2f, -0x1.7429a40000000p-32f, 0x1.e20bf40000000p-1f, 0x1.359ad80000000p-26f },
+	{ 0x1.6821380000000p-2f, 0x1.471afe0000000p-27f, 0x1.df4ab40000000p-1f, -0x1.4278a20000000p-29f },
+	{ 0x1.7710260000000p-2f, -0x1.5137be0000000p-27f, 0x1.dc6b7e0000000p-1f, 0x1.732b220000000p-26f },
+	{ 0x1.85e7a20000000p-2f, -0x1.afb2d60000000p-27f, 0x1.d96e820000000p-1f, 0x1.ee353c0000000p-26f },
+	{ 0x1.94a6be0000000p-2f, 0x1.3ea8d80000000p-27f, 0x1.d653f00000000p-1f, 0x1.cf90100000000p-27f },
+	{ 0x1.a34c920000000p-2f, -0x1.9d799c0000000p-29f, 0x1.d31bf80000000p-1f, 0x1.b1af800000000p-26f },
+	{ 0x1.b1d8300000000p-2f, 0x1.4c85860000000p-28f, 0x1.cfc6d00000000p-1f, -0x1.6b54980000000p-27f },
+	{ 0x1.c048b20000000p-2f, -0x1.09d7ec0000000p-27f, 0x1.cc54aa0000000p-1f, 0x1.594b980000000p-28f },
+	{ 0x1.ce9d2e0000000p-2f, 0x1.ea52900000000p-29f, 0x1.c8c5c00000000p-1f, -0x1.cc795e0000000p-27f },
+	{ 0x1.dcd4c20000000p-2f, -0x1.59ac6c0000000p-27f, 0x1.c51a480000000p-1f, 0x1.7162ec0000000p-26f },
+	{ 0x1.eaee880000000p-2f, -0x1.769f420000000p-27f, 0x1.c152800000000p-1f, 0x1.96df540000000p-27f },
+	{ 0x1.f8e99e0000000p-2f, 0x1.daaf260000000p-28f, 0x1.bd6ea40000000p-1f, -0x1.dfad620000000p-26f },
+	{ 0x1.0362940000000p-1f, -0x1.8e59aa0000000p-27f, 0x1.b96eee0000000p-1f, 0x1.eb10820000000p-26f },
+	{ 0x1.0a40220000000p-1f, -0x1.61f0000000000p-29f, 0x1.b553a40000000p-1f, 0x1.0c104e0000000p-29f },
+	{ 0x1.110d0c0000000p-1f, 0x1.2da70e0000000p-27f, 0x1.b11d040000000p-1f, 0x1.62a4c60000000p-29f },
+	{ 0x1.17c8e60000000p-1f, -0x1.a224a00000000p-30f, 0x1.accb520000000p-1f, 0x1.bda77a0000000p-27f },
+	{ 0x1.1e73440000000p-1f, -0x1.b935160000000p-26f, 0x1.a85ed40000000p-1f, 0x1.b9f0160000000p-28f },
+	{ 0x1.250bba0000000p-1f, -0x1.90ee880000000p-26f, 0x1.a3d7d00000000p-1f, 0x1.a95ee80000000p-28f },
+	{ 0x1.2b91de0000000p-1f, 0x1.5108440000000p-26f, 0x1.9f368e0000000p-1f, 0x1.b225f00000000p-26f },
+	{ 0x1.32054c0000000p-1f, -0x1.d6e8760000000p-26f, 0x1.9a7b5a0000000p-1f, 0x1.b5328a0000000p-28f },
+	{ 0x1.3865980000000p-1f, -0x1.753afa0000000p-26f, 0x1.95a67e0000000p-1f, 0x1.963f980000000p-34f },
+	{ 0x1.3eb25e0000000p-1f, -0x1.9265580000000p-26f, 0x1.90b8480000000p-1f, -0x1.ec89420000000p-27f },
+	{ 0x1.44eb380000000p-1f, 0x1.cf386a0000000p-29f, 0x1.8bb1060000000p-1f, -0x1.688dc00000000p-27f },
+	{ 0x1.4b0fc40000000p-1f, 0x1.aaadd80000000p-27f, 0x1.8691080000000p-1f, 0x1.aef4d80000000p-26f },
+	{ 0x1.511fa00000000p-1f, -0x1.4265720000000p-28f, 0x1.8158a40000000p-1f, -0x1.cdd2540000000p-26f },
+	{ 0x1.571a6a0000000p-1f, -0x1.3254ca0000000p-26f, 0x1.7c08280000000p-1f, -0x1.ec35620000000p-30f },
+	{ 0x1.5cffc20000000p-1f, -0x1.280e1e0000000p-26f, 0x1.769fec0000000p-1f, 0x1.9548480000000p-27f },
+	{ 0x1.62cf4a0000000p-1f, -0x1.b794e20000000p-27f, 0x1.7120460000000p-1f, 0x1.f4eed00000000p-26f },
+	{ 0x1.6888a40000000p-1f, 0x1.c269660000000p-26f, 0x1.6b89900000000p-1f, -0x1.5841280000000p-27f },
+	{ 0x1.6e2b780000000p-1f, -0x1.dfa1100000000p-28f, 0x1.65dc200000000p-1f, -0x1.0a39a40000000p-28f },
+	{ 0x1.73b7680000000p-1f, 0x1.bd4af00000000p-30f, 0x1.6018520000000p-1f, 0x1.bd58f80000000p-27f },
+};
+
+RM_HD float sc_tab(int j, int w)
+{
+#if defined(__CUDA_ARCH__)
+	return SC_TAB_D[j][w];
+#else
+	return SC_TAB_H[j][w];
+#endif
+}
+
+// sin x and cos x rounded to float (*s, *c) and the residuals of those
+// roundings (*rs, *rc: float-float value minus the rounded value).
+RM_HD void ff_sincos_core(float x, float* s, float* c, float* rs, float* rc)
+{
+	if (fabsf(x) < SC_TINY) {
+		*s = x; *rs = -(x * x * x) * (1.0f / 6.0f);
+		*c = 1.0f; *rc = -(x * x) * 0.5f;
+		return;
+	}
+	// x = k pi/2 + r, r = rh + rl
+	const float kf = rintf(x * SC_TWO_OVER_PI);
+	const int k = (int)kf;
+	const float t1 = x - kf * SC_P1;                 // both exact
+	const FF q2 = ff_two_prod(kf, SC_P2);
+	const FF q3 = ff_two_prod(kf, SC_P3);
+	const FF a1 = ff_two_sum(t1, -q2.h);
+	const FF a2 = ff_two_sum(a1.h, -q2.l);
+	const FF a3 = ff_two_sum(a2.h, -q3.h);
+	const float lo0 = ((a1.l + a2.l) + a3.l) - q3.l - kf * SC_P4;
+	const FF r = ff_two_sum(a3.h, lo0);
+	// r = j/64 + d
+	const float jf = rintf(r.h * 64.0f);
+	const int j = (int)jf;
+	const FF d = ff_two_sum(r.h - jf * (1.0f / 64.0f), r.l);   // the difference is exact
+	const int ja = j < 0 ? -j : j;
+	const float sg = j < 0 ? -1.0f : 1.0f;
+	const float Sh = sg * sc_tab(ja, 0), Sl = sg * sc_tab(ja, 1);
+	const float Ch = sc_tab(ja, 2), Cl = sc_tab(ja, 3);
+	// 1 - cos d = eh + el, sin d = d.h + sl
+	const FF dd = ff_two_prod(d.h, d.h);
+	const float eh = 0.5f * dd.h;
+	const float el = (0.5f * dd.l + d.h * d.l) - dd.h * dd.h * (1.0f / 24.0f);
+	const float s3 = (d.h * dd.h) * (1.0f / 6.0f) + dd.h * d.l * 0.5f - (d.h * dd.h) * dd.h * (1.0f / 120.0f);
+	const float sl = d.l - s3;
+	// sin r = S + C sin d - S (1 - cos d)
+	float sr, srr;
+	{
+		const FF A = ff_two_prod(Ch, d.h);
+		const FF B = ff_two_prod(Sh, eh);
+		const FF t = ff_two_sum(Sh, A.h);
+		const FF u = ff_two_sum(t.h, -B.h);
+		const float rest = ((Sl + A.l) - B.l) + ((Ch * sl + Cl * d.h) - (Sh * el + Sl * eh));
+		const float lo = (t.l + u.l) + rest;
+		sr = u.h + lo;
+		srr = lo - (sr - u.h);
+	}
+	// cos r = C - S sin d - C (1 - cos d)
+	float cr, crr;
+	{
+		const FF A = ff_two_prod(Sh, d.h);
+		const FF B = ff_two_prod(Ch, eh);
+		const FF t = ff_two_sum(Ch, -A.h);
+		const FF u = ff_two_sum(t.h, -B.h);
+		const float rest = ((Cl - A.l) - B.l) - ((Sh * sl + Sl * d.h) + (Ch * el + Cl * eh));
+		const float lo = (t.l + u.l) + rest;
+		cr = u.h + lo;
+		crr = lo - (cr - u.h);
+	}
+	switch (k & 3) {
+	case 0: *s = sr; *rs = srr; *c = cr; *rc = crr; break;
+	case 1: *s = cr; *rs = crr; *c = -sr; *rc = -srr; break;
+	case 2: *s = -sr; *rs = -srr; *c = -cr; *rc = -crr; break;
+	default: *s = -cr; *rs = -crr; *c = sr; *rc = srr; break;
+	}
+}
+
+// |r| / (half the spacing of floats from f toward r), as a float: exact,
+// since the spacing is a power of two.
+RM_HD float sc_midpoint_ratio(float f, float r)
+{
+	const uint32_t b = rm_bits(f) & 0x7fffffffu;
+	if (b < (25u << 23)) return 0.0f;    // |f| < 2^-102 (never reached above SC_TINY)
+	float half = rm_float((b & 0x7f800000u) - (24u << 23));
+	if ((b & 0x007fffffu) == 0 && ((r < 0.0f) != (f < 0.0f))) half *= 0.5f;
+	return fabsf(r) / half;
+}
+
+// open-addressing tables of (argument bits, host sinf / cosf bits), key 0 =
+// empty; sym: the host library is odd/even (sinf(-x) = -sinf(x),
+// cosf(-x) = cosf(x) on the whole domain), the keys are |x|
+struct SinCosExceptions {
+	const uint2* sin_slots;
+	const uint2* cos_slots;
+	uint32_t sin_mask, cos_mask;
+	int sin_shift, cos_shift;
+	float sin_near, cos_near;   // look up when sc_midpoint_ratio >= this
+	int sym;
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ float sc_patch(const uint2* slots, uint32_t mask, int shift, int sym, bool odd, float x,
+                                          float y)
+{
+	const uint32_t b = sym ? (__float_as_uint(x) & 0x7fffffffu) : __float_as_uint(x);
+	uint32_t h = ff_hash(b, shift);
+	for (;;) {
+		const uint2 e = __ldg(&slots[h]);
+		if (e.x == 0) return y;
+		if (e.x == b) {
+			const float v = __uint_as_float(e.y);
+			return (sym && odd && x < 0.0f) ? -v : v;
+		}
+		h = (h + 1) & mask;
+	}
+}
+
+// The host C library's sinf(x) and cosf(x), exactly for |x| <= SC_LIMIT.
+__device__ __forceinline__ void ref_sincosf(const SinCosExceptions& T, float x, float* s, float* c)
+{
+	if (!(fabsf(x) <= SC_LIMIT)) {
+		*s = (float)sin((double)x);
+		*c = (float)cos((double)x);
+		return;
+	}
+	float fs, fc, rs, rc;
+	ff_sincos_core(x, &fs, &fc, &rs, &rc);
+	if (sc_midpoint_ratio(fs, rs) >= T.sin_near) fs = sc_patch(T.sin_slots, T.sin_mask, T.sin_shift, T.sym, true, x, fs);
+	if (sc_midpoint_ratio(fc, rc) >= T.cos_near) fc = sc_patch(T.cos_slots, T.cos_mask, T.cos_shift, T.sym, false, x, fc);
+	*s = fs;
+	*c = fc;
+}
+__device__ __forceinline__ float ref_sinf(const SinCosExceptions& T, float x)
+{
+	if (!(fabsf(x) <= SC_LIMIT)) return (float)sin((double)x);
+	float fs, fc, rs, rc;
+	ff_sincos_core(x, &fs, &fc, &rs, &rc);
+	if (sc_midpoint_ratio(fs, rs) >= T.sin_near) fs = sc_patch(T.sin_slots, T.sin_mask, T.sin_shift, T.sym, true, x, fs);
+	return fs;
+}
+#endif
+
+// host side (refmath.cpp): table shared by all simulations on a device
+bool sincos_exceptions_for_device(SinCosExceptions* out, size_t* count, std::string& err);
+
 }  // namespace umans
