@@ -137,3 +137,34 @@ def test_ref_sincosf_edges():
     x = np.concatenate([near, np.float32([0.0, -0.0, 1e-45, -1e-45, 1e-30, 2.0 ** -12, -(2.0 ** -12), 64.0, -64.0,
                                           np.nextafter(np.float32(2.0 ** -12), np.float32(0))])]).astype(np.float32)
     _check_sincos(x[np.abs(x) <= 64])
+
+
+FRESH = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from umans_gb300 import Simulation
+g = dict(np.load(sys.argv[2]))
+open(sys.argv[3], "wb").write(g["xml"].tobytes())
+sim = Simulation(sys.argv[3])
+done, worst = 0, 0.0
+for k, s in enumerate(g["steps"]):
+    sim.step(int(s) - done)
+    done = int(s)
+    worst = max(worst, float(np.abs(sim.positions() - g["pos"][k]).max()))
+print(worst)
+"""
+
+
+@pytest.mark.parametrize("name", ["crossing40_RVO", "toric60_Dutra"])
+def test_first_simulation_of_a_process_uses_the_tables(name, tmp_path):
+    """A process whose first simulation needs the sine tables sets them itself
+    (random-sample rotations are detected from the sampling schedule)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    npz = os.path.join(root, "tests", "golden", name + ".npz")
+    r = subprocess.run([sys.executable, "-c", FRESH, root, npz, str(tmp_path / "x.xml")], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert float(r.stdout.strip().splitlines()[-1]) == 0.0

@@ -1845,13 +1845,11 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	}
 	d_->edges = edges_dev_;
 	if (!build_tables()) return false;
-	// the host sinf/cosf: random-sample rotations, the gradient rotations of
-	// TtcaDca and FOEAvoidance, the segment collision times
-	bool need_trig = !edges_.empty();
-	for (const auto& p : pols_) {
-		need_trig |= p.table_random != 0;
+	// the host sinf/cosf: random-sample rotations (build_tables), the gradient
+	// rotations of TtcaDca and FOEAvoidance, the segment collision times
+	bool need_trig = need_trig_ || !edges_.empty();
+	for (const auto& p : pols_)
 		for (int c = 0; c < p.ncost; ++c) need_trig |= p.cost[c].kind == K_TTCADCA || p.cost[c].kind == K_FOE;
-	}
 	if (need_trig && !set_device_sincos(err_)) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;
@@ -1921,6 +1919,8 @@ bool Engine::build_tables()
 		maxdraws = std::max(maxdraws, (size_t)p.nsamples * p.draws);
 	}
 	if (table.empty()) table.push_back(SampleEntry{ 0, 0, 0, 0 });
+	need_trig_ = false;
+	for (const auto& p : pols) need_trig_ |= p.table_random != 0;
 	std::vector<uint32_t> pw(maxdraws + 3);
 	pw[0] = 1;
 	for (size_t k = 1; k < pw.size(); ++k) pw[k] = (uint32_t)(((uint64_t)pw[k - 1] * LCG_A) % LCG_M);

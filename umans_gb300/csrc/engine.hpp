@@ -188,6 +188,7 @@ private:
 	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
 	int prof_steps_ = 0;
 	std::vector<int> pol_scen_;   // scenario of each policy
+	bool need_trig_ = false;      // a policy samples random rotations (build_tables)
 	// k_agent launches: one per kernel group (scenarios ordered by group in
 	// cell space)
 	struct KGroup {

@@ -561,6 +561,7 @@ struct SinCosExceptions {
 __device__ __forceinline__ float sc_patch(const uint2* slots, uint32_t mask, int shift, int sym, bool odd, float x,
                                           float y)
 {
+	if (slots == nullptr) return y;   // tables not set on this device: the float-float value
 	const uint32_t b = sym ? (__float_as_uint(x) & 0x7fffffffu) : __float_as_uint(x);
 	uint32_t h = ff_hash(b, shift);
 	for (;;) {
