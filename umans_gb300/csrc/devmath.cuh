@@ -155,17 +155,15 @@ UD bool angle_less(float2 a, float2 b, float thr, float cos_thr)
 
 UD bool vclockwise(float2 a, float2 b) { float c = a.x * b.y - a.y * b.x; return c < 0; }
 
-// getLineIntersection: vector2D.h:249-272 (double)
+// getLineIntersection: vector2D.h:249-272 (float-float fast path, double
+// pipeline when the fast path cannot decide; refmath.hpp)
 UD bool line_intersection(float2 a, float2 b, float2 c, float2 d, float2* res)
 {
-	double a1 = b.y - a.y, b1 = a.x - b.x;
-	double c1 = __dadd_rn(__dmul_rn(a1, (double)a.x), __dmul_rn(b1, (double)a.y));
-	double a2 = d.y - c.y, b2 = c.x - d.x;
-	double c2 = __dadd_rn(__dmul_rn(a2, (double)c.x), __dmul_rn(b2, (double)c.y));
-	double det = __dsub_rn(__dmul_rn(a1, b2), __dmul_rn(a2, b1));
-	if (fabs(det) < 0.00001) return false;
-	res->x = (float)__ddiv_rn(__dsub_rn(__dmul_rn(b2, c1), __dmul_rn(b1, c2)), det);
-	res->y = (float)__ddiv_rn(__dsub_rn(__dmul_rn(a1, c2), __dmul_rn(a2, c1)), det);
+	float x, y;
+	const int r = line_intersection_ff(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, &x, &y);
+	if (r == 0) return false;
+	if (r < 0 && !line_intersection_d(a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, &x, &y)) return false;
+	*res = V(x, y);
 	return true;
 }
 

@@ -603,4 +603,94 @@ __device__ __forceinline__ float ref_sinf(const SinCosExceptions& T, float x)
 // host side (refmath.cpp): table shared by all simulations on a device
 bool sincos_exceptions_for_device(SinCosExceptions* out, size_t* count, std::string& err);
 
+// ---------------------------------------------------------------------------
+// getLineIntersection (vector2D.h:249-272) without FP64 in the common case.
+//
+// The reference intersects lines in double: a1, b1, a2, b2 are float
+// differences, c1, c2 and the determinant sums of exact products rounded to
+// double, the result coordinates (b2 c1 - b1 c2) / det and (a1 c2 - a2 c1) /
+// det rounded to double and then to float.  FP64 is slow on this GPU, and
+// Paris evaluates the intersection for every (sample, neighbour) pair.  The
+// same expressions are evaluated here in float-float arithmetic (~2^-46),
+// with a bound on the distance between that value and the double
+// pipeline's (both within a few 2^-46 of the exact value, amplified by the
+// cancellation in det and in the numerators).  When the float rounding of
+// every value within the bound is the same, and the parallel-lines test is
+// decided outside its own bound, the float-float result is the reference's;
+// otherwise the caller evaluates the double pipeline (line_intersection_d).
+
+// the double pipeline, as the reference evaluates it (no contraction)
+RM_HD bool line_intersection_d(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
+                               float* rx, float* ry)
+{
+	const double a1 = (double)(by - ay), b1 = (double)(ax - bx);
+	const double c1 = a1 * (double)ax + b1 * (double)ay;
+	const double a2 = (double)(dy - cy), b2 = (double)(cx - dx);
+	const double c2 = a2 * (double)cx + b2 * (double)cy;
+	const double det = a1 * b2 - a2 * b1;
+	if (fabs(det) < 0.00001) return false;
+	*rx = (float)((b2 * c1 - b1 * c2) / det);
+	*ry = (float)((a1 * c2 - a2 * c1) / det);
+	return true;
+}
+
+RM_HD FF ff_add2(FF x, FF y)
+{
+	const FF s = ff_two_sum(x.h, y.h);
+	return ff_two_sum(s.h, s.l + (x.l + y.l));
+}
+RM_HD FF ff_mulf(FF x, float b)
+{
+	const FF p = ff_two_prod(x.h, b);
+	return ff_fast_two_sum(p.h, p.l + x.l * b);
+}
+RM_HD FF ff_div2(FF n, FF d)
+{
+	const float q1 = n.h / d.h;
+	const FF p = ff_two_prod(q1, d.h);
+	const FF r = ff_add2(n, FF{ -p.h, -(p.l + q1 * d.l) });
+	return ff_fast_two_sum(q1, r.h / d.h);
+}
+// true when every value within `bound` of v rounds to the float v.h
+RM_HD bool ff_rounds_to_h(FF v, float bound)
+{
+	const uint32_t b = rm_bits(v.h) & 0x7fffffffu;
+	if (b < (40u << 23) || b >= 0x7e800000u) return false;   // |v| < 2^-87 or > 2^126, inf, nan
+	float half = rm_float((b & 0x7f800000u) - (24u << 23));
+	if ((b & 0x007fffffu) == 0) half *= 0.5f;                 // finer spacing below a power of two
+	return half - fabsf(v.l) > bound;
+}
+
+// 1: intersection (*rx, *ry), 0: parallel, -1: undecided (use the double pipeline)
+RM_HD int line_intersection_ff(float ax, float ay, float bx, float by, float cx, float cy, float dx, float dy,
+                               float* rx, float* ry)
+{
+	const float a1 = by - ay, b1 = ax - bx, a2 = dy - cy, b2 = cx - dx;
+	const FF c1 = ff_add2(ff_two_prod(a1, ax), ff_two_prod(b1, ay));
+	const FF c2 = ff_add2(ff_two_prod(a2, cx), ff_two_prod(b2, cy));
+	const FF p = ff_two_prod(a1, b2), q = ff_two_prod(a2, b1);
+	const FF det = ff_add2(p, FF{ -q.h, -q.l });
+	// magnitudes for the error bounds (float estimates; the 2^-43 factor is
+	// ~8x the float-float and double error constants)
+	const float TINY = 0x1p-100f;
+	const float Mc1 = fabsf(a1 * ax) + fabsf(b1 * ay) + TINY;
+	const float Mc2 = fabsf(a2 * cx) + fabsf(b2 * cy) + TINY;
+	const float Mdet = fabsf(p.h) + fabsf(q.h) + TINY;
+	const float adet = fabsf(det.h);
+	const float T = 1e-5f;
+	const float margin = 0x1p-43f * Mdet + 0x1p-20f * T;
+	if (adet < T - margin) return 0;
+	if (!(adet > T + margin)) return -1;
+	const FF nx = ff_add2(ff_mulf(c1, b2), ff_mulf(c2, -b1));
+	const FF ny = ff_add2(ff_mulf(c2, a1), ff_mulf(c1, -a2));
+	const FF X = ff_div2(nx, det), Y = ff_div2(ny, det);
+	const float kdet = Mdet / adet + 1.0f;
+	const float Bx = 0x1p-43f * ((fabsf(b2) * Mc1 + fabsf(b1) * Mc2) / adet + fabsf(X.h) * kdet);
+	const float By = 0x1p-43f * ((fabsf(a1) * Mc2 + fabsf(a2) * Mc1) / adet + fabsf(Y.h) * kdet);
+	if (!ff_rounds_to_h(X, Bx) || !ff_rounds_to_h(Y, By)) return -1;
+	*rx = X.h;
+	*ry = Y.h;
+	return 1;
+}
+
 }  // namespace umans
