@@ -133,11 +133,12 @@ int umans_stream(umans_sim* sim, void** stream);
 /* device addresses of the float2 position / velocity arrays (list order) */
 int umans_device_state(umans_sim* sim, void** pos, void** vel);
 /* Profiling: when enabled, each step runs without the CUDA graph and is
- * bracketed by CUDA events on the simulation's stream (whole step, and the
- * fused per-agent kernel); totals accumulate until the next umans_profile. */
+ * bracketed by CUDA events on the simulation's stream (whole step, the grid
+ * build k_bbox..k_scatter, and the fused per-agent kernels); totals
+ * accumulate until the next umans_profile. */
 int umans_profile(umans_sim* sim, int enable);
 int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_ms, int* steps,
-                         int* kernels_per_step);
+                         int* kernels_per_step, double* grid_build_ms);
 /* Differentiable form (no counterpart in the reference), for calibrating
  * force-model parameters against observed trajectories.  Supported policies:
  * method "gradient" with SocialForcesAvoidance, PowerLaw and

@@ -62,7 +62,7 @@ _SIGS = {
     "umans_device_state": (C.c_int, [P, C.POINTER(P), C.POINTER(P)]),
     "umans_profile": (C.c_int, [P, C.c_int]),
     "umans_profile_totals": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int),
-                                       C.POINTER(C.c_int)]),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "umans_diff_begin": (C.c_int, [P, C.c_int, C.c_int, P, C.c_float]),
     "umans_diff_forward": (C.c_int, [P, C.POINTER(C.c_double)]),
     "umans_diff_backward": (C.c_int, [P, P, P, P]),

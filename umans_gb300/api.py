@@ -120,10 +120,12 @@ class Simulation:
         self._check(self._lib.umans_profile(self._h, int(bool(enable))))
 
     def profile_totals(self) -> dict:
-        a, b = C.c_double(), C.c_double()
+        a, b, g = C.c_double(), C.c_double(), C.c_double()
         n, k = C.c_int(), C.c_int()
-        self._check(self._lib.umans_profile_totals(self._h, C.byref(a), C.byref(b), C.byref(n), C.byref(k)))
-        return dict(agent_kernel_ms=a.value, step_ms=b.value, steps=n.value, kernels_per_step=k.value)
+        self._check(self._lib.umans_profile_totals(self._h, C.byref(a), C.byref(b), C.byref(n), C.byref(k),
+                                                   C.byref(g)))
+        return dict(agent_kernel_ms=a.value, step_ms=b.value, steps=n.value, kernels_per_step=k.value,
+                    grid_build_ms=g.value)
 
     # --- state ----------------------------------------------------------
     def state(self) -> dict:

@@ -258,12 +258,14 @@ int umans_profile(umans_sim* s, int enable)
 	return UMANS_OK;
 }
 
-int umans_profile_totals(umans_sim* s, double* agent_kernel_ms, double* step_ms, int* steps, int* kernels_per_step)
+int umans_profile_totals(umans_sim* s, double* agent_kernel_ms, double* step_ms, int* steps, int* kernels_per_step,
+                         double* grid_build_ms)
 {
 	if (!s) return UMANS_ERR_ARGUMENT;
-	double a = 0, b = 0;
+	double a = 0, b = 0, g = 0;
 	int n = 0;
-	s->eng->profile_totals(&a, &b, &n);
+	s->eng->profile_totals(&a, &b, &n, &g);
+	if (grid_build_ms) *grid_build_ms = g;
 	if (agent_kernel_ms) *agent_kernel_ms = a;
 	if (step_ms) *step_ms = b;
 	if (steps) *steps = n;

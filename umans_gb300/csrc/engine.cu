@@ -2316,11 +2316,13 @@ bool Engine::run_steps(int nsteps, bool record)
 			if (profile_) {
 				CK(cudaEventRecord(ps1_, stream_));
 				CK(cudaEventSynchronize(ps1_));
-				float a = 0, b = 0;
+				float a = 0, b = 0, g = 0;
 				cudaEventElapsedTime(&a, pa0_, pa1_);
 				cudaEventElapsedTime(&b, ps0_, ps1_);
+				cudaEventElapsedTime(&g, ps0_, pa0_);
 				prof_agent_ms_ += a;
 				prof_step_ms_ += b;
+				prof_grid_ms_ += g;
 				prof_steps_ += 1;
 			}
 		}

@@ -90,9 +90,9 @@ public:
 	// Profiling mode: every step is launched without the graph, with CUDA
 	// events on the engine's stream around the step and around k_agent;
 	// the elapsed times accumulate until reset.
-	void set_profile(bool on) { profile_ = on; prof_agent_ms_ = prof_step_ms_ = 0; prof_steps_ = 0; }
-	void profile_totals(double* agent_ms, double* step_ms, int* steps) const
-	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; }
+	void set_profile(bool on) { profile_ = on; prof_agent_ms_ = prof_step_ms_ = prof_grid_ms_ = 0; prof_steps_ = 0; }
+	void profile_totals(double* agent_ms, double* step_ms, int* steps, double* grid_ms) const
+	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; *grid_ms = prof_grid_ms_; }
 	int kernels_per_step() const;
 
 	// ---- differentiable form ------------------------------------------
@@ -185,7 +185,7 @@ private:
 	bool snap_valid_ = false;
 	bool steps_pending_ = false;   // steps enqueued whose status has not been read
 	double snap_time_ = 0;
-	double prof_agent_ms_ = 0, prof_step_ms_ = 0;
+	double prof_agent_ms_ = 0, prof_step_ms_ = 0, prof_grid_ms_ = 0;
 	int prof_steps_ = 0;
 	std::vector<int> pol_scen_;   // scenario of each policy
 	bool need_trig_ = false;      // a policy samples random rotations (build_tables)
