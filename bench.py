@@ -65,8 +65,9 @@ def workload(name: str, tmp: str, agents: int = 0):
         cfg = dict(workload="socialforces_toric", agents=n, world=f"toric {side:.0f}x{side:.0f} m",
                    policy="SocialForcesAvoidance(range 5)+GoalReachingForce, gradient", dt=0.1)
     elif name == "karamouzas_corridor":
-        sc = S.karamouzas_corridor()
-        cfg = dict(workload="karamouzas_corridor", agents=1_000_000, world="infinite, 10000x100 m corridor",
+        n = agents or 1_000_000
+        sc = S.karamouzas_corridor(n)
+        cfg = dict(workload="karamouzas_corridor", agents=n, world=f"infinite, {n // 100}x100 m corridor",
                    policy="Karamouzas(range 10), regular sampling 181 samples", dt=0.05)
     elif name == "circle_orca":
         sc = S.circle_orca()
@@ -245,6 +246,49 @@ def diff_leg(tmp: str, sets: int = 256, n: int = 512, steps: int = 100, every: i
                              "gradients are checked at short horizons in tests/test_gpu_diff.py",
             "timing": f"median of {reps} after one warm-up, host clock around synchronous calls; "
                       "inputs (tape ~0.7 GB) exceed L2"}
+
+
+def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: int = 0,
+               cpu_seconds: float = 10.0) -> dict:
+    """Another configuration of the reference's benchmark list, timed like the
+    headline (per-step CUDA events, L2 flushed before each step), with the
+    reference CPU step beside it (on the full case, or on a smaller case at
+    the same density when the full one would take minutes per step)."""
+    import torch
+    from umans_gb300 import Simulation
+    sub = os.path.join(tmp, name)
+    os.makedirs(sub, exist_ok=True)
+    path, n, cfg = workload(name, sub)
+    sim = Simulation(path)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    sim.step(warmup)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+            evs[k][0].record(stream)
+        sim.step_async(1)
+        evs[k][1].record(stream)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    t_ms = sum(a.elapsed_time(b) for a, b in evs)
+    sim.close()
+    out = dict(config=dict(cfg, timed_steps=f"steps {warmup + 1}..{warmup + steps}",
+                           l2="flushed (256 MiB write) before every timed step"),
+               value=n * steps / (t_ms / 1e3), unit="agent-steps/s", steps=steps, warmup=warmup,
+               ms_per_step=t_ms / steps)
+    if cpu_agents >= 0:
+        cpath, cn = path, n
+        if cpu_agents:
+            csub = os.path.join(sub, "cpu")
+            os.makedirs(csub, exist_ok=True)
+            cpath, cn, _ = workload(name, csub, cpu_agents)
+        cb = cpu_baseline(cpath, cn, seconds=cpu_seconds, max_steps=steps if not cpu_agents else 10_000)
+        if cpu_agents:
+            cb["sample"] = cb["sample"].replace("full", "same-density") + f" (the GPU case has {n} agents)"
+        out["cpu_baseline"] = cb
+    return out
 
 
 def cpu_baseline(path: str, n_agents: int, seconds: float = 30.0, threads: int | None = None, max_steps: int = 500):
@@ -436,6 +480,12 @@ def run_ours(args):
         cpu = cpu_baseline(path, n, max_steps=args.steps) if (rank == 0 and world == 1 and not args.no_cpu) else None
         batched = None if args.no_batch else batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
         diff = None if args.no_diff else diff_leg(tmp, sets=args.diff_sets)
+        extra = None
+        if not args.no_extra and world == 1:
+            extra = {"small_orca_circle": config_leg("circle_orca", tmp, 300, args.warmup, flush,
+                                                     cpu_agents=0 if not args.no_cpu else -1),
+                     "sampling_heavy_karamouzas": config_leg("karamouzas_corridor", tmp, 5, 3, flush,
+                                                             cpu_agents=20_000 if not args.no_cpu else -1)}
     if rank != 0:
         return
     cfg = dict(cfg, l2="flushed (256 MiB write) before every timed step; state ~10 MB would fit in L2",
@@ -471,6 +521,8 @@ def run_ours(args):
         line["batched"] = batched
     if diff:
         line["differentiable"] = diff
+    if extra:
+        line["other_configs"] = extra
     print(json.dumps(line))
 
 
@@ -485,6 +537,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the small ORCA and sampling-heavy Karamouzas configurations")
     ap.add_argument("--agents", type=int, default=0,
                     help="agents of the SocialForces workload at the same density (default 100000)")
     ap.add_argument("--diff-sets", type=int, default=256, help="parameter sets of the differentiable leg")
