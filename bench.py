@@ -387,10 +387,19 @@ def run_ours(args):
     import torch
     torch.cuda.set_device(local)
     with tempfile.TemporaryDirectory() as tmp:
+        legs = {}
+        tl = time.perf_counter()
+
+        def lap(name):
+            nonlocal tl
+            now = time.perf_counter()
+            legs[name] = round(now - tl, 1)
+            tl = now
         path, n, cfg = workload(args.workload, tmp, args.agents)
         sim = Simulation(path)
         stream = torch.cuda.ExternalStream(sim.stream)
         flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        lap("setup")
         sim.step(args.warmup)
         # --- device-resident throughput, L2 flushed before every step ----
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -411,6 +420,7 @@ def run_ours(args):
         t_ms = max_over_ranks(dist, t_ms)
         value = replica_rate(world, n, args.steps, t_ms / 1e3)
         sim.close()
+        lap("plain")
         # --- back-to-back steps (L2 warm), same step range, fresh state ----
         sim = Simulation(path)
         stream = torch.cuda.ExternalStream(sim.stream)
@@ -449,6 +459,7 @@ def run_ours(args):
         sm_max = clocks.get("sm_max_mhz") or 2070.0
         fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
         sim.close()
+        lap("warm_and_profile")
         # --- e2e through the reference-facing C functions ----------------
         u = UMANS()
         assert u.startSimulation(path, 1)
@@ -477,15 +488,20 @@ def run_ours(args):
         te = max_over_ranks(dist, te)
         u.cleanUp()
         e2e_value = replica_rate(world, n, args.steps, te)
+        lap("e2e")
         cpu = cpu_baseline(path, n, max_steps=args.steps) if (rank == 0 and world == 1 and not args.no_cpu) else None
+        lap("cpu_baseline")
         batched = None if args.no_batch else batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
+        lap("batched")
         diff = None if args.no_diff else diff_leg(tmp, sets=args.diff_sets)
+        lap("differentiable")
         extra = None
         if not args.no_extra and world == 1:
             extra = {"small_orca_circle": config_leg("circle_orca", tmp, 300, args.warmup, flush,
                                                      cpu_agents=0 if not args.no_cpu else -1),
                      "sampling_heavy_karamouzas": config_leg("karamouzas_corridor", tmp, 5, 3, flush,
                                                              cpu_agents=20_000 if not args.no_cpu else -1)}
+        lap("other_configs")
     if rank != 0:
         return
     cfg = dict(cfg, l2="flushed (256 MiB write) before every timed step; state ~10 MB would fit in L2",
@@ -523,6 +539,7 @@ def run_ours(args):
         line["differentiable"] = diff
     if extra:
         line["other_configs"] = extra
+    line["leg_seconds"] = legs
     print(json.dumps(line))
 
 
