@@ -104,10 +104,8 @@ __device__ __forceinline__ float o2f(unsigned u)
 }
 
 // bounding box of the agents of each infinite-world scenario
-__global__ void k_bbox(DevState S)
+__device__ __forceinline__ void bbox_one(const DevState& S, int i)
 {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= S.n) return;
 	const int s = S.agent_scen[i];
 	if (S.scen[s].world == W_TORIC) return;
 	const float2 p = S.pos[i];
@@ -119,6 +117,43 @@ __global__ void k_bbox(DevState S)
 		atomicMin(&B[0], a); atomicMin(&B[1], b);
 		atomicMax(&B[2], c); atomicMax(&B[3], d);
 	}
+}
+__global__ void k_bbox(DevState S)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < S.n) bbox_one(S, i);
+}
+
+// grid of scenario s (origin, cell size, counts) from its bounding box, which
+// is reset for the next step; returns the scenario's cell count
+__device__ int grid_params(const DevState& S, int s)
+{
+	const ScenDesc sd = S.scen[s];
+	unsigned* B = S.bbox + 4 * s;
+	float x0, y0, ex, ey;
+	if (sd.world == W_TORIC) {
+		x0 = -0.5f * sd.width; y0 = -0.5f * sd.height; ex = sd.width; ey = sd.height;
+	} else {
+		x0 = o2f(__ldcg(&B[0])); y0 = o2f(__ldcg(&B[1]));
+		ex = o2f(__ldcg(&B[2])) - x0; ey = o2f(__ldcg(&B[3])) - y0;
+		if (sd.n == 0) { x0 = y0 = 0; ex = ey = 1; }
+	}
+	B[0] = B[1] = f2o(FLT_MAX);
+	B[2] = B[3] = f2o(-FLT_MAX);
+	if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
+		atomicOr(S.status, ST_GRID_OVERFLOW);
+		x0 = y0 = 0; ex = ey = 1;
+	}
+	float cs = sd.max_range / S.cells_per_range;
+	if (!(cs >= 1e-3f)) cs = 1e-3f;
+	// +2 per axis: nx, ny below come from float divisions that may round up
+	while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)sd.max_cells) cs *= 2.0f;
+	GridParams g;
+	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
+	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
+	g.ncells = g.nx * g.ny; g.pad = 0;
+	S.grid[s] = g;
+	return g.ncells;
 }
 
 // One block: grid parameters of every scenario, then the exclusive scan of
@@ -133,33 +168,9 @@ __global__ void __launch_bounds__(1024) k_grid(DevState S)
 	int local = 0;
 	for (int k = 0; k < per && s0 + k < ns; ++k) {
 		const int s = S.scen_order[s0 + k];
-		const ScenDesc sd = S.scen[s];
-		unsigned* B = S.bbox + 4 * s;
-		float x0, y0, ex, ey;
-		if (sd.world == W_TORIC) {
-			x0 = -0.5f * sd.width; y0 = -0.5f * sd.height; ex = sd.width; ey = sd.height;
-		} else {
-			x0 = o2f(B[0]); y0 = o2f(B[1]);
-			ex = o2f(B[2]) - x0; ey = o2f(B[3]) - y0;
-			if (sd.n == 0) { x0 = y0 = 0; ex = ey = 1; }
-		}
-		B[0] = B[1] = f2o(FLT_MAX);
-		B[2] = B[3] = f2o(-FLT_MAX);
-		if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
-			atomicOr(S.status, ST_GRID_OVERFLOW);
-			x0 = y0 = 0; ex = ey = 1;
-		}
-		float cs = sd.max_range / S.cells_per_range;
-		if (!(cs >= 1e-3f)) cs = 1e-3f;
-		// +2 per axis: nx, ny below come from float divisions that may round up
-		while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)sd.max_cells) cs *= 2.0f;
-		GridParams g;
-		g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
-		g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
-		g.ncells = g.nx * g.ny; g.pad = 0;
-		S.grid[s] = g;
-		S.cell_base[s] = g.ncells;
-		local += g.ncells;
+		const int nc = grid_params(S, s);
+		S.cell_base[s] = nc;
+		local += nc;
 	}
 	__shared__ int tot[1024];
 	tot[threadIdx.x] = local;
@@ -187,17 +198,21 @@ __device__ __forceinline__ int cell_coord(float v, float v0, float inv, int nmax
 	return c >= nmax ? nmax - 1 : c;
 }
 
+// cell of agent i (grid g, cells of its scenario from cb) and its histogram count
+__device__ __forceinline__ void count_one(const DevState& S, int i, const GridParams& g, int cb)
+{
+	const float2 p = S.pos[i];
+	const int c = cb + cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
+	S.cell[i] = c;
+	const unsigned peers = __match_any_sync(__activemask(), c);
+	if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.cnt[c], __popc(peers));
+}
 __global__ void k_count(DevState S)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= S.n) return;
 	const int sc = S.agent_scen[i];
-	const GridParams g = S.grid[sc];
-	const float2 p = S.pos[i];
-	const int c = S.cell_base[sc] + cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
-	S.cell[i] = c;
-	const unsigned peers = __match_any_sync(__activemask(), c);
-	if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.cnt[c], __popc(peers));
+	count_one(S, i, S.grid[sc], S.cell_base[sc]);
 }
 
 // exclusive scan of cnt[0..ncells) in 3 passes; 1024 cells per block
@@ -282,10 +297,8 @@ __global__ void k_scan_down(DevState S)
 	if (blockIdx.x == 0 && threadIdx.x == 0) S.start[nc] = S.n;
 }
 
-__global__ void k_scatter(DevState S)
+__device__ __forceinline__ void scatter_one(const DevState& S, int i)
 {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= S.n) return;
 	const int c = S.cell[i];
 	const unsigned act = __activemask();
 	const unsigned peers = __match_any_sync(act, c);
@@ -315,6 +328,62 @@ __global__ void k_scatter(DevState S)
 	S.sE[t] = make_float4(eb.x, eb.y, vmag(v), 0.0f);
 	S.sSlot[t] = i;
 	S.sId[t] = S.id[i];
+}
+__global__ void k_scatter(DevState S)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < S.n) scatter_one(S, i);
+}
+
+// The whole grid build of a small single-scenario world in one block (the
+// same steps as k_bbox .. k_scatter, phases separated by block barriers):
+// one launch instead of seven, for worlds whose steps are launch-bound.
+// Values written by atomics in one phase are read through L2 (__ldcg).
+constexpr int SMALL_MAX_AGENTS = 4096, SMALL_MAX_CELLS = 32768;
+__global__ void __launch_bounds__(1024) k_build_small(DevState S)
+{
+	const int n = S.n, tid = threadIdx.x, nt = blockDim.x;
+	for (int i = tid; i < n; i += nt) bbox_one(S, i);
+	__syncthreads();
+	__shared__ GridParams g;
+	__shared__ int ncs;
+	if (tid == 0) {
+		const int nc = grid_params(S, 0);
+		S.cell_base[0] = 0;
+		S.cell_base[1] = nc;
+		g = S.grid[0];
+		ncs = nc;
+	}
+	__syncthreads();
+	for (int i = tid; i < n; i += nt) count_one(S, i, g, 0);
+	__syncthreads();
+	// exclusive scan of the histogram: per thread a run of cells, then the
+	// block's thread sums
+	const int nc = ncs;
+	const int per = (nc + nt - 1) / nt;
+	const int c0 = min(nc, tid * per), c1 = min(nc, c0 + per);
+	int local = 0;
+	for (int c = c0; c < c1; ++c) local += __ldcg(&S.cnt[c]);
+	__shared__ int tot[1024];
+	tot[tid] = local;
+	__syncthreads();
+	for (int o = 1; o < nt; o <<= 1) {
+		const int v = tid >= o ? tot[tid - o] : 0;
+		__syncthreads();
+		tot[tid] += v;
+		__syncthreads();
+	}
+	int run = tot[tid] - local;
+	for (int c = c0; c < c1; ++c) {
+		const int v = __ldcg(&S.cnt[c]);
+		S.start[c] = run;
+		S.fill[c] = run;
+		S.cnt[c] = 0;   // histogram is all-zero between steps
+		run += v;
+	}
+	if (tid == 0) S.start[nc] = n;
+	__syncthreads();
+	for (int i = tid; i < n; i += nt) scatter_one(S, i);
 }
 
 // ------------------------------------------------------------------------
@@ -2177,16 +2246,7 @@ void Engine::enqueue_step()
 	S.maxnb = maxnb_;
 	const int wpb = opt_.warps_per_block;
 	const size_t smem = (size_t)wpb * maxnb_ * 16;
-	const int threads = 256;
-	const int nb = std::max(1, (n_ + threads - 1) / threads);
-	k_bbox<<<nb, threads, 0, stream_>>>(S);
-	k_grid<<<1, 1024, 0, stream_>>>(S);
-	k_count<<<nb, threads, 0, stream_>>>(S);
-	const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
-	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
-	k_scan_top<<<1, 1024, 0, stream_>>>(S);
-	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
-	k_scatter<<<nb, threads, 0, stream_>>>(S);
+	enqueue_grid(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
 	// the agents of each kernel group form one range of the cell-sorted
 	// arrays (scenarios are ordered by group in cell space)
@@ -2204,14 +2264,16 @@ void Engine::enqueue_step()
 		if (te[k] <= tb[k]) return;
 		DevState A = S;
 		A.t_begin = tb[k]; A.t_end = te[k];
-		A.total_warps = g.blocks * wpb;
+		// no more blocks than the group has agents for (small worlds)
+		const int blocks = std::min(g.blocks, std::max(1, (te[k] - tb[k] + wpb - 1) / wpb));
+		A.total_warps = blocks * wpb;
 		A.scratch = S.scratch + g.scratch_off;
 		A.obs_list = S.obs_list + g.obs_off;
 		if (S.tape_list) {
-			if (g.mode == 1) k_agent<1, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
-			else k_agent<0, true><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
-		} else if (g.mode == 1) k_agent<1><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
-		else k_agent<0><<<g.blocks, wpb * 32, smem, st>>>(A, 0);
+			if (g.mode == 1) k_agent<1, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
+			else k_agent<0, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
+		} else if (g.mode == 1) k_agent<1><<<blocks, wpb * 32, smem, st>>>(A, 0);
+		else k_agent<0><<<blocks, wpb * 32, smem, st>>>(A, 0);
 	};
 	// one after the other: each launch fills the GPU (measured: running the
 	// groups on concurrent streams was no faster)
@@ -2219,7 +2281,32 @@ void Engine::enqueue_step()
 	if (profile_) cudaEventRecord(pa1_, stream_);
 }
 
-int Engine::kernels_per_step() const { return 7 + (int)groups_.size(); }
+bool Engine::small_world() const
+{
+	return scen_.size() == 1 && n_ <= SMALL_MAX_AGENTS && d_->max_cells <= SMALL_MAX_CELLS;
+}
+
+// The grid build: one block for a small single-scenario world, else the
+// seven grid-wide kernels.
+void Engine::enqueue_grid(const DevState& S)
+{
+	if (small_world()) {
+		k_build_small<<<1, 1024, 0, stream_>>>(S);
+		return;
+	}
+	const int threads = 256;
+	const int nb = std::max(1, (n_ + threads - 1) / threads);
+	k_bbox<<<nb, threads, 0, stream_>>>(S);
+	k_grid<<<1, 1024, 0, stream_>>>(S);
+	k_count<<<nb, threads, 0, stream_>>>(S);
+	const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	k_scan_top<<<1, 1024, 0, stream_>>>(S);
+	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	k_scatter<<<nb, threads, 0, stream_>>>(S);
+}
+
+int Engine::kernels_per_step() const { return (small_world() ? 1 : 7) + (int)groups_.size(); }
 
 bool Engine::capture_graph()
 {
@@ -2709,15 +2796,7 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	float4* scr = nullptr;
 	if (!dalloc(scr, (size_t)T.total_warps * 2 * dump_nb, err_)) return false;
 	T.scratch = scr;
-	const int threads = 256, nb = (n_ + threads - 1) / threads;
-	k_bbox<<<nb, threads, 0, stream_>>>(T);
-	k_grid<<<1, 1024, 0, stream_>>>(T);
-	k_count<<<nb, threads, 0, stream_>>>(T);
-	const int sb = (T.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
-	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
-	k_scan_top<<<1, 1024, 0, stream_>>>(T);
-	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(T);
-	k_scatter<<<nb, threads, 0, stream_>>>(T);
+	enqueue_grid(T);
 	T.t_begin = 0;
 	T.t_end = n_;
 	k_agent<0><<<blocks, wpb * 32, smem, stream_>>>(T, 1);

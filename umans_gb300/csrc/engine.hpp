@@ -94,6 +94,7 @@ public:
 	void profile_totals(double* agent_ms, double* step_ms, int* steps, double* grid_ms) const
 	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; *grid_ms = prof_grid_ms_; }
 	int kernels_per_step() const;
+	bool small_world() const;   // one-block grid build (k_build_small)
 
 	// ---- differentiable form ------------------------------------------
 	// Episode: `steps` steps from the current state (recorded as the
@@ -138,6 +139,7 @@ private:
 	bool take_snapshot();
 	bool restore_snapshot();
 	void enqueue_step();
+	void enqueue_grid(const DevState& S);
 	bool capture_graph();
 	void invalidate_graph();
 	bool apply_pending_agents();
