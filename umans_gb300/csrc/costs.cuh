@@ -28,6 +28,13 @@ struct NbView {
 	const float4* edges;
 	const uint32_t* obs;
 	int KO;
+	// optional: the sample-invariant part of ttc_pair for every neighbour
+	// within pp_range, in list order (P = p - p_j, |P|^2 - (r + r_j)^2,
+	// v_j.x; v_j.y in pv), built once per agent before a sampling sweep
+	const float4* pp = nullptr;
+	const float* pv = nullptr;
+	int KP = 0;
+	float pp_range = -1.0f;
 };
 
 // PhantomAgent position offset of displacement group g (worldToric.cpp:61-79):
@@ -91,11 +98,21 @@ UD float ttc_first(const AgentCtx& A, const NbView& N, float2 vel, float maxDist
 {
 	float minT = MAXF;
 	const float md2 = maxDist * maxDist;
-	for (int k = 0; k < N.K; ++k) {
-		if (N.d2[k] > md2) continue;
-		const float t = ttc_pair(A.pos, vel, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
-		if (ignoreCurrent && t == 0) continue;
-		if (t < minT) minT = t;
+	if (N.pp != nullptr && maxDist == N.pp_range) {
+		// the same pairs and the same values (ttc_pair_pre), from the cache
+		for (int k = 0; k < N.KP; ++k) {
+			const float4 q = N.pp[k];
+			const float t = ttc_pair_pre(vel, V(q.x, q.y), q.z, V(q.w, N.pv[k]));
+			if (ignoreCurrent && t == 0) continue;
+			if (t < minT) minT = t;
+		}
+	} else {
+		for (int k = 0; k < N.K; ++k) {
+			if (N.d2[k] > md2) continue;
+			const float t = ttc_pair(A.pos, vel, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+			if (ignoreCurrent && t == 0) continue;
+			if (t < minT) minT = t;
+		}
 	}
 	for (int k = 0; k < N.KO; ++k) {
 		float2 a, b;

@@ -1151,6 +1151,44 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 		const SampleEntry e = S.table[pol.table_offset + bestI];
 		return vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
 	}
+	// costs that take the time to first collision per sample: the
+	// sample-invariant pair terms once per agent (not with ORCA, whose lines
+	// use the same scratch)
+	NbView NC = N;
+	{
+		float cr = -1.0f;
+		bool orca = false;
+		for (int ci = 0; ci < ncost; ++ci) {
+			const int kd = pol.cost[ci].kind;
+			orca |= kd == K_ORCA;
+			if (cr < 0.0f && (kd == K_RVO || kd == K_VANTOLL || kd == K_PLEDESTRIANS || kd == K_MOUSSAID ||
+			                  kd == K_KARAMOUZAS))
+				cr = pol.cost[ci].range;
+		}
+		if (cr >= 0.0f && !orca) {
+			const float md2 = cr * cr;
+			int KP = 0;
+			for (int b0 = 0; b0 < N.K; b0 += 32) {
+				const int k = b0 + lane;
+				const bool inr = k < N.K && !(N.d2[k] > md2);
+				const unsigned m = __ballot_sync(0xffffffffu, inr);
+				if (inr) {
+					const float2 Pd = vsub(A.pos, nb_pos(N, k));
+					const float R = A.radius + nb_radius(N, k);
+					const float2 vj = nb_vel(N, k);
+					const int idx = KP + __popc(m & ((1u << lane) - 1u));
+					pair4[idx] = make_float4(Pd.x, Pd.y, vdot(Pd, Pd) - R * R, vj.x);
+					pairv[idx] = vj.y;
+				}
+				KP += __popc(m);
+			}
+			__syncwarp();
+			NC.pp = pair4;
+			NC.pv = pairv;
+			NC.KP = KP;
+			NC.pp_range = cr;
+		}
+	}
 	for (int i = lane; i < pol.nsamples; i += 32) {
 		float2 v;
 		const int d0 = i * pol.draws;   // draws before this sample
@@ -1175,7 +1213,7 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			if (pol.cost[ci].kind == K_RANDOM)   // RandomFunction::GetCost: RandomFunction.cpp:25-28
 				cv = rng_uniform(mulmod(S.lcgpow[++jr], rng0), -1, 1);
 			else
-				cv = eval_cost(A, N, pol.cost[ci], P, ci, v);
+				cv = eval_cost(A, NC, pol.cost[ci], P, ci, v);
 			tc += coeff * cv;
 		}
 		if (tc < bestC) { bestC = tc; bestI = i; }
