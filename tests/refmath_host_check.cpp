@@ -4,7 +4,8 @@
 //    pipeline, on Paris-like, obstacle-like and adversarial inputs;
 //  * ff_sincos_core differs from the C library's sinf/cosf only at arguments
 //    whose value lies close to a rounding midpoint (the only ones the device
-//    looks up).
+//    looks up);
+//  * exp_gauss equals the double expression it stands for.
 #include "../umans_gb300/csrc/refmath.hpp"
 
 #include <cmath>
@@ -69,5 +70,17 @@ int main(int argc, char** argv)
 		if (c != lc) { ++diff; unflagged += sc_midpoint_ratio(c, rc) < 0.75f; }
 	}
 	std::printf("sincos n=%ld differ=%ld unflagged=%ld\n", m, diff, unflagged);
-	return (bad == 0 && unflagged == 0) ? 0 : 1;
+
+	long ge = 0, gbad = 0;
+	std::uniform_real_distribution<float> G(0, 1);
+	for (long i = 0; i < 4 * per_mode; ++i) {
+		const float sc = (i & 3) == 0 ? 0.1f : ((i & 3) == 1 ? 3.0f : ((i & 3) == 2 ? 15.0f : 40.0f));
+		const float a = sc * G(g), b = (i & 4) ? 0.0f : sc * G(g);
+		const double ad = a, bd = b;
+		const float want = (float)std::exp(-0.5 * (ad * ad + bd * bd));
+		++ge;
+		if (exp_gauss(a, b) != want) ++gbad;
+	}
+	std::printf("gauss n=%ld mismatches=%ld\n", ge, gbad);
+	return (bad == 0 && unflagged == 0 && gbad == 0) ? 0 : 1;
 }

@@ -25,3 +25,4 @@ def test_refmath_host_check(tmp_path):
     lines = dict(l.split(" ", 1) for l in r.stdout.strip().splitlines())
     assert "mismatches=0" in lines["isect"]
     assert "unflagged=0" in lines["sincos"]
+    assert "mismatches=0" in lines["gauss"]

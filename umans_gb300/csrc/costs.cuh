@@ -382,8 +382,7 @@ UD float cost_paris(const AgentCtx& A, const NbView& N, const CostDesc& c, float
 // costForTtcaDca: TtcaDca.cpp:40-43
 UD float ttcadca_pair_cost(float ttca, float dca, float sT, float sD)
 {
-	const double a = (double)(ttca / sT), b = (double)(dca / sD);
-	return (float)exp(-0.5 * __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)));
+	return exp_gauss(ttca / sT, dca / sD);
 }
 
 // TtcaDca::GetCost: TtcaDca.cpp:62-129
@@ -394,9 +393,8 @@ UD float cost_ttcadca(const AgentCtx& A, const NbView& N, const CostDesc& c, flo
 	const float rs = c.range * c.range;
 	const float alpha = vangle_exact(v, A.pref);
 	const float ds = vmag(v) - A.prefspeed;
-	const double qa = (double)(alpha / sA), qs = (double)(ds / sS);
-	const float Ca = (float)exp(-0.5 * __dmul_rn(qa, qa));
-	const float Cs = (float)exp(-0.5 * __dmul_rn(qs, qs));
+	const float Ca = exp_gauss(alpha / sA, 0.0f);
+	const float Cs = exp_gauss(ds / sS, 0.0f);
 	const float move = 1 - (Ca + Cs) / 2.0f;
 	float oc = 0, sc = 0;
 	for (int k = 0; k < N.K; ++k) {

@@ -780,12 +780,12 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 			fy[k] = f.y;
 		}
 	}
+	// neighbours beyond the cost's range hold +0.0 (see ordered_sums)
 	__syncwarp();
 	float acc = 0.0f;
 	if (lane < 2) {
 		const float* src = lane ? fy : fx;
-		for (int k = 0; k < N.K; ++k)
-			if (N.d2[k] <= rs) acc += src[k];
+		for (int k = 0; k < N.K; ++k) acc += src[k];
 	}
 	const float ax = __shfl_sync(0xffffffffu, acc, 0);
 	const float ay = __shfl_sync(0xffffffffu, acc, 1);
@@ -883,14 +883,36 @@ __device__ float2 orca_solve(const AgentCtx& A, const NbView& N, const CostDesc&
 // gradients (uniform across the warp)
 // ------------------------------------------------------------------------
 // TtcaDca::GetGradient: TtcaDca.cpp:131-262
-__device__ float2 grad_ttcadca(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v)
+// Sums of per-neighbour terms in neighbour order: lane j < nsum adds z_j[0..K)
+// sequentially (entries of neighbours that contribute nothing hold +0.0,
+// which leaves a sum that starts at +0.0 unchanged: x + (+0) = x for x != -0,
+// and such sums never reach -0.0).  Returns the sums in s[0..nsum).
+__device__ __forceinline__ void ordered_sums(const float* z0, const float* z1, const float* z2, int nsum, int K,
+                                             int lane, float* s)
+{
+	__syncwarp();
+	float acc = 0.0f;
+	if (lane < nsum) {
+		const float* src = lane == 0 ? z0 : (lane == 1 ? z1 : z2);
+		for (int k = 0; k < K; ++k) acc += src[k];
+	}
+	s[0] = __shfl_sync(0xffffffffu, acc, 0);
+	s[1] = __shfl_sync(0xffffffffu, acc, 1);
+	s[2] = __shfl_sync(0xffffffffu, acc, 2);
+	__syncwarp();
+}
+
+// TtcaDca::GetGradient (TtcaDca.cpp:130-223): the per-neighbour terms
+// lane-parallel into z0..z2, then the reference's three sums in order
+__device__ float2 grad_ttcadca(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v, int lane, float* z0,
+                               float* z1, float* z2)
 {
 	const float sA = c.p[0], sS = c.p[1], sT = c.p[2], sD = c.p[3];
 	const float viewHalf = (float)(REF_PI / 2.0);
 	const float eps = 0.001f;
 	const float rs = c.range * c.range;
-	float GradTh = 0, GradS = 0, total = 0;
-	for (int k = 0; k < N.K; ++k) {
+	for (int k = lane; k < N.K; k += 32) {
+		z0[k] = 0.0f; z1[k] = 0.0f; z2[k] = 0.0f;
 		if (N.d2[k] > rs) continue;
 		const float2 np = nb_pos(N, k);
 		const float nr = nb_radius(N, k);
@@ -926,10 +948,14 @@ __device__ float2 grad_ttcadca(const AgentCtx& A, const NbView& N, const CostDes
 		const float gCS = -cost * (gTS * tf + gDS * df);
 		const float gCA = -cost * (gTA * tf + gDA * df);
 		const float scale = 1 / vsq(dp);
-		total += scale;
-		GradTh += gCA * scale;
-		GradS += gCS * scale;
+		z0[k] = gCA * scale;
+		z1[k] = gCS * scale;
+		z2[k] = scale;
 	}
+	float sums[3];
+	ordered_sums(z0, z1, z2, 3, N.K, lane, sums);
+	float GradTh = sums[0], GradS = sums[1];
+	const float total = sums[2];
 	if (total > 0) { GradTh /= total; GradS /= total; }
 	// getMovementCostGradient: TtcaDca.cpp:54-60 (counterClockwiseAngle)
 	float alpha = vangle_exact(v, A.pref);
@@ -946,14 +972,15 @@ __device__ float2 grad_ttcadca(const AgentCtx& A, const NbView& N, const CostDes
 }
 
 // FOEAvoidance::GetGradient: FOEAvoidance.cpp:94-143
-__device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v)
+__device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v, int lane, float* z0,
+                           float* z1)
 {
 	if (viszero(v)) return V(0, 0);
 	const float2 Vn = vnorm(v);
 	const float rs = c.range * c.range;
 	const double LN10 = 2.302585092994045684;
-	float gt = 0, gv = 0;
-	for (int k = 0; k < N.K; ++k) {
+	for (int k = lane; k < N.K; k += 32) {
+		z0[k] = 0.0f; z1[k] = 0.0f;
 		if (N.d2[k] > rs) continue;
 		const float2 dv = vsub(nb_vel(N, k), v), dp = vsub(nb_pos(N, k), A.pos);
 		const float2 Vel = V(Vn.y * dv.x + -Vn.x * dv.y, Vn.x * dv.x + Vn.y * dv.y);
@@ -964,9 +991,13 @@ __device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c
 		const float sigma = (float)__ddiv_rn((double)((A.radius + nb_radius(N, k)) / Pos.y), LN10);
 		const float sg = (float)((0 < dx) - (dx < 0));
 		const float E = foe_importance(ttc) * ref_expf(A.ex, -fabsf(dx) / sigma);
-		gt += E * sg * (xf * xf - xg * xg - (vmag(v) / (-Vel.y))) / sigma;
-		gv += E * sg * (-xf / (-Vel.y)) / sigma;
+		z0[k] = E * sg * (xf * xf - xg * xg - (vmag(v) / (-Vel.y))) / sigma;
+		z1[k] = E * sg * (-xf / (-Vel.y)) / sigma;
 	}
+	float sums[3];
+	ordered_sums(z0, z1, z1, 2, N.K, lane, sums);
+	float gt = sums[0];
+	const float gv = sums[1];
 	if (gt < -0.1f) gt = -0.1f;
 	else if (gt > 0.1f) gt = 0.1f;
 	float sn, cs;
@@ -1419,8 +1450,9 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 						grad_draws += 2;
 						g = V(gx, gy);
 					} else if (c.kind == K_GENERIC) g = V(0, 0);   // FD of a zero cost
-					else if (c.kind == K_TTCADCA) g = grad_ttcadca(A, N, c, A.vel);
-					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel);
+					else if (c.kind == K_TTCADCA)
+						g = grad_ttcadca(A, N, c, A.vel, lane, fx, fy, reinterpret_cast<float*>(proj));
+					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel, lane, fx, fy);
 					else {
 						// CostFunction::GetGradient default: costFunction.cpp:36-54;
 						// lanes 0..3 evaluate the four probes

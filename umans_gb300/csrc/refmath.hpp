@@ -278,6 +278,40 @@ RM_HD float ff_expf_core(float x, bool* near = nullptr)
 	return f * rm_float((uint32_t)(kq + 127) << 23);
 }
 
+// e^(xh + xl) for xh in [FF_EXP_LO, 0] and |xl| <= ulp(xh): the same
+// reduction and series as ff_expf_core with the low part of the argument
+// added to the reduced argument; returns the unrounded value hi + lo in
+// [2^-1, 2^1] and the exact scale 2^kq (the result is (hi + lo) * scale).
+RM_HD void ff_exp_ff(float xh, float xl, float* hi, float* lo, float* scale)
+{
+	const float INV = 92.33248138427734f;      // 64 / ln 2
+	const float L1 = 0x1.62cp-7f;              // ln2/64 = L1 + L2 + L3, L1 with 11 bits
+	const float L2 = 0x1.217f7ep-18f;
+	const float L3 = -0x1.c610cap-43f;
+	const float kf = rintf(xh * INV);
+	const int k = (int)kf;
+	const float t1 = xh - kf * L1;             // kf*L1 exact; difference exact (Sterbenz)
+	const FF q = ff_two_prod(kf, L2);
+	const FF r0 = ff_two_sum(t1, -q.h);
+	const float rl0 = ((r0.l - q.l) - kf * L3) + xl;
+	const FF r = ff_two_sum(r0.h, rl0);
+	const float h = r.h, l = r.l;
+	const FF h2 = ff_two_prod(h, h);
+	float tail = (1.0f / 6.0f) + h * ((1.0f / 24.0f) + h * ((1.0f / 120.0f) + h * (1.0f / 720.0f)));
+	tail = tail * (h * h * h) + (h * h * l) * 0.5f;
+	const FF a = ff_two_sum(h, h2.h * 0.5f);
+	const float lo0 = a.l + (l + (h2.l * 0.5f + (h * l + tail)));
+	const FF s = ff_fast_two_sum(1.0f, a.h);
+	const float sl = s.l + lo0;
+	const int j = k & 63;
+	const int kq = (k - j) / 64;               // floor(k / 64)
+	const float Th = ff_exp2_tab(j, 0), Tl = ff_exp2_tab(j, 1);
+	const FF m = ff_two_prod(Th, s.h);
+	*hi = m.h;
+	*lo = m.l + (Th * sl + Tl * s.h);
+	*scale = rm_float((uint32_t)(kq + 127) << 23);   // kq in [-126, 0]
+}
+
 // open-addressing table of (argument bits, host expf bits); key 0 = empty
 struct ExpExceptions {
 	const uint2* slots;
@@ -691,6 +725,30 @@ RM_HD int line_intersection_ff(float ax, float ay, float bx, float by, float cx,
 	*rx = X.h;
 	*ry = Y.h;
 	return 1;
+}
+
+// ---------------------------------------------------------------------------
+// (float)exp(-0.5 * ((double)a * a + (double)b * b)): the Gaussians of TtcaDca
+// (TtcaDca.cpp:40-43 and :54-60), evaluated in double by the reference.  The
+// squares are exact in float-float, their sum within 2^-47, so the argument
+// is within 2^-46 |x| of the double one; the float-float exponential
+// (ff_exp_ff) is then rounded to float when every value within the combined
+// bound rounds the same way, else the double expression is evaluated.
+RM_HD float exp_gauss(float a, float b)
+{
+	const FF q = ff_add2(ff_two_prod(a, a), ff_two_prod(b, b));
+	const float xh = -0.5f * q.h, xl = -0.5f * q.l;
+	if (xh < -104.5f) return 0.0f;    // below 2^-150.7: the float rounding is 0
+	if (xh >= FF_EXP_LO && xh <= 0.0f) {
+		float hi, lo, sc;
+		ff_exp_ff(xh, xl, &hi, &lo, &sc);
+		const float f = hi + lo;
+		const FF v = FF{ f, lo - (f - hi) };
+		const float bound = (0x1p-45f * fabsf(xh) + 0x1p-41f) * f;
+		if (ff_rounds_to_h(v, bound)) return f * sc;
+	}
+	const double ad = (double)a, bd = (double)b;
+	return (float)exp(-0.5 * (ad * ad + bd * bd));
 }
 
 }  // namespace umans
