@@ -218,6 +218,7 @@ def read_scenario(path: str) -> dict:
         raise ValueError("no policies")
 
     ids, pos, goal, rad, pref, maxs, maxa, pidx = [], [], [], [], [], [], [], []
+    start, rmg = [], []
     taken = set()
     next_id = 0
     ablock = sim.find("Agents")
@@ -247,6 +248,11 @@ def read_scenario(path: str) -> dict:
             g = (_f32(ge.get("x")), _f32(ge.get("y"))) if ge is not None else p
             ids.append(aid); pos.append(p); goal.append(g); rad.append(r); pref.append(ps)
             maxs.append(ms); maxa.append(ma); pidx.append(policy_ids.index(_int(pol.get("id"))))
+            # crowdSimulator.cpp:436, 470-475 (QueryBoolAttribute / QueryFloatAttribute)
+            st = _f32(ae.get("start_time")) if ae.get("start_time") is not None else 0.0
+            rg = _bool(ae.get("remove_at_goal")) if ae.get("remove_at_goal") is not None else False
+            start.append(st)
+            rmg.append(bool(rg))
     # obstacles (crowdSimulator.cpp:496-514, 633-645): every polygon's
     # closed outline, polygons in file order (Polygon2D.cpp:27-35)
     edges = []
@@ -264,7 +270,8 @@ def read_scenario(path: str) -> dict:
                 policies=policies, ids=np.array(ids, np.int64),
                 pos=np.array(pos, f).reshape(-1, 2), goal=np.array(goal, f).reshape(-1, 2),
                 radius=np.array(rad, f), pref_speed=np.array(pref, f), max_speed=np.array(maxs, f),
-                max_accel=np.array(maxa, f), policy_index=np.array(pidx, np.int32))
+                max_accel=np.array(maxa, f), policy_index=np.array(pidx, np.int32),
+                start_time=np.array(start, f), remove_at_goal=np.array(rmg, np.uint8))
 
 
 _lib = None
@@ -299,6 +306,7 @@ def _load():
         lib.up_neighbors.argtypes = [P, C.c_int, P, P, P, P, C.c_int]
         lib.up_libm_expf.argtypes = [P, P, C.c_long]
         lib.up_libm_sincosf.argtypes = [P, P, P, C.c_long]
+        lib.up_set_dynamics.argtypes = [P, P, P]
         lib.up_set_obstacles.argtypes = [P, C.c_int, P]
         _lib = lib
     return _lib
@@ -337,6 +345,11 @@ class PortSim:
                       ("ids", "pos", "goal", "radius", "pref_speed", "max_speed", "max_accel", "policy_index")]
         self._h = lib.up_create(len(s["ids"]), s["world"], s["width"], s["height"], s["dt"],
                                 C.cast(pols, C.c_void_p), len(s["policies"]), *(_p(a) for a in self._keep))
+        st = np.ascontiguousarray(s.get("start_time", np.zeros(0, np.float32)), np.float32)
+        rg = np.ascontiguousarray(s.get("remove_at_goal", np.zeros(0, np.uint8)), np.uint8)
+        if (st.size and (st > 0).any()) or (rg.size and rg.any()):
+            self._keep += [st, rg]
+            lib.up_set_dynamics(self._h, _p(st), _p(rg))
         edges = np.ascontiguousarray(s.get("edges", np.zeros((0, 4), np.float32)), np.float32)
         if edges.shape[0]:
             self._keep.append(edges)

@@ -138,6 +138,22 @@ struct up_world {
 	/* grid */
 	int *cell_start, *cell_items, gnx, gny, gcells_cap;
 	float gx0, gy0, gcs;
+	/* dynamic population (worldBase.cpp:79-86, 124-127, 161-235): the arrays
+	 * above hold the current agent list in its order, with room for every
+	 * agent; agents with a start time wait in `pend` (file order, stably
+	 * sorted by start time) */
+	unsigned char* rmg;      /* remove at goal, per list slot (or NULL) */
+	int cap;
+	struct up_pending* pend;
+	int npend, next_pend;
+};
+
+struct up_pending {
+	long long id;
+	v2 pos, goal;
+	float radius, prefspeed, maxspeed, maxacc, start;
+	int policy;
+	unsigned char rmg;
 };
 
 /* ------------------------------------------------------------------ */
@@ -1182,8 +1198,54 @@ static void make_ctx(up_world* w, int i, actx* A)
 	A->maxacc = w->maxacc[i]; A->dt = w->dt; A->relax = w->pol[w->policy[i]].relax_time;
 }
 
+/* the slot state of a new agent (Agent constructor, setPosition, setGoal:
+ * agent.cpp:29-47, 108-115) */
+static void init_slot(up_world* w, int i, long long id, v2 pos, v2 goal, float radius, float prefspeed,
+                      float maxspeed, float maxacc, int policy)
+{
+	w->id[i] = id;
+	w->pos[i] = pos;
+	w->goal[i] = goal;
+	w->radius[i] = radius; w->prefspeed[i] = prefspeed;
+	w->maxspeed[i] = maxspeed; w->maxacc[i] = maxacc;
+	w->policy[i] = policy;
+	w->rng[i] = minstd_seed((uint64_t)(unsigned int)id);
+	w->vel[i] = w->vwf[i] = w->pref[i] = w->next[i] = w->contact[i] = V(0, 0);
+	w->view[i] = V(0, 0);
+	if (goal.x != pos.x || goal.y != pos.y) w->view[i] = vnorm(vsub(goal, pos));
+	w->nb[i].n = 0;
+	w->ob[i].n = 0;
+}
+
+/* WorldBase::removeAgentAtListIndex: worldBase.cpp:207-235 (the last agent
+ * moves into the freed slot); the slots' list buffers are swapped */
+static void remove_slot(up_world* w, int i)
+{
+	const int last = w->n - 1;
+	if (i != last) {
+		w->id[i] = w->id[last];
+		v2* vs[] = { w->pos, w->vel, w->goal, w->pref, w->next, w->vwf, w->view, w->contact };
+		for (int k = 0; k < 8; ++k) vs[k][i] = vs[k][last];
+		float* fs[] = { w->radius, w->prefspeed, w->maxspeed, w->maxacc };
+		for (int k = 0; k < 4; ++k) fs[k][i] = fs[k][last];
+		w->policy[i] = w->policy[last];
+		w->rng[i] = w->rng[last];
+		if (w->rmg) w->rmg[i] = w->rmg[last];
+		nbrlist t = w->nb[i]; w->nb[i] = w->nb[last]; w->nb[last] = t;
+		seglist u = w->ob[i]; w->ob[i] = w->ob[last]; w->ob[last] = u;
+	}
+	w->n = last;
+}
+
 static void do_step(up_world* w)
 {   /* WorldBase::DoStep: worldBase.cpp:79-128 */
+	/* agents whose start time has come join the end of the list */
+	while (w->next_pend < w->npend && (double)w->pend[w->next_pend].start <= w->time) {
+		const struct up_pending* a = &w->pend[w->next_pend++];
+		const int i = w->n++;
+		init_slot(w, i, a->id, a->pos, a->goal, a->radius, a->prefspeed, a->maxspeed, a->maxacc, a->policy);
+		if (w->rmg) w->rmg[i] = a->rmg;
+	}
 	const int n = w->n;
 	grid_build(w);
 #pragma omp parallel for schedule(dynamic, 64)
@@ -1225,6 +1287,10 @@ static void do_step(up_world* w)
 		}
 	}
 	w->time += w->dt;
+	/* agents at their goal that are to be removed there, from the back */
+	if (w->rmg)
+		for (int i = n - 1; i >= 0; --i)
+			if (w->rmg[i] && vsq(vsub(w->goal[i], w->pos[i])) <= w->radius[i] * w->radius[i]) remove_slot(w, i);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1269,7 +1335,9 @@ up_world* up_create(int n, int world_type, float width, float height, float dt,
 void up_free(up_world* w)
 {
 	if (!w) return;
-	for (int i = 0; i < w->n; ++i) { free(w->nb[i].v); free(w->ob[i].v); }
+	const int slots = w->cap > w->n ? w->cap : w->n;
+	for (int i = 0; i < slots; ++i) { free(w->nb[i].v); free(w->ob[i].v); }
+	free(w->rmg); free(w->pend);
 	free(w->nb); free(w->ob); free(w->edges); free(w->pol); free(w->id);
 	free(w->pos); free(w->vel); free(w->goal); free(w->pref); free(w->next); free(w->vwf);
 	free(w->view); free(w->contact); free(w->radius); free(w->prefspeed); free(w->maxspeed);
@@ -1285,6 +1353,38 @@ void up_set_obstacles(up_world* w, int ne, const float* edges)
 	for (int k = 0; k < ne; ++k) {
 		w->edges[k].a = V(edges[4 * k], edges[4 * k + 1]);
 		w->edges[k].b = V(edges[4 * k + 2], edges[4 * k + 3]);
+	}
+}
+
+void up_set_dynamics(up_world* w, const float* start_time, const unsigned char* remove_at_goal)
+{   /* WorldBase::AddAgent (worldBase.cpp:161-188) at time 0: an agent with a
+	 * start time > 0 waits in the insertion queue, the others form the list */
+	w->cap = w->n;
+	w->rmg = (unsigned char*)calloc((size_t)(w->n > 0 ? w->n : 1), 1);
+	w->pend = (struct up_pending*)malloc(sizeof(struct up_pending) * (size_t)(w->n > 0 ? w->n : 1));
+	w->npend = w->next_pend = 0;
+	int m = 0;
+	for (int i = 0; i < w->n; ++i) {
+		const float st = start_time ? start_time[i] : 0.0f;
+		const unsigned char rg = remove_at_goal ? remove_at_goal[i] : 0;
+		if ((double)st <= w->time) {
+			init_slot(w, m, w->id[i], w->pos[i], w->goal[i], w->radius[i], w->prefspeed[i], w->maxspeed[i],
+			          w->maxacc[i], w->policy[i]);
+			w->rmg[m++] = rg;
+		} else {
+			struct up_pending* a = &w->pend[w->npend++];
+			a->id = w->id[i]; a->pos = w->pos[i]; a->goal = w->goal[i];
+			a->radius = w->radius[i]; a->prefspeed = w->prefspeed[i]; a->maxspeed = w->maxspeed[i];
+			a->maxacc = w->maxacc[i]; a->policy = w->policy[i]; a->start = st; a->rmg = rg;
+		}
+	}
+	w->n = m;
+	/* stable insertion sort by start time (equal times keep file order) */
+	for (int i = 1; i < w->npend; ++i) {
+		struct up_pending a = w->pend[i];
+		int j = i - 1;
+		while (j >= 0 && w->pend[j].start > a.start) { w->pend[j + 1] = w->pend[j]; --j; }
+		w->pend[j + 1] = a;
 	}
 }
 

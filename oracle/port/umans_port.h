@@ -72,6 +72,9 @@ up_world* up_create(int n, int world_type, float width, float height, float dt,
 void up_free(up_world* w);
 /* static obstacle edges (ax, ay, bx, by), in file order */
 void up_set_obstacles(up_world* w, int ne, const float* edges);
+/* timed insertion and remove-at-goal (per agent, in creation order; either
+ * may be NULL); call once, right after up_create */
+void up_set_dynamics(up_world* w, const float* start_time, const unsigned char* remove_at_goal);
 int up_num_agents(const up_world* w);
 double up_time(const up_world* w);
 /* runs n steps with `threads` OpenMP threads; returns wall seconds */

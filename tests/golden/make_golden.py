@@ -6,9 +6,12 @@ Each fixture is an .npz holding the scenario XML (utf-8 bytes), the agent
 ids, and the reference's float32 positions and velocities after the listed
 steps; some also hold the reference's neighbour lists (ids and
 PhantomAgent::distSqr in the reference's order) for the lists used in given
-steps.  Run from the repository root:
+steps.  The arrivals40_* fixtures (timed insertion and remove-at-goal) hold
+per snapshot the ids in the reference's list order and their positions.
+Run from the repository root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py arrivals   # the arrivals40_* ones
 
 It needs oracle/_ref/libumans_ref.so, i.e. the reference sources.
 """
@@ -66,9 +69,37 @@ def run(name, scen, steps, every=1, nb_steps=(), nb_agents=None):
     print(f"{name}: n={len(ids)} steps={steps} snapshots={len(snaps)}")
 
 
-def main():
+def run_dynamic(name, scen, steps, every=1):
+    """Like run() for a changing population: each snapshot holds the ids in
+    the reference's list order and their positions (ragged: snap_off)."""
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, name + ".xml")
+        scen.write(path)
+        xml = open(path, "rb").read()
+        sim = ref.RefSim(path, threads=4)
+        snaps, ids, pos, off = [], [], [], [0]
+        for s in range(1, steps + 1):
+            sim.step(1)
+            if s % every == 0 or s == 1:
+                st = sim.state()
+                snaps.append(s)
+                ids.append(st["ids"].astype(np.int32))
+                pos.append(st["pos"].astype(np.float32))
+                off.append(off[-1] + len(st["ids"]))
+        sim.close()
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), xml=np.frombuffer(xml, np.uint8), dyn=np.int32(1),
+                        steps=np.array(snaps, np.int32), snap_off=np.array(off, np.int64),
+                        snap_ids=np.concatenate(ids), snap_pos=np.concatenate(pos).reshape(-1, 2))
+    print(f"{name}: steps={steps} snapshots={len(snaps)} agents per snapshot {[len(i) for i in ids][:8]}...")
+
+
+def main(only=None):
     if not ref.available():
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    if only == "arrivals":
+        for m in S.MODEL_POLICIES:
+            run_dynamic(f"arrivals40_{m}", S.model_arrivals(m), 100, every=5)
+        return
     for m in S.MODEL_POLICIES:
         run(f"circle24_{m}", S.model_circle(m), 100, every=5)
         run(f"crossing40_{m}", S.model_crossing(m), 100, every=5)
@@ -87,6 +118,8 @@ def main():
     for k, n in ((0, 40), (1, 90), (2, 150), (3, 64), (4, 120), (5, 33)):
         run(f"batch{k}_n{n}", S.batch_member(k, n), 60, every=5)
     run("calibration512", S.calibration_set(), 100, every=10)
+    for m in S.MODEL_POLICIES:
+        run_dynamic(f"arrivals40_{m}", S.model_arrivals(m), 100, every=5)
     with open(os.path.join(OUT, "PROVENANCE.txt"), "w") as fh:
         cc = subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0]
         fh.write("Golden fixtures: UMANS reference engine compiled from its own sources by\n"
@@ -96,4 +129,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import golden_names, neighbour_lists
+from conftest import assert_same_population, dynamic_golden_names, dynamic_snapshots, golden_names, neighbour_lists
 from oracle.port import PortSim
 from test_oracle_golden import assert_same_list
 from umans_gb300 import Simulation, scenarios as S
@@ -49,6 +49,20 @@ def test_trajectory_matches_reference(name, golden_xml):
           f"over {min(done, 100)} steps = {worst_all:.3g} m")
     assert worst <= TOL, f"{name}: max deviation {worst} m"
     assert worst_all == 0.0, f"{name}: not bit-identical ({worst_all} m)"
+
+
+@pytest.mark.parametrize("name", dynamic_golden_names())
+def test_dynamic_population_matches_reference(name, golden_xml):
+    """Timed insertion and remove-at-goal (worldBase.cpp:79-86, 124-127): the
+    same agents at bit-identical positions at every snapshot."""
+    path, g = golden_xml(name)
+    sim = Simulation(path)
+    done = 0
+    for s, ids, pos in dynamic_snapshots(g):
+        sim.step(s - done)
+        done = s
+        st = sim.state()
+        assert_same_population(st["ids"], st["pos"], ids, pos, f"{name} step {s}")
 
 
 @pytest.mark.parametrize("name", [n for n in golden_names() if n.startswith(("toric60", "orca_circle50",

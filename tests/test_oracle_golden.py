@@ -8,7 +8,7 @@ port is in fact bit-identical on the machine that made the fixtures.
 import numpy as np
 import pytest
 
-from conftest import golden_names, neighbour_lists
+from conftest import assert_same_population, dynamic_golden_names, dynamic_snapshots, golden_names, neighbour_lists
 from oracle.port import PortSim
 
 TOL = 1e-4   # m, max per-agent position deviation over the first 100 steps
@@ -30,6 +30,20 @@ def test_port_trajectory_matches_reference(name, golden_xml):
         if s <= 100:
             worst = max(worst, dev)
     assert worst <= TOL, f"{name}: max deviation {worst} m"
+
+
+@pytest.mark.parametrize("name", dynamic_golden_names())
+def test_port_dynamic_population_matches_reference(name, golden_xml):
+    """Timed insertion and remove-at-goal: the same agents at the same
+    positions at every snapshot."""
+    path, g = golden_xml(name)
+    sim = PortSim(path, threads=2)
+    done = 0
+    for s, ids, pos in dynamic_snapshots(g):
+        sim.step(s - done)
+        done = s
+        st = sim.state()
+        assert_same_population(st["ids"].astype(np.int32), st["pos"], ids, pos, f"{name} step {s}")
 
 
 @pytest.mark.parametrize("name", [n for n in golden_names() if n.startswith(("toric60", "orca_circle50",

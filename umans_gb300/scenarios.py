@@ -83,6 +83,8 @@ class Scenario:
     max_speed: np.ndarray = None    # (n,) float32
     policy_id: np.ndarray = None    # (n,) int
     obstacles: list = field(default_factory=list)   # polygons: (k, 2) vertex arrays
+    start_time: np.ndarray = None   # (n,) float32 or None: timed insertion (s)
+    remove_at_goal: np.ndarray = None   # (n,) bool or None
 
     @property
     def n(self) -> int:
@@ -101,9 +103,14 @@ class Scenario:
                f'<Simulation delta_time="{_f(self.dt)}"{end}>', w,
                "<Policies>", *self.policies, "</Policies>", "<Agents>"]
         for i in range(self.n):
+            extra = ""
+            if self.start_time is not None and self.start_time[i] != 0:
+                extra += f' start_time="{_f(self.start_time[i])}"'
+            if self.remove_at_goal is not None and self.remove_at_goal[i]:
+                extra += ' remove_at_goal="true"'
             out.append(
                 f'<Agent rad="{_f(self.radius[i])}" pref_speed="{_f(self.pref_speed[i])}" '
-                f'max_speed="{_f(self.max_speed[i])}">'
+                f'max_speed="{_f(self.max_speed[i])}"{extra}>'
                 f'<pos x="{_f(self.pos[i, 0])}" y="{_f(self.pos[i, 1])}"/>'
                 f'<goal x="{_f(self.goal[i, 0])}" y="{_f(self.goal[i, 1])}"/>'
                 f'<Policy id="{int(self.policy_id[i])}"/></Agent>')
@@ -296,6 +303,26 @@ def model_crossing(model: str, n: int = 40, seed: int = 11) -> Scenario:
     goal = np.concatenate([a + [20, 0], b + [0, 20]])
     return Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
                     **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+
+
+def model_arrivals(model: str, n: int = 40, seed: int = 17) -> Scenario:
+    """Two crossing groups whose agents enter at staggered times (some at the
+    same time) and leave at their goals (most of them): the dynamic
+    population of WorldBase::DoStep (timed insertion, remove-at-goal)."""
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    a = np.stack([rng.uniform(-9, -5, h), rng.uniform(-2.5, 2.5, h)], 1)
+    b = np.stack([rng.uniform(-2.5, 2.5, n - h), rng.uniform(-9, -5, n - h)], 1)
+    pos = np.concatenate([a, b])
+    goal = np.concatenate([a + [11, 0], b + [0, 11]])
+    sc = Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
+                  **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+    start = np.round(rng.uniform(0.0, 4.0, n), 1).astype(np.float32)
+    start[rng.random(n) < 0.3] = 0.0
+    start[[1, 2, 3]] = start[0] = np.float32(1.5)      # a tie in the insertion queue
+    sc.start_time = start
+    sc.remove_at_goal = rng.random(n) < 0.8
+    return sc
 
 
 # Policies with the RandomFunction and Generic cost functions (the per-agent
