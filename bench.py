@@ -52,6 +52,9 @@ GRID_BYTES_PER_AGENT = 128
 # plus ~40 per agent (goal force, clamps, integration)
 SF_FLOP_PER_PAIR = 67
 SF_FLOP_PER_AGENT = 40
+# FP32 operations of one pair collision time (costFunction.cpp:173-227: the
+# quadratic with one sqrt and two divisions, the range and zero tests)
+KARAMOUZAS_FLOP_PER_TTC = 30
 
 
 def workload(name: str, tmp: str, agents: int = 0):
@@ -273,11 +276,33 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
     sim.synchronize()
     torch.cuda.synchronize()
     t_ms = sum(a.elapsed_time(b) for a, b in evs)
+    work = None
+    if name == "karamouzas_corridor":
+        # samples inside the Karamouzas window and pair collision times, counted
+        # in the kernel over two profiled steps (FLOPs as counted from the
+        # reference source: ~30 per pair collision time, the preferred-velocity
+        # sweep once per agent plus one sweep per window sample)
+        sim.profile(True)
+        sim.step(2)
+        pr = sim.profile_totals()
+        cn = sim.profile_counters()
+        sim.profile(False)
+        agents = max(cn["karamouzas_agents"], 1)
+        s_eval = cn["karamouzas_window_samples"] / agents
+        kbar = cn["karamouzas_pair_ttc"] / max(cn["karamouzas_window_samples"], 1)
+        flop = KARAMOUZAS_FLOP_PER_TTC * kbar * (1.0 + s_eval)
+        kms = pr["agent_kernel_ms"] / max(pr["steps"], 1)
+        fp32_peak = 152 * 128 * 2 * 2070.0 * 1e6 / 1e12
+        work = dict(window_samples_per_agent=s_eval, pairs_per_sample=kbar, flop_per_agent_step=flop,
+                    k_agent_ms=kms, achieved_tflops=flop * n / (kms * 1e-3) / 1e12,
+                    peak_tflops_nominal=fp32_peak, frac=flop * n / (kms * 1e-3) / 1e12 / fp32_peak)
     sim.close()
     out = dict(config=dict(cfg, timed_steps=f"steps {warmup + 1}..{warmup + steps}",
                            l2="flushed (256 MiB write) before every timed step"),
                value=n * steps / (t_ms / 1e3), unit="agent-steps/s", steps=steps, warmup=warmup,
                ms_per_step=t_ms / steps)
+    if work:
+        out["fp32_roofline"] = work
     if cpu_agents >= 0:
         cpath, cn = path, n
         if cpu_agents:

@@ -139,6 +139,11 @@ int umans_device_state(umans_sim* sim, void** pos, void** vel);
 int umans_profile(umans_sim* sim, int enable);
 int umans_profile_totals(umans_sim* sim, double* agent_kernel_ms, double* step_ms, int* steps,
                          int* kernels_per_step, double* grid_build_ms);
+/* Work counters of the profiled steps (since umans_profile(sim, 1)), first n
+ * of: Karamouzas samples inside the deviation/speed window (the samples whose
+ * collision times are swept, Karamouzas.cpp:39-44), pair collision times
+ * evaluated for them, agents through that sampling path. */
+int umans_profile_counters(umans_sim* sim, unsigned long long* counts, int n);
 /* Differentiable form (no counterpart in the reference), for calibrating
  * force-model parameters against observed trajectories.  Supported policies:
  * method "gradient" with SocialForcesAvoidance, PowerLaw and

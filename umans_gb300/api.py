@@ -127,6 +127,12 @@ class Simulation:
         return dict(agent_kernel_ms=a.value, step_ms=b.value, steps=n.value, kernels_per_step=k.value,
                     grid_build_ms=g.value)
 
+    def profile_counters(self) -> dict:
+        c = np.zeros(3, np.uint64)
+        self._check(self._lib.umans_profile_counters(self._h, _p(c), 3))
+        return dict(karamouzas_window_samples=int(c[0]), karamouzas_pair_ttc=int(c[1]),
+                    karamouzas_agents=int(c[2]))
+
     # --- state ----------------------------------------------------------
     def state(self) -> dict:
         n = self.n

@@ -258,6 +258,13 @@ int umans_profile(umans_sim* s, int enable)
 	return UMANS_OK;
 }
 
+int umans_profile_counters(umans_sim* s, unsigned long long* counts, int n)
+{
+	if (!s || (n > 0 && !counts)) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->profile_counters(counts, n)) return fail(s, UMANS_ERR_DEVICE, s->eng->error());
+	return UMANS_OK;
+}
+
 int umans_profile_totals(umans_sim* s, double* agent_kernel_ms, double* step_ms, int* steps, int* kernels_per_step,
                          double* grid_build_ms)
 {

@@ -56,6 +56,9 @@ struct DevState {
 	int *cell, *cnt, *start, *fill, *blocksum;
 	GridParams* grid;       // [nscen]
 	unsigned* bbox;         // [4 * nscen]
+	// profiling only (else null): Karamouzas samples inside the window, pairs
+	// swept per window sample, agents through that path
+	unsigned long long* counters;
 	int* status;
 	const PolicyDesc* pols;
 	const SampleEntry* table;
@@ -1105,6 +1108,7 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			}
 			__syncwarp();
 		}
+		unsigned long long n_in = 0;
 		for (int i0 = 0; i0 < pol.nsamples; i0 += 32) {
 			const int i = i0 + lane;
 			float2 v = V(0, 0);
@@ -1121,6 +1125,7 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 			// KS samples inside the window at a time: their sweeps share the
 			// pair loads and run as independent chains
 			unsigned m = __ballot_sync(0xffffffffu, in);
+			n_in += __popc(m);
 			while (m) {
 				int si[KS];
 				float2 sv[KS];
@@ -1169,6 +1174,11 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 					if (tc < bestC) { bestC = tc; bestI = i0 + si[j]; }
 				}
 			}
+		}
+		if (S.counters && lane == 0) {
+			atomicAdd(&S.counters[0], n_in);
+			atomicAdd(&S.counters[1], n_in * (unsigned long long)KP);
+			atomicAdd(&S.counters[2], 1ull);
 		}
 		// samples outside the window all cost `outside`; like every sample
 		// they count only below the initial best (MAXF), and then the first
@@ -2316,6 +2326,7 @@ void Engine::enqueue_step()
 	S.maxnb = maxnb_;
 	const int wpb = opt_.warps_per_block;
 	const size_t smem = (size_t)wpb * maxnb_ * 16;
+	S.counters = profile_ ? counters_ : nullptr;
 	enqueue_grid(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
 	// the agents of each kernel group form one range of the cell-sorted
@@ -2374,6 +2385,27 @@ void Engine::enqueue_grid(const DevState& S)
 	k_scan_top<<<1, 1024, 0, stream_>>>(S);
 	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
+}
+
+void Engine::set_profile(bool on)
+{
+	profile_ = on;
+	prof_agent_ms_ = prof_step_ms_ = prof_grid_ms_ = 0;
+	prof_steps_ = 0;
+	if (on) {
+		if (!counters_ && cudaMalloc(&counters_, 3 * sizeof(unsigned long long)) != cudaSuccess) counters_ = nullptr;
+		if (counters_) cudaMemsetAsync(counters_, 0, 3 * sizeof(unsigned long long), stream_);
+	}
+}
+
+bool Engine::profile_counters(unsigned long long* out, int n)
+{
+	for (int k = 0; k < n; ++k) out[k] = 0;
+	if (!counters_) return true;
+	unsigned long long c[3];
+	CK(cudaMemcpy(c, counters_, sizeof(c), cudaMemcpyDeviceToHost));
+	for (int k = 0; k < n && k < 3; ++k) out[k] = c[k];
+	return true;
 }
 
 int Engine::kernels_per_step() const { return (small_world() ? 1 : 7) + (int)groups_.size(); }

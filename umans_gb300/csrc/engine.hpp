@@ -90,7 +90,9 @@ public:
 	// Profiling mode: every step is launched without the graph, with CUDA
 	// events on the engine's stream around the step and around k_agent;
 	// the elapsed times accumulate until reset.
-	void set_profile(bool on) { profile_ = on; prof_agent_ms_ = prof_step_ms_ = prof_grid_ms_ = 0; prof_steps_ = 0; }
+	void set_profile(bool on);
+	// counters of the last profiled steps (see DevState::counters)
+	bool profile_counters(unsigned long long* out, int n);
 	void profile_totals(double* agent_ms, double* step_ms, int* steps, double* grid_ms) const
 	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; *grid_ms = prof_grid_ms_; }
 	int kernels_per_step() const;
@@ -180,6 +182,7 @@ private:
 	cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
 	cudaEvent_t pa0_ = nullptr, pa1_ = nullptr, ps0_ = nullptr, ps1_ = nullptr;
 	bool profile_ = false;
+	unsigned long long* counters_ = nullptr;   // [3], device
 	// batch snapshot for re-running a batch after a capacity overflow
 	float2 *snap_pos_ = nullptr, *snap_vel_ = nullptr, *snap_view_ = nullptr, *snap_vwf_ = nullptr;
 	uint32_t* snap_rng_ = nullptr;
