@@ -261,8 +261,11 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
     from umans_gb300 import Simulation
     sub = os.path.join(tmp, name)
     os.makedirs(sub, exist_ok=True)
+    t0 = time.perf_counter()
     path, n, cfg = workload(name, sub)
+    t_write = time.perf_counter() - t0
     sim = Simulation(path)
+    t_load = time.perf_counter() - t0 - t_write
     stream = torch.cuda.ExternalStream(sim.stream)
     sim.step(warmup)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -303,6 +306,7 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
                ms_per_step=t_ms / steps)
     if work:
         out["fp32_roofline"] = work
+    t_gpu = time.perf_counter() - t0 - t_write - t_load
     if cpu_agents >= 0:
         cpath, cn = path, n
         if cpu_agents:
@@ -313,6 +317,8 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
         if cpu_agents:
             cb["sample"] = cb["sample"].replace("full", "same-density") + f" (the GPU case has {n} agents)"
         out["cpu_baseline"] = cb
+    out["leg_seconds"] = dict(write_scenario=round(t_write, 1), load=round(t_load, 1), gpu=round(t_gpu, 1),
+                              cpu=round(time.perf_counter() - t0 - t_write - t_load - t_gpu, 1))
     return out
 
 
