@@ -12,6 +12,7 @@ Run from the repository root:
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py arrivals   # the arrivals40_* ones
+    python tests/golden/make_golden.py blocks     # the (toric_)blocks60_* ones
 
 It needs oracle/_ref/libumans_ref.so, i.e. the reference sources.
 """
@@ -93,12 +94,26 @@ def run_dynamic(name, scen, steps, every=1):
     print(f"{name}: steps={steps} snapshots={len(snaps)} agents per snapshot {[len(i) for i in ids][:8]}...")
 
 
+BLOCK_MODELS = ("SocialForces", "Karamouzas", "RVO", "Moussaid", "VanToll", "PLEdestrians", "PowerLaw")
+
+
+def blocks():
+    """Scenarios with hundreds of obstacle edges (the engine's edge grid)."""
+    for m in BLOCK_MODELS:
+        run(f"blocks60_{m}", S.model_block_field(m), 100, every=5)
+    for m in ("SocialForces", "Karamouzas", "RVO"):
+        run(f"toric_blocks60_{m}", S.model_toric_block_field(m), 100, every=5)
+
+
 def main(only=None):
     if not ref.available():
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
     if only == "arrivals":
         for m in S.MODEL_POLICIES:
             run_dynamic(f"arrivals40_{m}", S.model_arrivals(m), 100, every=5)
+        return
+    if only == "blocks":
+        blocks()
         return
     for m in S.MODEL_POLICIES:
         run(f"circle24_{m}", S.model_circle(m), 100, every=5)
@@ -120,6 +135,7 @@ def main(only=None):
     run("calibration512", S.calibration_set(), 100, every=10)
     for m in S.MODEL_POLICIES:
         run_dynamic(f"arrivals40_{m}", S.model_arrivals(m), 100, every=5)
+    blocks()
     with open(os.path.join(OUT, "PROVENANCE.txt"), "w") as fh:
         cc = subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0]
         fh.write("Golden fixtures: UMANS reference engine compiled from its own sources by\n"

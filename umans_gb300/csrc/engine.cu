@@ -67,6 +67,9 @@ struct DevState {
 	int maxnb, total_warps, max_cells;   // max_cells: capacity of the cell arrays (all scenarios)
 	int t_begin, t_end;   // cell-sorted agents this k_agent launch updates
 	const float4* edges;  // obstacle edges of all scenarios (ScenDesc::edge_off)
+	const int* og_start;  // edge grids (ScenDesc::og_*): cell starts,
+	const int2* og_items; // items (global edge index, cell x),
+	const int4* og_ecell; // per global edge its cell range (x0, y0, x1, y1)
 	uint32_t* obs_list;   // per warp: max_obs entries of the agent's obstacle list
 	int max_obs;
 	const int* scen_order;   // [nscen]: scenarios in cell-space order (grouped by kernel)
@@ -723,17 +726,71 @@ __device__ int gather_obstacles(const DevState& S, const ScenDesc& sd, float2 p,
 			if (!active) continue;
 		}
 		const float2 q = vadd(p, disp);
-		for (int b0 = 0; b0 < sd.nedges; b0 += 32) {
-			const int k = b0 + lane;
-			bool ok = false;
-			if (k < sd.nedges) {
-				const float4 E = S.edges[sd.edge_off + k];
-				ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
+		if (sd.og_nx == 0) {
+			for (int b0 = 0; b0 < sd.nedges; b0 += 32) {
+				const int k = b0 + lane;
+				bool ok = false;
+				if (k < sd.nedges) {
+					const float4 E = S.edges[sd.edge_off + k];
+					ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
+				}
+				const unsigned m = __ballot_sync(0xffffffffu, ok);
+				if (ok) out[K + __popc(m & lt)] = ((uint32_t)g << 28) | (uint32_t)(sd.edge_off + k);
+				K += __popc(m);
 			}
-			const unsigned m = __ballot_sync(0xffffffffu, ok);
-			if (ok) out[K + __popc(m & lt)] = ((uint32_t)g << 28) | (uint32_t)(sd.edge_off + k);
-			K += __popc(m);
+			continue;
 		}
+		// edge grid: the cells covering the query square (with a 1% cell
+		// margin); an edge is taken in the first of them that its own box
+		// covers, so once, and the same distance test decides; the group's
+		// edges are then put in edge (file) order
+		const int gs = K;
+		const int qx0 = obs_cell((q.x - r - sd.og_x0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_nx);
+		const int qx1 = obs_cell((q.x + r - sd.og_x0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_nx);
+		const int qy0 = obs_cell((q.y - r - sd.og_y0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_ny);
+		const int qy1 = obs_cell((q.y + r - sd.og_y0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_ny);
+		for (int cy = qy0; cy <= qy1; ++cy) {
+			const int row = sd.og_start + cy * sd.og_nx;
+			const int i0 = S.og_start[row + qx0], i1 = S.og_start[row + qx1 + 1];
+			for (int b0 = i0; b0 < i1; b0 += 32) {
+				const int it = b0 + lane;
+				bool ok = false;
+				int e = 0;
+				if (it < i1) {
+					const int2 item = S.og_items[it];
+					e = item.x;
+					const int4 ec = S.og_ecell[e];
+					if (item.y == max(ec.x, qx0) && cy == max(ec.y, qy0)) {
+						const float4 E = S.edges[e];
+						ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
+					}
+				}
+				const unsigned m = __ballot_sync(0xffffffffu, ok);
+				if (ok) out[K + __popc(m & lt)] = (uint32_t)e;
+				K += __popc(m);
+			}
+		}
+		__syncwarp();
+		// rank sort of the group's edge indices (distinct)
+		const int cnt = K - gs;
+		if (cnt <= 32) {
+			const uint32_t v = lane < cnt ? out[gs + lane] : 0xffffffffu;
+			int rank = 0;
+			for (int j = 0; j < cnt; ++j) rank += __shfl_sync(0xffffffffu, v, j) < v;
+			__syncwarp();
+			if (lane < cnt) out[gs + rank] = ((uint32_t)g << 28) | v;
+		} else {
+			if (lane == 0) {
+				for (int a = gs + 1; a < K; ++a) {
+					const uint32_t v = out[a];
+					int b = a - 1;
+					while (b >= gs && out[b] > v) { out[b + 1] = out[b]; --b; }
+					out[b + 1] = v;
+				}
+				for (int a = gs; a < K; ++a) out[a] |= (uint32_t)g << 28;
+			}
+		}
+		__syncwarp();
 	}
 	__syncwarp();
 	return K;
@@ -1993,6 +2050,18 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		CK(cudaMemcpy(edges_dev_, edges_.data(), sizeof(float4) * edges_.size(), cudaMemcpyHostToDevice));
 	}
 	d_->edges = edges_dev_;
+	build_edge_grids();
+	if (!og_items_.empty()) {
+		if (!dalloc(og_start_dev_, og_start_.size(), err_) || !dalloc(og_items_dev_, og_items_.size(), err_) ||
+		    !dalloc(og_ecell_dev_, og_ecell_.size(), err_))
+			return false;
+		CK(cudaMemcpy(og_start_dev_, og_start_.data(), sizeof(int) * og_start_.size(), cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(og_items_dev_, og_items_.data(), sizeof(int2) * og_items_.size(), cudaMemcpyHostToDevice));
+		CK(cudaMemcpy(og_ecell_dev_, og_ecell_.data(), sizeof(int4) * og_ecell_.size(), cudaMemcpyHostToDevice));
+	}
+	d_->og_start = og_start_dev_;
+	d_->og_items = og_items_dev_;
+	d_->og_ecell = og_ecell_dev_;
 	if (!build_tables()) return false;
 	// the host sinf/cosf: random-sample rotations (build_tables), the gradient
 	// rotations of TtcaDca and FOEAvoidance, the segment collision times
@@ -2004,6 +2073,49 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	if (!upload_all()) return false;
 	if (!choose_maxnb()) return false;
 	return true;
+}
+
+// Edge grids of the scenarios with many obstacle edges (host, once): cell size
+// the scenario's largest interaction range (doubled until the grid has at
+// most 4 cells per edge + 1024), each edge listed in every cell its bounding
+// box overlaps, in edge order.
+void Engine::build_edge_grids()
+{
+	og_start_.clear();
+	og_items_.clear();
+	og_ecell_.assign(edges_.size(), make_int4(0, 0, -1, -1));
+	for (auto& D : scen_) {
+		D.og_nx = D.og_ny = 0;
+		if (D.nedges < OBS_GRID_MIN_EDGES) continue;
+		float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
+		for (int k = 0; k < D.nedges; ++k) {
+			const float4 e = edges_[D.edge_off + k];
+			x0 = std::min(x0, std::min(e.x, e.z)); x1 = std::max(x1, std::max(e.x, e.z));
+			y0 = std::min(y0, std::min(e.y, e.w)); y1 = std::max(y1, std::max(e.y, e.w));
+		}
+		if (!(x1 >= x0 && y1 >= y0) || !std::isfinite(x1 - x0) || !std::isfinite(y1 - y0)) continue;
+		float cs = std::max(D.max_range, 1e-3f);
+		while (((double)(x1 - x0) / cs + 1.0) * ((double)(y1 - y0) / cs + 1.0) > 4.0 * D.nedges + 1024) cs *= 2.0f;
+		const float inv = 1.0f / cs;
+		const int nx = (int)((x1 - x0) * inv) + 1, ny = (int)((y1 - y0) * inv) + 1;
+		std::vector<std::vector<int2>> cells((size_t)nx * ny);
+		for (int k = 0; k < D.nedges; ++k) {
+			const float4 e = edges_[D.edge_off + k];
+			const int4 c = make_int4(obs_cell(std::min(e.x, e.z), x0, inv, nx), obs_cell(std::min(e.y, e.w), y0, inv, ny),
+			                         obs_cell(std::max(e.x, e.z), x0, inv, nx), obs_cell(std::max(e.y, e.w), y0, inv, ny));
+			og_ecell_[D.edge_off + k] = c;
+			for (int cy = c.y; cy <= c.w; ++cy)
+				for (int cx = c.x; cx <= c.z; ++cx) cells[(size_t)cy * nx + cx].push_back(make_int2(D.edge_off + k, cx));
+		}
+		D.og_x0 = x0; D.og_y0 = y0; D.og_inv = inv; D.og_nx = nx; D.og_ny = ny;
+		// og_start_[D.og_start + cell] .. [+ 1]: the cell's items (absolute)
+		D.og_start = (int)og_start_.size();
+		for (const auto& c : cells) {
+			og_start_.push_back((int)og_items_.size());
+			og_items_.insert(og_items_.end(), c.begin(), c.end());
+		}
+		og_start_.push_back((int)og_items_.size());
+	}
 }
 
 bool Engine::build_tables()

@@ -207,6 +207,15 @@ private:
 	int* scen_order_dev_ = nullptr;
 	std::vector<float4> edges_;      // obstacle edges of all scenarios
 	float4* edges_dev_ = nullptr;
+	// edge grids (ScenDesc::og_*): per scenario cell starts, items (global
+	// edge index, cell x), and each edge's cell range (x0, y0, x1, y1)
+	std::vector<int> og_start_;
+	std::vector<int2> og_items_;
+	std::vector<int4> og_ecell_;
+	int* og_start_dev_ = nullptr;
+	int2* og_items_dev_ = nullptr;
+	int4* og_ecell_dev_ = nullptr;
+	void build_edge_grids();
 	AgentRecord* io_host_ = nullptr;   // page-locked staging for AgentData exchange
 	int* status_host_ = nullptr;       // page-locked copy of the device status word
 	size_t io_host_cap_ = 0;

@@ -7,6 +7,7 @@
 // (src/Engine/core/costFunctionFactory.cpp:41-61), identified by kind, with
 // its range, coefficient and model parameters.
 #pragma once
+#include <cmath>
 #include <cstdint>
 
 namespace umans {
@@ -82,7 +83,26 @@ struct ScenDesc {
 	int agent_off, n;     // its agents occupy list slots [agent_off, agent_off + n)
 	int max_cells;        // cap on its grid's cell count
 	int edge_off, nedges; // its obstacle edges in the concatenated edge array
+	// uniform grid over its edges (og_nx == 0: none, the edges are scanned):
+	// cell (cx, cy) holds the edges whose bounding box overlaps it, as items
+	// [og_start + start[cy * og_nx + cx], ...) of the engine's item arrays
+	float og_x0, og_y0, og_inv;
+	int og_nx, og_ny, og_start;
 };
+
+// scenarios with at least this many edges get an edge grid
+constexpr int OBS_GRID_MIN_EDGES = 256;
+
+// cell coordinate along one axis, the same on the host and the device
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline int obs_cell(float v, float v0, float inv, int n)
+{
+	const float f = (v - v0) * inv;
+	int c = (f >= 0.0f) ? (int)fminf(f, 2.0e9f) : 0;   // NaN -> 0
+	return c >= n ? n - 1 : c;
+}
 
 // Grid parameters written by the device each step.
 struct GridParams {

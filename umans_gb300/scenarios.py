@@ -394,6 +394,46 @@ def model_toric_obstacle(model: str, n: int = 60, side: float = 8.0, seed: int =
     return sc
 
 
+def block_field(nblocks: int, side: float, rng, size=(0.3, 0.8), keep_clear=None) -> list:
+    """nblocks small rotated quadrilaterals scattered in a side x side square
+    (4 edges each), away from the points in keep_clear (k, 2)."""
+    out = []
+    while len(out) < nblocks:
+        c = rng.uniform(-side / 2, side / 2, 2)
+        if keep_clear is not None and len(keep_clear) and np.min(np.linalg.norm(keep_clear - c, axis=1)) < 1.2:
+            continue
+        h = rng.uniform(*size) / 2
+        a = rng.uniform(0, np.pi / 2)
+        rot = np.array([[np.cos(a), -np.sin(a)], [np.sin(a), np.cos(a)]])
+        sq = np.array([[-h, -h], [h, -h], [h, h], [-h, h]]) @ rot.T + c
+        out.append(sq.astype(np.float32))
+    return out
+
+
+def model_block_field(model: str, n: int = 60, seed: int = 18) -> Scenario:
+    """Agents crossing a 30 x 30 m field of 80 small blocks (320 edges: the
+    edge-grid path of the obstacle query)."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-15, 15, (n, 2))
+    goal = -pos + rng.uniform(-2, 2, (n, 2))
+    sc = Scenario(dt=0.1, world="Infinite", policies=[MODEL_POLICIES[model]],
+                  **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+    sc.obstacles = block_field(80, 30.0, rng, keep_clear=np.concatenate([pos, goal]))
+    return sc
+
+
+def model_toric_block_field(model: str, n: int = 60, side: float = 14.0, seed: int = 19) -> Scenario:
+    """A 14 x 14 m toric world with 70 small blocks (280 edges), some next to
+    the world's edges (displaced queries through the edge grid)."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-side / 2, side / 2, (n, 2))
+    goal = pos + rng.uniform(-30, 30, (n, 2))
+    sc = Scenario(dt=0.1, world="Toric", width=side, height=side, policies=[MODEL_POLICIES[model]],
+                  **_agents(n, pos, goal, pref=1.3, maxs=1.6))
+    sc.obstacles = block_field(70, side - 0.8, rng, size=(0.2, 0.5), keep_clear=pos)
+    return sc
+
+
 def model_toric(model: str, n: int = 60, side: float = 12.0, seed: int = 12) -> Scenario:
     """A small toric world (wrap-around neighbours, including displaced
     duplicates when the range exceeds half the side)."""
