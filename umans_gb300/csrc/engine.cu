@@ -3382,6 +3382,10 @@ Engine::~Engine()
 		if (e) cudaEventDestroy(e);
 	if (scen_order_dev_) cudaFree(scen_order_dev_);
 	if (edges_dev_) cudaFree(edges_dev_);
+	if (og_start_dev_) cudaFree(og_start_dev_);
+	if (og_items_dev_) cudaFree(og_items_dev_);
+	if (og_ecell_dev_) cudaFree(og_ecell_dev_);
+	if (counters_) cudaFree(counters_);
 	if (ev0_) cudaEventDestroy(ev0_);
 	if (ev1_) cudaEventDestroy(ev1_);
 	if (stream_) cudaStreamDestroy(stream_);
