@@ -24,7 +24,13 @@ costs, in an infinite world, evaluated in float64 over pair lists:
   i.e. a = sum_c coeff_c F_c / mass_c, clamped to the maximum acceleration,
   new velocity clamped to the maximum speed; zero at the goal
   (Policy::ComputeNewVelocity, policy.cpp:43-76);
-* contact forces: Policy::getContactForces (policy.cpp:107-141);
+* contact forces: Policy::getContactForces (policy.cpp:107-141), with the
+  obstacle edges as well;
+* static obstacles: each agent's edges within the policy's range
+  (WorldBase::computeNeighboringObstacles, worldBase.cpp:62-77), the
+  SocialForces obstacle force (SocialForcesAvoidance.cpp:112-140) and
+  contact with edges (policy.cpp:126-137), the nearest point of an edge as
+  nearestPointOnLine with onSegment (vector2D.h:274-296);
 * integration: Agent::UpdateVelocityAndPosition (agent.cpp:71-93), contact
   acceleration = force / 80.
 
@@ -100,6 +106,26 @@ def _clamp(v, L, flag):
     return np.where(flag[:, None], v / np.where(m > 0, m, 1.0)[:, None] * L[:, None], v)
 
 
+def _edge_regime(p, a, b):
+    """0: nearest point interior, 1: end a (k >= 1), 2: end b (k <= 0), 3:
+    point-like edge (a == b)."""
+    line = a - b
+    L2 = (line * line).sum(-1)
+    k = ((p - b) * line).sum(-1) / np.where(L2 > 0, L2, 1.0)
+    reg = np.where(k >= 1, 1, np.where(k <= 0, 2, 0))
+    return np.where(L2 > 0, reg, 3)
+
+
+def _edge_diff(p, a, b, reg):
+    """p - nearest point of the edge, the nearest point's regime given."""
+    line = a - b
+    L2 = (line * line).sum(-1)
+    k = ((p - b) * line).sum(-1) / np.where(L2 > 0, L2, 1.0)
+    k = np.where(reg == 0, k, np.where(reg == 1, 1.0, 0.0))
+    nearest = np.where((reg == 3)[:, None], a, a * k[:, None] + b * (1 - k)[:, None])
+    return p - nearest
+
+
 def step(sc: dict, pols, pos, vel, params=None, branches=None, record=None):
     """One step in float64 from (pos, vel).  params = (V0, sigma, k, tau0)
     overriding the policy's values, or None.  branches: a dict made by
@@ -135,6 +161,22 @@ def step(sc: dict, pols, pos, vel, params=None, branches=None, record=None):
     X = pos[I] - pos[J]
     d2 = (X * X).sum(-1)
     rsum = radius[I] + radius[J]
+    # obstacle edges within the policy's range, per agent
+    edges = np.asarray(sc.get("edges", np.zeros((0, 4))), np.float64).reshape(-1, 4)
+    if len(edges):
+        if B:
+            Io, Eo, reg = B["Io"], B["Eo"], B["reg"]
+        else:
+            ii, ee = np.meshgrid(np.arange(n), np.arange(len(edges)), indexing="ij")
+            ii, ee = ii.ravel(), ee.ravel()
+            rg = _edge_regime(pos[ii], edges[ee, :2], edges[ee, 2:])
+            dd = _edge_diff(pos[ii], edges[ee, :2], edges[ee, 2:], rg)
+            sel = (dd * dd).sum(-1) <= P["range"] ** 2
+            Io, Eo, reg = ii[sel], ee[sel], rg[sel]
+        R_["Io"], R_["Eo"], R_["reg"] = Io, Eo, reg
+        odiff = _edge_diff(pos[Io], edges[Eo, :2], edges[Eo, 2:], reg)
+        od2 = (odiff * odiff).sum(-1)
+        odist = np.sqrt(od2)
     acc = np.zeros_like(vel)
     for ci, c in enumerate(P["costs"]):
         if c["kind"] == K_GR:
@@ -181,6 +223,14 @@ def step(sc: dict, pols, pos, vel, params=None, branches=None, record=None):
             R_[f"ok{ci}"] = ok
             use = inr & ok
             F = _sum_to(I[use], f[use], n)
+            if c["kind"] == K_SF and len(edges):
+                oinr = B[f"oinr{ci}"] if B else od2 <= c["range"] ** 2
+                ook = B[f"ook{ci}"] if B else odist >= 0.001
+                R_[f"oinr{ci}"], R_[f"ook{ci}"] = oinr, ook
+                U0, Rr = c["p"][3], c["p"][4]
+                fo = odiff * (U0 / Rr * np.exp(-odist / Rr))[:, None]
+                uo = oinr & ook
+                F = F + _sum_to(Io[uo], fo[uo], n)
         acc += c["coeff"] * F / c["p"][5]
     acl = B["acl"] if B else _norm(acc) > maxa
     acc = _clamp(acc, maxa, acl)
@@ -197,6 +247,12 @@ def step(sc: dict, pols, pos, vel, params=None, branches=None, record=None):
         R_["take"] = take
         f = X[take] / md[take][:, None] * (P["contact"] * inter[take])[:, None]
         contact = _sum_to(I[take], f, n)
+        if len(edges):
+            ointer = radius[Io] - odist
+            otake = B["otake"] if B else (ointer > 0) & (odist > 0)
+            R_["otake"] = otake
+            fo = odiff[otake] / odist[otake][:, None] * (P["contact"] * ointer[otake])[:, None]
+            contact = contact + _sum_to(Io[otake], fo, n)
     vel2 = u + contact / 80.0 * dt
     return pos + vel2 * dt, vel2
 

@@ -58,3 +58,19 @@ def test_tangent_matches_central_differences_when_smooth(tmp_path):
     tan = calib64.tangent_gradient(sc, states, tg, w, p0, [(np.eye(4)[k], z, z) for k in range(4)])
     fd = calib64.central_difference(lambda p: calib64.loss(sc, steps, tg, w, params=p), p0, 1e-5)
     assert np.linalg.norm(tan - fd) <= 1e-4 * np.linalg.norm(fd)
+
+
+def test_obstacle_steps_match_the_port(tmp_path):
+    """Walls and blocks: SocialForces obstacle forces and contact with edges."""
+    sc = port.read_scenario(S.calibration_walls().write(str(tmp_path / "w.xml")))
+    assert len(sc["edges"]) == 40
+    pols = calib64.policy_arrays(sc)
+    P = port.PortSim(sc)
+    worst = 0.0
+    for _ in range(30):
+        st0 = P.state()
+        P.step(1)
+        st = P.state()
+        p, v = calib64.step(sc, pols, st0["pos"].astype(np.float64), st0["vel"].astype(np.float64))
+        worst = max(worst, float(np.abs(p - st["pos"]).max()))
+    assert worst <= 1e-4

@@ -223,8 +223,48 @@ def test_unsupported_policies_are_rejected(tmp_path):
         s.diff_begin(np.zeros((3, s.n, 2), np.float32))
 
 
-def test_obstacles_are_rejected(tmp_path):
-    path = S.model_obstacle_crossing("SocialForces", n=10).write(str(tmp_path / "obst.xml"))
-    s = Simulation(path)
-    with pytest.raises(UmansError, match="obstacles"):
-        s.diff_begin(np.zeros((3, s.n, 2), np.float32))
+def _walls_case(tmp_path, steps):
+    path = S.calibration_walls().write(str(tmp_path / "w.xml"))
+    h = Simulation(S.calibration_walls(HELD_OUT).write(str(tmp_path / "w_held.xml")))
+    targets = []
+    for _ in range(steps):
+        h.step(1)
+        targets.append(h.positions())
+    h.close()
+    return path, np.array(targets)
+
+
+def test_obstacle_parameter_gradient_vs_float64_tangent(tmp_path):
+    """Walls and blocks (SocialForces obstacle forces, contact with edges):
+    the obstacle terms enter the adjoint through the agents' positions."""
+    steps = 15
+    path, tg = _walls_case(tmp_path, steps)
+    _, g, p0 = _engine_gradient(path, tg, 4)
+    sc = port.read_scenario(path)
+    n = len(sc["ids"])
+    states = _float_states(path, steps)
+    z = np.zeros((n, 2))
+    ref = calib64.tangent_gradient(sc, states, tg, 1.0 / (steps * n), p0, [(np.eye(4)[k], z, z) for k in range(4)])
+    err = _relerr(g[0], ref)
+    print("engine", g[0], "tangent", ref, "rel err", err)
+    assert err <= TOL
+
+
+def test_obstacle_state_gradient_vs_float64_tangent(tmp_path):
+    steps = 12
+    path, tg = _walls_case(tmp_path, steps)
+    _, (g, gp, gv), p0 = _engine_gradient(path, tg, 5, with_state=True)
+    sc = port.read_scenario(path)
+    n = len(sc["ids"])
+    states = _float_states(path, steps)
+    rng = np.random.default_rng(1)
+    dirs = [(np.zeros(4), rng.standard_normal((n, 2)), rng.standard_normal((n, 2))) for _ in range(3)]
+    # the agents touching the walls alone
+    e = np.zeros((n, 2))
+    e[:4] = rng.standard_normal((4, 2))
+    dirs.append((np.zeros(4), e, np.zeros((n, 2))))
+    ref = calib64.tangent_gradient(sc, states, tg, 1.0 / (steps * n), p0, dirs, h=1e-6)
+    eng = np.array([(gp * dp).sum() + (gv * dv).sum() for _, dp, dv in dirs])
+    err = _relerr(eng, ref)
+    print("engine", eng, "tangent", ref, "rel err", err)
+    assert err <= TOL

@@ -207,5 +207,52 @@ UDA float2 contact_adj(float2 D, float rsum, float scale, float2 lC)
 	return mul2(sub2(mul2(sub2(lC, mul2(n, dot2(n, lC))), rsum / m), lC), scale);
 }
 
+// Obstacle edge (a, b) seen from p: diff = p - nearest point of the segment
+// (nearestPointOnLine with onSegment, vector2D.h:274-296) and whether the
+// nearest point is interior (then d diff / d p = I - u u^T, u along the
+// edge; at an end point or for a point-like edge it is I).
+struct EdgeSeen { float2 diff, u; bool interior; };
+UDA EdgeSeen edge_seen(float2 p, float2 a, float2 b)
+{
+	EdgeSeen r;
+	r.interior = false;
+	r.u = v2(0, 0);
+	r.diff = vsub(p, nearest_on_segment(p, a, b));
+	if (a.x == b.x && a.y == b.y) return r;
+	const float2 line = vsub(a, b);
+	const float k = vdot(vsub(p, b), line) / vsq(line);
+	if (k > 0 && k < 1) {
+		r.interior = true;
+		r.u = mul2(line, 1.0f / sqrtf(dot2(line, line)));
+	}
+	return r;
+}
+// P^T v for P = d diff / d p
+UDA float2 edge_proj(const EdgeSeen& e, float2 v)
+{
+	return e.interior ? sub2(v, mul2(e.u, dot2(e.u, v))) : v;
+}
+
+// SocialForcesAvoidance::ComputeObstacleInteractionForce
+// (SocialForcesAvoidance.cpp:112-140): F = diff (U0/R) exp(-|diff|/R) for
+// |diff| >= 0.001; adjoint of p from the adjoint lF of F
+UDA float2 sf_obstacle_adj(const AgentCtx& A, const CostDesc& c, const EdgeSeen& e, float2 lF)
+{
+	const float dist = sqrtf(dot2(e.diff, e.diff));
+	if (dist < 0.001f) return v2(0, 0);
+	const float U0 = c.p[3], R = c.p[4];
+	const float G = U0 / R * expf(-dist / R);
+	// d F / d diff = G I + diff (dG/d dist) diff^T / dist, dG/d dist = -G/R
+	const float2 ld = add2(mul2(lF, G), mul2(e.diff, -G / R * dot2(e.diff, lF) / dist));
+	return edge_proj(e, ld);
+}
+
+// contact with an edge (policy.cpp:126-137): the agent-pair contact force
+// with D = diff and r_j = 0
+UDA float2 edge_contact_adj(const EdgeSeen& e, float radius, float scale, float2 lC)
+{
+	return edge_proj(e, contact_adj(e.diff, radius, scale, lC));
+}
+
 #undef UDA
 }  // namespace umans

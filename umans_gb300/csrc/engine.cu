@@ -1826,6 +1826,29 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 				if (lvj.y != 0) atomicAdd(&S.lam_in_v[j].y, lvj.y);
 			}
 		}
+		// static obstacle edges (the list recomputed from the state the step
+		// started from, as the forward step gathered it): SocialForces
+		// obstacle forces (compute_force) and contact with edges
+		if (sd.nedges > 0 && (moving || contact)) {
+			NbView N;
+			N.edges = S.edges; N.W = sd.width; N.H = sd.height;
+			uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
+			N.obs = ol;
+			N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
+			for (int k = lane; k < N.KO; k += 32) {
+				float2 a, b;
+				nb_seg(N, k, &a, &b);
+				const EdgeSeen es = edge_seen(A.pos, a, b);
+				if (moving)
+					for (int c = 0; c < pol.ncost; ++c) {
+						const CostDesc& cd = pol.cost[c];
+						if (cd.kind != K_SOCIALFORCES || dist2_to_segment(A.pos, a, b) > cd.range * cd.range) continue;
+						lpi = add2(lpi, sf_obstacle_adj(A, cd, es, mul2(la, cd.coeff / cd.p[5])));
+					}
+				if (contact) lpi = add2(lpi, edge_contact_adj(es, A.radius, pol.contact_scale, lC));
+			}
+			__syncwarp();
+		}
 		// warp sums (lane 0 also holds the goal-force terms)
 		float vals[8] = { lpi.x, lpi.y, lvi.x, lvi.y, dV0, dsig, dk, dtau0 };
 		for (int q = 0; q < 8; ++q)
@@ -3126,7 +3149,7 @@ void Engine::diff_free()
 	Diff& D = df_;
 	void* ptrs[] = { D.s0_pos, D.s0_vel, D.s0_view, D.s0_vwf, D.s0_rng, D.targets, D.ck_pos, D.ck_vel, D.seg_pos,
 	                 D.seg_vel, D.seg_acc, D.tape, D.tape_cnt, D.lam_p, D.lam_v, D.lo_p, D.lo_v, D.adj_nb, D.dparams,
-	                 D.loss };
+	                 D.loss, D.obs_list };
 	for (void* p : ptrs)
 		if (p) cudaFree(p);
 	D = Diff();
@@ -3147,7 +3170,6 @@ bool Engine::diff_begin(int steps, int every, const float* targets, float weight
 		err_ = "the differentiable form needs a fixed agent set (no delayed starts, no removal at the goal)";
 		return false;
 	}
-	if (!edges_.empty()) { err_ = "the differentiable form does not support static obstacles"; return false; }
 	for (size_t pi = 0; pi < pols_.size(); ++pi) {
 		const PolicyDesc& P = pols_[pi];
 		bool ok = P.method == M_GRADIENT;
@@ -3174,7 +3196,8 @@ bool Engine::diff_begin(int steps, int every, const float* targets, float weight
 	    !dalloc(D.seg_acc, nn * D.every, err_) || !dalloc(D.tape_cnt, nn * D.every, err_) ||
 	    !dalloc(D.lam_p, nn, err_) || !dalloc(D.lam_v, nn, err_) || !dalloc(D.lo_p, nn, err_) ||
 	    !dalloc(D.lo_v, nn, err_) || !dalloc(D.adj_nb, nn, err_) || !dalloc(D.dparams, 4 * scen_.size(), err_) ||
-	    !dalloc(D.loss, 1, err_)) {
+	    !dalloc(D.loss, 1, err_) ||
+	    (!edges_.empty() && !dalloc(D.obs_list, (size_t)num_sms_ * 5 * 4 * std::max(d_->max_obs, 1), err_))) {
 		diff_free();
 		return false;
 	}
@@ -3340,6 +3363,7 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 			A.lam_in_p = D.lam_p; A.lam_in_v = D.lam_v;
 			A.dparams = D.dparams;
 			A.adj_nb = D.adj_nb;
+			A.obs_list = D.obs_list;   // k_adjoint warps (at most num_sms * 5 blocks of 4)
 			k_adj_prep<<<(n + 255) / 256, 256, 0, stream_>>>(A);
 			k_adjoint<<<adj_blocks, 128, 0, stream_>>>(A);
 		}

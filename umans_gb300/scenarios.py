@@ -232,6 +232,25 @@ def calibration_set(params=None, n: int = 512, side: float = 40.0, seed: int = 5
     return Scenario(dt=0.1, world="Infinite", policies=[pol], **_agents(n, pos, goal))
 
 
+def calibration_walls(params=None, n: int = 48, side: float = 16.0, seed: int = 6) -> Scenario:
+    """A calibration parameter set in a walled square with a few blocks (the
+    differentiable form with static obstacles): the square's four walls just
+    outside the agents' area (four agents start touching them), and 6 blocks
+    inside it."""
+    sc = calibration_set(params, n=n, side=side, seed=seed)
+    h = side / 2 + 0.6
+    sc.pos[:4] = np.array([[h - 0.2, 1.0], [-h + 0.2, -1.0], [2.0, h - 0.25], [-2.0, -h + 0.25]], np.float32)
+    t = 0.4
+    sc.obstacles = [np.array(q, np.float32) for q in (
+        [[-h - t, -h - t], [h + t, -h - t], [h + t, -h], [-h - t, -h]],
+        [[-h - t, h], [h + t, h], [h + t, h + t], [-h - t, h + t]],
+        [[-h - t, -h], [-h, -h], [-h, h], [-h - t, h]],
+        [[h, -h], [h + t, -h], [h + t, h], [h, h]])]
+    rng = np.random.default_rng(seed + 100)
+    sc.obstacles += block_field(6, side - 2.0, rng, size=(0.6, 1.2), keep_clear=sc.pos)
+    return sc
+
+
 # The policy configurations the reference ships, one per navigation model
 # (parameter values as in the reference's examples/policies/*.xml; the same
 # values are needed for trajectories to be comparable).
