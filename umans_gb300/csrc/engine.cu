@@ -3196,8 +3196,7 @@ bool Engine::diff_begin(int steps, int every, const float* targets, float weight
 	    !dalloc(D.seg_acc, nn * D.every, err_) || !dalloc(D.tape_cnt, nn * D.every, err_) ||
 	    !dalloc(D.lam_p, nn, err_) || !dalloc(D.lam_v, nn, err_) || !dalloc(D.lo_p, nn, err_) ||
 	    !dalloc(D.lo_v, nn, err_) || !dalloc(D.adj_nb, nn, err_) || !dalloc(D.dparams, 4 * scen_.size(), err_) ||
-	    !dalloc(D.loss, 1, err_) ||
-	    (!edges_.empty() && !dalloc(D.obs_list, (size_t)num_sms_ * 5 * 4 * std::max(d_->max_obs, 1), err_))) {
+	    !dalloc(D.loss, 1, err_)) {
 		diff_free();
 		return false;
 	}
@@ -3328,6 +3327,16 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 	CK(cudaMemsetAsync(D.lam_v, 0, nb2, stream_));
 	CK(cudaMemsetAsync(D.dparams, 0, sizeof(float) * 4 * scen_.size(), stream_));
 	const int adj_blocks = std::max(1, std::min((n + 3) / 4, num_sms_ * 5));
+	// per-warp obstacle lists of k_adjoint, at the capacity the step uses
+	// (configure sets it; at most num_sms * 5 blocks of 4 warps)
+	if (!edges_.empty() && D.obs_cap != S.max_obs) {
+		if (D.obs_list) cudaFree(D.obs_list);
+		D.obs_list = nullptr;
+		D.obs_cap = 0;
+		if (S.max_obs <= 0) { err_ = "obstacle list capacity not configured"; return false; }
+		if (!dalloc(D.obs_list, (size_t)num_sms_ * 5 * 4 * S.max_obs, err_)) return false;
+		D.obs_cap = S.max_obs;
+	}
 	for (int c = D.nck - 1; c >= 0 && n > 0; --c) {
 		const int t0 = c * D.every, m = std::min(D.every, D.steps - t0);
 		// recompute the segment from its checkpoint, recording lists and states

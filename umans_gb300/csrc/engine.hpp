@@ -239,7 +239,8 @@ private:
 		float4* adj_nb = nullptr;                    // n: neighbour terms of the step being reversed
 		float* dparams = nullptr;
 		double* loss = nullptr;
-		uint32_t* obs_list = nullptr;                // per k_adjoint warp: max_obs entries
+		uint32_t* obs_list = nullptr;                // per k_adjoint warp: obs_cap entries
+		int obs_cap = 0;
 	} df_;
 	bool diff_restore_start();
 	bool diff_alloc_tape();
