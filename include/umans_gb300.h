@@ -149,6 +149,7 @@ int umans_profile_counters(umans_sim* sim, unsigned long long* counts, int n);
  * method "gradient" with SocialForcesAvoidance, PowerLaw and
  * GoalReachingForce costs (ForceBasedFunction::GetGradient,
  * src/Engine/CostFunctions/ForceBasedFunction.cpp:32-36), contact forces
+ * and static obstacles (SocialForcesAvoidance.cpp:112-140, policy.cpp:126-137)
  * included; a fixed agent set.
  *
  * umans_diff_begin records the current state as the episode's start and the
