@@ -706,6 +706,66 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 	return K;
 }
 
+// The edge-grid query of gather_obstacles for one displacement group: the
+// cells covering the query square (with a 1% cell margin); an edge is taken
+// in the first of them that its own box covers, so once, and the same
+// distance test decides; the group's edges are then put in edge (file)
+// order.  Appends to out[K..]; returns the new count.
+__device__ __forceinline__ int gather_obstacles_grid(const DevState& S, const ScenDesc& sd, float2 q, float r, int g,
+                                                  int lane, uint32_t* out, int K)
+{
+	const float r2 = r * r;
+	const unsigned lt = (1u << lane) - 1u;
+	const int gs = K;
+	const int qx0 = obs_cell((q.x - r - sd.og_x0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_nx);
+	const int qx1 = obs_cell((q.x + r - sd.og_x0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_nx);
+	const int qy0 = obs_cell((q.y - r - sd.og_y0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_ny);
+	const int qy1 = obs_cell((q.y + r - sd.og_y0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_ny);
+	for (int cy = qy0; cy <= qy1; ++cy) {
+		const int row = sd.og_start + cy * sd.og_nx;
+		const int i0 = S.og_start[row + qx0], i1 = S.og_start[row + qx1 + 1];
+		for (int b0 = i0; b0 < i1; b0 += 32) {
+			const int it = b0 + lane;
+			bool ok = false;
+			int e = 0;
+			if (it < i1) {
+				const int2 item = S.og_items[it];
+				e = item.x;
+				const int4 ec = S.og_ecell[e];
+				if (item.y == max(ec.x, qx0) && cy == max(ec.y, qy0)) {
+					const float4 E = S.edges[e];
+					ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
+				}
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, ok);
+			if (ok) out[K + __popc(m & lt)] = (uint32_t)e;
+			K += __popc(m);
+		}
+	}
+	__syncwarp();
+	// rank sort of the group's edge indices (distinct)
+	const int cnt = K - gs;
+	if (cnt <= 32) {
+		const uint32_t v = lane < cnt ? out[gs + lane] : 0xffffffffu;
+		int rank = 0;
+		for (int j = 0; j < cnt; ++j) rank += __shfl_sync(0xffffffffu, v, j) < v;
+		__syncwarp();
+		if (lane < cnt) out[gs + rank] = ((uint32_t)g << 28) | v;
+	} else {
+		if (lane == 0) {
+			for (int a = gs + 1; a < K; ++a) {
+				const uint32_t v = out[a];
+				int b = a - 1;
+				while (b >= gs && out[b] > v) { out[b + 1] = out[b]; --b; }
+				out[b + 1] = v;
+			}
+			for (int a = gs; a < K; ++a) out[a] |= (uint32_t)g << 28;
+		}
+	}
+	__syncwarp();
+	return K;
+}
+
 // Obstacle edges within range of the agent (worldBase.cpp:62-77), per
 // displacement group as the agents (worldToric.cpp:32-79): edges in file
 // order, each group's appended after the previous one.  Returns the count.
@@ -740,56 +800,7 @@ __device__ int gather_obstacles(const DevState& S, const ScenDesc& sd, float2 p,
 			}
 			continue;
 		}
-		// edge grid: the cells covering the query square (with a 1% cell
-		// margin); an edge is taken in the first of them that its own box
-		// covers, so once, and the same distance test decides; the group's
-		// edges are then put in edge (file) order
-		const int gs = K;
-		const int qx0 = obs_cell((q.x - r - sd.og_x0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_nx);
-		const int qx1 = obs_cell((q.x + r - sd.og_x0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_nx);
-		const int qy0 = obs_cell((q.y - r - sd.og_y0) * sd.og_inv - 0.01f, 0.0f, 1.0f, sd.og_ny);
-		const int qy1 = obs_cell((q.y + r - sd.og_y0) * sd.og_inv + 0.01f, 0.0f, 1.0f, sd.og_ny);
-		for (int cy = qy0; cy <= qy1; ++cy) {
-			const int row = sd.og_start + cy * sd.og_nx;
-			const int i0 = S.og_start[row + qx0], i1 = S.og_start[row + qx1 + 1];
-			for (int b0 = i0; b0 < i1; b0 += 32) {
-				const int it = b0 + lane;
-				bool ok = false;
-				int e = 0;
-				if (it < i1) {
-					const int2 item = S.og_items[it];
-					e = item.x;
-					const int4 ec = S.og_ecell[e];
-					if (item.y == max(ec.x, qx0) && cy == max(ec.y, qy0)) {
-						const float4 E = S.edges[e];
-						ok = dist2_to_segment(q, V(E.x, E.y), V(E.z, E.w)) <= r2;
-					}
-				}
-				const unsigned m = __ballot_sync(0xffffffffu, ok);
-				if (ok) out[K + __popc(m & lt)] = (uint32_t)e;
-				K += __popc(m);
-			}
-		}
-		__syncwarp();
-		// rank sort of the group's edge indices (distinct)
-		const int cnt = K - gs;
-		if (cnt <= 32) {
-			const uint32_t v = lane < cnt ? out[gs + lane] : 0xffffffffu;
-			int rank = 0;
-			for (int j = 0; j < cnt; ++j) rank += __shfl_sync(0xffffffffu, v, j) < v;
-			__syncwarp();
-			if (lane < cnt) out[gs + rank] = ((uint32_t)g << 28) | v;
-		} else {
-			if (lane == 0) {
-				for (int a = gs + 1; a < K; ++a) {
-					const uint32_t v = out[a];
-					int b = a - 1;
-					while (b >= gs && out[b] > v) { out[b + 1] = out[b]; --b; }
-					out[b + 1] = v;
-				}
-				for (int a = gs; a < K; ++a) out[a] |= (uint32_t)g << 28;
-			}
-		}
+		K = gather_obstacles_grid(S, sd, q, r, g, lane, out, K);
 		__syncwarp();
 	}
 	__syncwarp();
@@ -1347,7 +1358,9 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 // compiled out, which lowers register use and raises occupancy.
 // TAPE: also record the neighbour lists and the pre-clamp acceleration for
 // the differentiable form's backward pass
-template <int MODE, bool TAPE = false>
+// OBST: the obstacle-edge gather compiled in (the force-only kernel of
+// obstacle-free groups leaves it out, which keeps its registers)
+template <int MODE, bool TAPE = false, bool OBST = true>
 __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
 {
 	extern __shared__ unsigned char smem[];
@@ -1405,7 +1418,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 			}
 			if (lane == 0) S.tape_cnt[slot] = K;
 		}
-		if (sd.nedges > 0) {
+		if (OBST && sd.nedges > 0) {
 			uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
 			N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
 			N.obs = ol;
@@ -1725,6 +1738,37 @@ __global__ void k_adj_prep(DevState S)
 // neighbour's terms added to its adjoint with one atomic per nonzero
 // component.  The parameters' adjoints (V0, sigma, k, tau0) are summed per
 // scenario.
+// this lane's share of the obstacle terms of an agent's position adjoint:
+// SocialForces obstacle forces (compute_force) and contact with edges, over
+// the edge list regathered from the reversed step's start state (not
+// inlined, to keep k_adjoint's registers for scenarios without obstacles)
+__device__ __noinline__ float2 obstacle_adjoint(const DevState& S, const ScenDesc& sd, const PolicyDesc& pol,
+                                                const AgentCtx& A, int gw, int lane, bool moving, bool contact,
+                                                float2 la, float2 lC)
+{
+	NbView N;
+	N.edges = S.edges; N.W = sd.width; N.H = sd.height;
+	uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
+	N.obs = ol;
+	N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
+	float2 lp = v2(0, 0);
+	for (int k = lane; k < N.KO; k += 32) {
+		float2 a, b;
+		nb_seg(N, k, &a, &b);
+		const EdgeSeen es = edge_seen(A.pos, a, b);
+		if (moving)
+			for (int c = 0; c < pol.ncost; ++c) {
+				const CostDesc& cd = pol.cost[c];
+				if (cd.kind != K_SOCIALFORCES || dist2_to_segment(A.pos, a, b) > cd.range * cd.range) continue;
+				lp = add2(lp, sf_obstacle_adj(A, cd, es, mul2(la, cd.coeff / cd.p[5])));
+			}
+		if (contact) lp = add2(lp, edge_contact_adj(es, A.radius, pol.contact_scale, lC));
+	}
+	__syncwarp();
+	return lp;
+}
+
+template <bool OBST>
 __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 {
 	const int lane = threadIdx.x & 31;
@@ -1829,26 +1873,8 @@ __global__ void __launch_bounds__(128) k_adjoint(DevState S)
 		// static obstacle edges (the list recomputed from the state the step
 		// started from, as the forward step gathered it): SocialForces
 		// obstacle forces (compute_force) and contact with edges
-		if (sd.nedges > 0 && (moving || contact)) {
-			NbView N;
-			N.edges = S.edges; N.W = sd.width; N.H = sd.height;
-			uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
-			N.obs = ol;
-			N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
-			for (int k = lane; k < N.KO; k += 32) {
-				float2 a, b;
-				nb_seg(N, k, &a, &b);
-				const EdgeSeen es = edge_seen(A.pos, a, b);
-				if (moving)
-					for (int c = 0; c < pol.ncost; ++c) {
-						const CostDesc& cd = pol.cost[c];
-						if (cd.kind != K_SOCIALFORCES || dist2_to_segment(A.pos, a, b) > cd.range * cd.range) continue;
-						lpi = add2(lpi, sf_obstacle_adj(A, cd, es, mul2(la, cd.coeff / cd.p[5])));
-					}
-				if (contact) lpi = add2(lpi, edge_contact_adj(es, A.radius, pol.contact_scale, lC));
-			}
-			__syncwarp();
-		}
+		if (OBST && sd.nedges > 0 && (moving || contact))
+			lpi = add2(lpi, obstacle_adjoint(S, sd, pol, A, gw, lane, moving, contact, la, lC));
 		// warp sums (lane 0 also holds the goal-force terms)
 		float vals[8] = { lpi.x, lpi.y, lvi.x, lvi.y, dV0, dsig, dk, dtau0 };
 		for (int q = 0; q < 8; ++q)
@@ -2062,7 +2088,11 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			const int j0 = (int)scen_order_.size();
 			for (size_t k = 0; k < scen_.size(); ++k)
 				if (cls[k] == c) scen_order_.push_back((int)k);
-			if ((int)scen_order_.size() > j0) groups_.push_back(KGroup{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 });
+			if ((int)scen_order_.size() > j0) {
+				KGroup g{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 };
+				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
+				groups_.push_back(g);
+			}
 		}
 		if (!dalloc(scen_order_dev_, scen_order_.size(), err_)) return false;
 		CK(cudaMemcpy(scen_order_dev_, scen_order_.data(), sizeof(int) * scen_order_.size(), cudaMemcpyHostToDevice));
@@ -2406,10 +2436,12 @@ void Engine::invalidate_graph()
 	graph_valid_ = false;
 }
 
-static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int mode = 0)
+static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int mode = 0, bool obst = true)
 {
 	int per_sm = 0;
-	if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1>, warps_per_block * 32, smem);
+	if (mode == 1 && !obst)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1, false, false>, warps_per_block * 32, smem);
+	else if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1>, warps_per_block * 32, smem);
 	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<0>, warps_per_block * 32, smem);
 	if (per_sm < 1) per_sm = 1;
 	return num_sms * per_sm;
@@ -2427,6 +2459,8 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		CK(cudaFuncSetAttribute(k_agent<1, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+		CK(cudaFuncSetAttribute(k_agent<1, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	}
 	mode_ = 1;
 	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
@@ -2436,7 +2470,7 @@ bool Engine::configure()
 	for (const auto& D : scen_) maxe = std::max(maxe, D.nedges);
 	S.max_obs = 5 * maxe;   // every edge, once per displacement group
 	for (auto& g : groups_) {
-		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode);
+		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode, g.obst);
 		if (opt_.occupancy < 1.0f) g.blocks = std::max(num_sms_, (int)(g.blocks * opt_.occupancy));
 		g.scratch_off = scr;
 		scr += (size_t)g.blocks * wpb * 2 * maxnb_;
@@ -2486,9 +2520,11 @@ void Engine::enqueue_step()
 		A.scratch = S.scratch + g.scratch_off;
 		A.obs_list = S.obs_list + g.obs_off;
 		if (S.tape_list) {
-			if (g.mode == 1) k_agent<1, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
+			if (g.mode == 1 && g.obst) k_agent<1, true, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
+			else if (g.mode == 1) k_agent<1, true, false><<<blocks, wpb * 32, smem, st>>>(A, 0);
 			else k_agent<0, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
-		} else if (g.mode == 1) k_agent<1><<<blocks, wpb * 32, smem, st>>>(A, 0);
+		} else if (g.mode == 1 && g.obst) k_agent<1, false, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
+		else if (g.mode == 1) k_agent<1, false, false><<<blocks, wpb * 32, smem, st>>>(A, 0);
 		else k_agent<0><<<blocks, wpb * 32, smem, st>>>(A, 0);
 	};
 	// one after the other: each launch fills the GPU (measured: running the
@@ -3374,7 +3410,8 @@ bool Engine::diff_backward(float* dparams, float* dpos0, float* dvel0)
 			A.adj_nb = D.adj_nb;
 			A.obs_list = D.obs_list;   // k_adjoint warps (at most num_sms * 5 blocks of 4)
 			k_adj_prep<<<(n + 255) / 256, 256, 0, stream_>>>(A);
-			k_adjoint<<<adj_blocks, 128, 0, stream_>>>(A);
+			if (edges_.empty()) k_adjoint<false><<<adj_blocks, 128, 0, stream_>>>(A);
+			else k_adjoint<true><<<adj_blocks, 128, 0, stream_>>>(A);
 		}
 	}
 	CK(cudaGetLastError());

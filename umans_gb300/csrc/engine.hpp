@@ -201,6 +201,7 @@ private:
 		int j0, j1;        // positions in scen_order_
 		int blocks;
 		size_t scratch_off, obs_off;
+		bool obst = false;   // a scenario of the group has obstacle edges
 	};
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
