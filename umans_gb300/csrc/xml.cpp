@@ -67,11 +67,16 @@ const XmlElement* XmlElement::first_child(const char* nm) const
 
 const XmlElement* XmlElement::next_sibling(const XmlElement* child, const char* nm) const
 {
-	bool found = false;
-	for (const auto& c : children) {
-		if (found && (!nm || c->name == nm)) return c.get();
-		if (c.get() == child) found = true;
+	// from the child's own position (constant time per step of a sibling walk)
+	size_t k = 0;
+	if (child && child->index < children.size() && children[child->index].get() == child) k = child->index + 1;
+	else {
+		while (k < children.size() && children[k].get() != child) ++k;
+		if (k == children.size()) return nullptr;
+		++k;
 	}
+	for (; k < children.size(); ++k)
+		if (!nm || children[k]->name == nm) return children[k].get();
 	return nullptr;
 }
 
@@ -176,6 +181,7 @@ struct Parser {
 			}
 			auto c = std::make_unique<XmlElement>();
 			if (!element(*c)) return false;
+			c->index = e.children.size();
 			e.children.push_back(std::move(c));
 		}
 	}
@@ -192,6 +198,7 @@ bool XmlDocument::parse(const std::string& text)
 		if (p.eof()) break;
 		auto c = std::make_unique<XmlElement>();
 		if (!p.element(*c)) { error = p.err; return false; }
+		c->index = root.children.size();
 		root.children.push_back(std::move(c));
 	}
 	if (root.children.empty()) { error = "no element in document"; return false; }

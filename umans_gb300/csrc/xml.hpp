@@ -17,6 +17,7 @@ struct XmlElement {
 	std::string name;
 	std::vector<std::pair<std::string, std::string>> attrs;
 	std::vector<std::unique_ptr<XmlElement>> children;
+	size_t index = 0;   // position among its parent's children
 
 	const char* attr(const char* key) const;
 	// tinyxml2-style typed queries: true when the attribute exists and parses
