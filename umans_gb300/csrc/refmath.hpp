@@ -1,4 +1,13 @@
-// Reference-exact float exponential for the device.
+// Reference-exact arithmetic shared by the host and the device:
+//  * the host C library's expf (this header comment), sinf and cosf (the
+//    section "Reference-exact float sine and cosine" below), reproduced bit
+//    for bit on the device;
+//  * the reference's double line intersection without FP64 in the common
+//    case (getLineIntersection section);
+//  * the double Gaussians of TtcaDca rounded to float (exp_gauss).
+// Every part is float-float arithmetic with exact products (FMA on the
+// device, Dekker on the host), so host and device compute the same bits, and
+// falls back to the exact computation where its error bound cannot decide.
 //
 // The reference evaluates exp(float) with the host C library's expf
 // (SocialForcesAvoidance.cpp:98, PowerLaw.cpp:62, FOEAvoidance.cpp:82), and
