@@ -77,6 +77,11 @@ enum umans_status {
 
 /* CrowdSimulator::FromConfigFile (crowdSimulator.cpp:516-647) */
 int umans_create(const char* config_file, umans_sim** out);
+/* Loads a scenario file on the host only (no device work): its agent count
+ * (timed insertions included), policies and obstacle edges; the loader's
+ * errors (CrowdSimulator::FromConfigFile, crowdSimulator.cpp:516-647) through
+ * umans_last_error(NULL). */
+int umans_scenario_info(const char* config_file, int* agents, int* policies, int* edges);
 /* as umans_create; max_neighbours <= 0 and cells_per_range <= 0 pick defaults */
 int umans_create_ex(const char* config_file, int max_neighbours, float cells_per_range, int use_graph,
                     umans_sim** out);

@@ -1,36 +1,35 @@
-"""Scenario generation and the oracle's XML reader (CPU)."""
-import numpy as np
+"""The scenario loader of the engine library on the host (no device work):
+counts, errors, and a large agents block loading in linear time."""
+import time
 
-from oracle.port import read_scenario
-from umans_gb300 import scenarios as S
+import pytest
 
-
-def test_generators_are_seeded(tmp_path):
-    a = S.socialforces_toric(n=500, density=0.625).to_xml()
-    b = S.socialforces_toric(n=500, density=0.625).to_xml()
-    assert a == b
-    assert S.batch_counts().min() >= 8 and S.batch_counts().max() <= 2048
+from umans_gb300 import UmansError, scenario_info, scenarios as S
 
 
-def test_float32_roundtrip(tmp_path):
-    sc = S.socialforces_toric(n=200, density=0.625)
-    p = sc.write(str(tmp_path / "s.xml"))
-    r = read_scenario(p)
-    assert np.array_equal(r["pos"], sc.pos)
-    assert np.array_equal(r["goal"], sc.goal)
-    assert np.array_equal(r["pref_speed"], sc.pref_speed)
+def test_counts(tmp_path):
+    info = scenario_info(S.model_block_field("SocialForces").write(str(tmp_path / "b.xml")))
+    assert info == dict(agents=60, policies=1, edges=320)
+    info = scenario_info(S.model_arrivals("ORCA").write(str(tmp_path / "a.xml")))
+    assert info["agents"] == 40 and info["edges"] == 0
 
 
-def test_lenient_xml_like_tinyxml(tmp_path):
-    # a stray root element and a comment with '--' (both occur in the reference's examples)
-    (tmp_path / "agents.xml").write_text(
-        '<?xml version="1.0"?><Simulation delta_time="0.1"/>\n<Agents>\n<!------ x ------>\n'
-        '<Agent><pos x="1" y="2"/><goal x="3" y="4"/><Policy id="7"/></Agent></Agents>')
-    (tmp_path / "s.xml").write_text(
-        '<Simulation delta_time="0.1"><World type="Infinite"/><Policies>'
-        '<Policy id="7" OptimizationMethod="gradient"><costfunction name="NoSuchModel"/>'
-        '<costfunction name="GoalReachingForce"/></Policy></Policies>'
-        '<Agents file="agents.xml"/></Simulation>')
-    r = read_scenario(str(tmp_path / "s.xml"))
-    assert len(r["ids"]) == 1 and r["policies"][0].ncost == 1
-    assert np.isclose(r["radius"][0], 0.24)
+def test_large_agents_block_loads_in_linear_time(tmp_path):
+    path = S.karamouzas_corridor(200_000).write(str(tmp_path / "k.xml"))
+    t = time.perf_counter()
+    info = scenario_info(path)
+    t = time.perf_counter() - t
+    assert info["agents"] == 200_000
+    # a sibling walk restarted from the first child made this quadratic
+    # (about 9 s on one x86 core); linear it is well below a second
+    assert t < 5.0, t
+
+
+def test_loader_errors(tmp_path):
+    p = tmp_path / "bad.xml"
+    p.write_text('<?xml version="1.0"?><Simulation delta_time="0.1"><World type="Infinite"/>'
+                 '<Agents><Agent><pos x="0" y="0"/><Policy id="0"/></Agent></Agents></Simulation>')
+    with pytest.raises(UmansError):
+        scenario_info(str(p))
+    with pytest.raises(UmansError):
+        scenario_info(str(tmp_path / "missing.xml"))

@@ -255,6 +255,17 @@ class Simulation:
         self._check(self._lib.umans_diff_end(self._h))
 
 
+def scenario_info(config_file: str) -> dict:
+    """Loads a scenario file on the host only: agents (timed insertions
+    included), policies and obstacle edges.  Raises UmansError with the
+    loader's message when the file would not load."""
+    lib = _lib.load()
+    a, p, e = C.c_int(), C.c_int(), C.c_int()
+    if lib.umans_scenario_info(os.fsencode(config_file), C.byref(a), C.byref(p), C.byref(e)) != 0:
+        raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+    return dict(agents=a.value, policies=p.value, edges=e.value)
+
+
 def read_trajectory(path: str):
     """Chunks of a trajectory.bin written by Simulation.record_start(binary=True):
     a list of (ids[n], times[steps], xy[steps, n, 2])."""

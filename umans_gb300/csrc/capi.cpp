@@ -54,6 +54,18 @@ int umans_create_ex(const char* config_file, int max_neighbours, float cells_per
 	return UMANS_OK;
 }
 
+int umans_scenario_info(const char* config_file, int* agents, int* policies, int* edges)
+{
+	if (!config_file) return fail(nullptr, UMANS_ERR_ARGUMENT, "null argument");
+	umans::Scenario sc;
+	std::string err;
+	if (!umans::load_scenario(config_file, sc, err)) return fail(nullptr, UMANS_ERR_LOAD, err);
+	if (agents) *agents = (int)sc.agents.size();
+	if (policies) *policies = (int)sc.policies.size();
+	if (edges) *edges = (int)sc.edges.size();
+	return UMANS_OK;
+}
+
 int umans_batch_create(const char* const* config_files, int n, umans_sim** out)
 {
 	if (!config_files || n <= 0 || !out) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
