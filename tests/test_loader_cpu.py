@@ -25,6 +25,23 @@ def test_large_agents_block_loads_in_linear_time(tmp_path):
     assert t < 5.0, t
 
 
+def test_cost_function_plugin_names(tmp_path):
+    """A policy whose only cost function is a plugin loads; an unknown name
+    is skipped with a warning, which leaves that policy without costs."""
+    def scen(cost):
+        return ('<?xml version="1.0"?><Simulation delta_time="0.1"><World type="Infinite"/>'
+                '<Policies><Policy id="0" OptimizationMethod="sampling">'
+                f'<costfunction name="{cost}" range="5" w="2"/></Policy></Policies>'
+                '<Agents><Agent><pos x="0" y="0"/><goal x="5" y="0"/><Policy id="0"/></Agent></Agents>'
+                '</Simulation>')
+    p = tmp_path / "plugin.xml"
+    p.write_text(scen("ExampleRVO"))
+    assert scenario_info(str(p)) == dict(agents=1, policies=1, edges=0)
+    p.write_text(scen("NoSuchCost"))
+    with pytest.raises(UmansError, match="cost function"):
+        scenario_info(str(p))
+
+
 def test_loader_errors(tmp_path):
     p = tmp_path / "bad.xml"
     p.write_text('<?xml version="1.0"?><Simulation delta_time="0.1"><World type="Infinite"/>'

@@ -32,6 +32,7 @@
 #include "costs.cuh"
 #include "orca.cuh"
 #include "adjoint.cuh"
+#include "plugins.cuh"
 
 namespace umans {
 
@@ -1105,6 +1106,7 @@ __device__ float eval_cost(const AgentCtx& A, const NbView& N, const CostDesc& c
 	case K_FOE: return cost_foe(A, N, c, v);
 	case K_GENERIC: return 0;   // GenericCost::GetCost: GenericCost.cpp:27-31
 	}
+	if (c.kind >= K_PLUGIN0) return plugin_cost(c.kind - K_PLUGIN0, A, N, c, v);
 	return 0;
 }
 

@@ -14,7 +14,8 @@ namespace umans {
 
 enum CostKind : int {
 	K_ORCA = 0, K_RVO, K_SOCIALFORCES, K_POWERLAW, K_GOALREACHING, K_KARAMOUZAS,
-	K_MOUSSAID, K_PARIS, K_VANTOLL, K_TTCADCA, K_FOE, K_PLEDESTRIANS, K_RANDOM, K_GENERIC, K_NUM_KINDS
+	K_MOUSSAID, K_PARIS, K_VANTOLL, K_TTCADCA, K_FOE, K_PLEDESTRIANS, K_RANDOM, K_GENERIC, K_NUM_KINDS,
+	K_PLUGIN0 = K_NUM_KINDS   // cost-function plugins: K_PLUGIN0 + index in kPlugins (plugins.hpp)
 };
 enum Method : int { M_GRADIENT = 0, M_SAMPLING = 1, M_GLOBAL = 2 };
 enum WorldType : int { W_INFINITE = 0, W_TORIC = 1 };

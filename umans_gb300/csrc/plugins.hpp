@@ -1,0 +1,41 @@
+// Cost-function plugins: the engine's counterpart of the reference's
+// CostFunction plugin API (src/Engine/core/costFunction.h:155-194: GetCost,
+// parseParameters, GetName; registration with registerCostFunction<T>(),
+// src/Engine/core/costFunctionFactory.h:44-53 and .cpp:41-61).
+//
+// A plugin has two parts, both added to the library at build time:
+//  * a host table entry below (kPlugins in plugins.cpp): the name a
+//    <costfunction name="..."/> element uses (GetName), and its parameters:
+//    XML attribute, slot in CostDesc::p, default (parseParameters); `range`
+//    and `coeff` are read for every cost function;
+//  * a device function in plugins.cuh, dispatched by plugin_cost():
+//      __device__ float cost(const AgentCtx& A, const NbView& N,
+//                            const CostDesc& c, float2 v);   // GetCost
+//    with the agent (A), its neighbour and obstacle lists (N) and the
+//    candidate velocity v, using the helpers of costs.cuh (time to first
+//    collision, closest approach, ...).
+// A plugin cost is evaluated inside the agent kernel like the built-in
+// per-sample costs: on every candidate of the sampling method, through the
+// default sampling of the global method (policy.h:74-86), and through the
+// default finite-difference gradient (costFunction.cpp:36-54) of the
+// gradient method.  Its kind is K_PLUGIN0 + its index in kPlugins.
+#pragma once
+
+namespace umans {
+
+struct PluginParam {
+	const char* attr;   // XML attribute
+	int slot;           // CostDesc::p index
+	float dflt;         // default value
+};
+
+struct PluginInfo {
+	const char* name;
+	const PluginParam* params;
+	int nparams;
+};
+
+extern const PluginInfo kPlugins[];
+extern const int kNumPlugins;
+
+}  // namespace umans

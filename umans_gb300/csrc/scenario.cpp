@@ -1,4 +1,5 @@
 #include "scenario.hpp"
+#include "plugins.hpp"
 
 #include <cfloat>
 #include <cmath>
@@ -15,12 +16,19 @@ static const char* KIND_NAMES[K_NUM_KINDS] = {
 	"ORCA", "RVO", "SocialForcesAvoidance", "PowerLaw", "GoalReachingForce", "Karamouzas",
 	"Moussaid", "Paris", "VanToll", "TtcaDca", "FOEAvoidance", "PLEdestrians", "RandomFunction", "Generic"};
 
-const char* cost_kind_name(int kind) { return (kind >= 0 && kind < K_NUM_KINDS) ? KIND_NAMES[kind] : "?"; }
+const char* cost_kind_name(int kind)
+{
+	if (kind >= 0 && kind < K_NUM_KINDS) return KIND_NAMES[kind];
+	if (kind >= K_PLUGIN0 && kind < K_PLUGIN0 + kNumPlugins) return kPlugins[kind - K_PLUGIN0].name;
+	return "?";
+}
 
 int cost_kind_from_name(const std::string& name)
 {
 	for (int k = 0; k < K_NUM_KINDS; ++k)
 		if (name == KIND_NAMES[k]) return k;
+	for (int k = 0; k < kNumPlugins; ++k)   // costFunctionFactory.cpp:41-61: registered plugins by name
+		if (name == kPlugins[k].name) return K_PLUGIN0 + k;
 	return -1;
 }
 
@@ -44,7 +52,12 @@ void cost_defaults(int kind, CostDesc& c)
 	case K_TTCADCA: c.p[0] = 2; c.p[1] = 2; c.p[2] = 1; c.p[3] = 0.3f; break;
 	case K_PLEDESTRIANS: c.p[0] = 2.23f; c.p[1] = 1.26f; c.p[2] = 0.5f; c.p[3] = 3; break;
 	case K_RANDOM: c.range = 0; break;                                 // RandomFunction.h: range_ = 0
-	default: break;
+	default:
+		if (kind >= K_PLUGIN0 && kind < K_PLUGIN0 + kNumPlugins) {
+			const PluginInfo& pl = kPlugins[kind - K_PLUGIN0];
+			for (int k = 0; k < pl.nparams; ++k) c.p[pl.params[k].slot] = pl.params[k].dflt;
+		}
+		break;
 	}
 }
 
@@ -70,7 +83,12 @@ static void parse_cost_params(const XmlElement* e, CostDesc& c)
 	case K_VANTOLL: rd("max_distance", 0); break;
 	case K_TTCADCA: rd("sigmaAngle_goal", 0); rd("sigmaSpeed_goal", 1); rd("sigmaTtca", 2); rd("sigmaDca", 3); break;
 	case K_PLEDESTRIANS: rd("w_a", 0); rd("w_b", 1); rd("t_min", 2); rd("t_max", 3); break;
-	default: break;
+	default:
+		if (c.kind >= K_PLUGIN0 && c.kind < K_PLUGIN0 + kNumPlugins) {
+			const PluginInfo& pl = kPlugins[c.kind - K_PLUGIN0];
+			for (int k = 0; k < pl.nparams; ++k) rd(pl.params[k].attr, pl.params[k].slot);
+		}
+		break;
 	}
 }
 
