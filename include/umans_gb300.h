@@ -82,6 +82,12 @@ int umans_create(const char* config_file, umans_sim** out);
  * errors (CrowdSimulator::FromConfigFile, crowdSimulator.cpp:516-647) through
  * umans_last_error(NULL). */
 int umans_scenario_info(const char* config_file, int* agents, int* policies, int* edges);
+/* The cost-function names a policy's <costfunction name="..."/> may use: the
+ * built-in costs, then the compiled-in plugins (the names registered with
+ * CostFunctionFactory, costFunctionFactory.cpp:41-61).  Writes up to cap
+ * pointers to static strings into names (may be NULL when cap is 0) and the
+ * total count into *n. */
+int umans_cost_functions(const char** names, int cap, int* n);
 /* as umans_create; max_neighbours <= 0 and cells_per_range <= 0 pick defaults */
 int umans_create_ex(const char* config_file, int max_neighbours, float cells_per_range, int use_graph,
                     umans_sim** out);

@@ -266,6 +266,19 @@ def scenario_info(config_file: str) -> dict:
     return dict(agents=a.value, policies=p.value, edges=e.value)
 
 
+def cost_functions() -> list:
+    """Names a policy's cost functions may use: the built-in costs, then the
+    compiled-in plugins (the reference's CostFunctionFactory registry)."""
+    lib = _lib.load()
+    n = C.c_int()
+    if lib.umans_cost_functions(None, 0, C.byref(n)) != 0:
+        raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+    buf = (C.c_char_p * n.value)()
+    if lib.umans_cost_functions(buf, n.value, C.byref(n)) != 0:
+        raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+    return [b.decode() for b in buf]
+
+
 def read_trajectory(path: str):
     """Chunks of a trajectory.bin written by Simulation.record_start(binary=True):
     a list of (ids[n], times[steps], xy[steps, n, 2])."""

@@ -66,6 +66,15 @@ int umans_scenario_info(const char* config_file, int* agents, int* policies, int
 	return UMANS_OK;
 }
 
+int umans_cost_functions(const char** names, int cap, int* n)
+{
+	if (!n || cap < 0 || (cap > 0 && !names)) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	const int total = umans::cost_function_count();
+	for (int k = 0; k < total && k < cap; ++k) names[k] = umans::cost_function_name(k);
+	*n = total;
+	return UMANS_OK;
+}
+
 int umans_batch_create(const char* const* config_files, int n, umans_sim** out)
 {
 	if (!config_files || n <= 0 || !out) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");

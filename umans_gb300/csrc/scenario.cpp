@@ -23,6 +23,14 @@ const char* cost_kind_name(int kind)
 	return "?";
 }
 
+int cost_function_count() { return K_NUM_KINDS + kNumPlugins; }
+
+const char* cost_function_name(int index)
+{
+	if (index < 0 || index >= cost_function_count()) return nullptr;
+	return cost_kind_name(index < K_NUM_KINDS ? index : K_PLUGIN0 + (index - K_NUM_KINDS));
+}
+
 int cost_kind_from_name(const std::string& name)
 {
 	for (int k = 0; k < K_NUM_KINDS; ++k)

@@ -43,5 +43,8 @@ void cost_defaults(int kind, CostDesc& c);
 // names the reference registers but this engine does not run.
 int cost_kind_from_name(const std::string& name);
 const char* cost_kind_name(int kind);
+// every registered cost-function name: built-in kinds, then plugins
+int cost_function_count();
+const char* cost_function_name(int index);
 
 }  // namespace umans

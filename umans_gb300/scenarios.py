@@ -75,7 +75,7 @@ class Scenario:
     width: float = 0.0
     height: float = 0.0
     end_time: float | None = None
-    policies: list[str] = field(default_factory=list)
+    policies: list = field(default_factory=list)   # <Policy> XML strings or policy.Policy objects
     pos: np.ndarray = None          # (n, 2) float32
     goal: np.ndarray = None         # (n, 2) float32
     radius: np.ndarray = None       # (n,) float32
@@ -101,7 +101,8 @@ class Scenario:
         end = f' end_time="{_f(self.end_time)}"' if self.end_time is not None else ""
         out = ['<?xml version="1.0" encoding="utf-8"?>',
                f'<Simulation delta_time="{_f(self.dt)}"{end}>', w,
-               "<Policies>", *self.policies, "</Policies>", "<Agents>"]
+               "<Policies>", *(p if isinstance(p, str) else p.to_xml() for p in self.policies),
+               "</Policies>", "<Agents>"]
         for i in range(self.n):
             extra = ""
             if self.start_time is not None and self.start_time[i] != 0:
