@@ -1,5 +1,9 @@
 """The scenario loader of the engine library on the host (no device work):
 counts, errors, and a large agents block loading in linear time."""
+import os
+import subprocess
+import sys
+import textwrap
 import time
 
 import pytest
@@ -50,3 +54,46 @@ def test_loader_errors(tmp_path):
         scenario_info(str(p))
     with pytest.raises(UmansError):
         scenario_info(str(tmp_path / "missing.xml"))
+
+
+_MUTATE = textwrap.dedent("""
+    import ctypes as C, random, sys
+    from umans_gb300 import _lib, scenarios as S
+    lib = _lib.load()
+    rng = random.Random(int(sys.argv[1]))
+    base = [S.model_block_field("SocialForces").to_xml().encode(),
+            S.model_arrivals("ORCA").to_xml().encode(),
+            S.model_toric_obstacle("RVO").to_xml().encode()]
+    toks = [b"<", b">", b"/", b'"', b"=", b"<!--", b"-->", b"<?", b"?>", b"&amp;", b"&", b"\\x00",
+            b"nan", b"inf", b"-1e39", b"<Agent>", b"</Agent>", b'<Policy id="0">', b"</Policy>",
+            b"<Obstacle>", b'<Point x="1" y="1"/>', b'id="-5"', b'width="0"', b'delta_time="0"',
+            b"<![CDATA[", b'SpeedSamples="-3"', b"<costfunction/>"]
+    a, p, e = C.c_int(), C.c_int(), C.c_int()
+    loaded = 0
+    for it in range(int(sys.argv[2])):
+        d = bytearray(rng.choice(base))
+        for _ in range(rng.randint(1, 6)):
+            op, pos = rng.random(), rng.randrange(len(d) + 1)
+            if op < 0.35: del d[pos:pos + rng.randint(1, 40)]
+            elif op < 0.7: d[pos:pos] = rng.choice(toks)
+            elif len(d): d[pos % len(d)] = rng.randrange(256)
+        if rng.random() < 0.1: d = d[:rng.randrange(len(d) + 1)]
+        with open(sys.argv[3], "wb") as fh: fh.write(bytes(d))
+        rc = lib.umans_scenario_info(sys.argv[3].encode(), C.byref(a), C.byref(p), C.byref(e))
+        assert rc in (0, 2), rc   # UMANS_OK or UMANS_ERR_LOAD
+        loaded += rc == 0
+    print("loaded", loaded)
+""")
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_mutated_files_load_or_fail_cleanly(seed, tmp_path):
+    """Seeded byte-level mutations of valid scenario files (deleted spans,
+    inserted markup, flipped bytes, truncation): the native loader either
+    loads or returns an error status, never crashes.  Runs in a child process
+    so that a crash fails this test only."""
+    env = dict(os.environ, PYTHONPATH=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    r = subprocess.run([sys.executable, "-c", _MUTATE, str(seed), "400", str(tmp_path / "m.xml")],
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.startswith("loaded")
