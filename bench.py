@@ -17,6 +17,7 @@ cross-scenario exchange) and rank 0 reports the aggregate.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes as C
 import json
 import math
@@ -384,11 +385,29 @@ def replica_rate(world: int, agents: int, steps: int, seconds: float) -> float:
     return world * agents * steps / seconds
 
 
+@contextlib.contextmanager
+def native_stdout_to_stderr():
+    """Sends what native code writes to standard output (the reference engine
+    reports world creation there) to standard error, so that standard output
+    carries the JSON line alone."""
+    libc = C.CDLL(None)
+    sys.stdout.flush()
+    saved = os.dup(1)
+    os.dup2(2, 1)
+    try:
+        yield
+    finally:
+        libc.fflush(None)
+        sys.stdout.flush()
+        os.dup2(saved, 1)
+        os.close(saved)
+
+
 def run_reference(args):
     rank, world, local, dist = dist_setup(args)
     if rank != 0:
         return
-    with tempfile.TemporaryDirectory() as tmp:
+    with tempfile.TemporaryDirectory() as tmp, native_stdout_to_stderr():
         path, n, cfg = workload(args.workload, tmp, args.agents)
         threads = os.cpu_count() or 1
         from oracle import ref as oref
@@ -408,7 +427,7 @@ def run_reference(args):
                                  "sample": f"{args.steps} steps of the full workload after {args.warmup} warm-up"},
                 "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+    print(json.dumps(line))
 
 
 def run_ours(args):
