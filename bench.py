@@ -328,18 +328,19 @@ def cpu_baseline(path: str, n_agents: int, seconds: float = 30.0, threads: int |
     restatement) on all host cores, over a bounded number of steps."""
     threads = threads or os.cpu_count() or 1
     from oracle import ref as oref
-    if oref.available():
-        sim = oref.RefSim(path, threads=threads)
-        kind = "reference"
-    else:
-        from oracle.port import PortSim
-        sim = PortSim(path, threads=threads)
-        kind = "port"
-    t1 = sim.step(1)
-    # the per-step cost grows as the crowd condenses: time the same step range
-    # as the GPU when the budget allows
-    steps = max(1, min(max_steps, int(seconds / max(t1, 1e-6) / 1.3)))
-    t = sim.step(steps)
+    with native_stdout_to_stderr():
+        if oref.available():
+            sim = oref.RefSim(path, threads=threads)
+            kind = "reference"
+        else:
+            from oracle.port import PortSim
+            sim = PortSim(path, threads=threads)
+            kind = "port"
+        t1 = sim.step(1)
+        # the per-step cost grows as the crowd condenses: time the same step
+        # range as the GPU when the budget allows
+        steps = max(1, min(max_steps, int(seconds / max(t1, 1e-6) / 1.3)))
+        t = sim.step(steps)
     return dict(value=n_agents * steps / t, unit="agent-steps/s", cores=threads, kind=kind,
                 sample=f"{steps} steps of the full {n_agents}-agent workload after 1 warm-up step")
 
