@@ -1,12 +1,24 @@
 // Host tables of the cost-function plugins (plugins.hpp).
 #include "plugins.hpp"
 
+#include "model.hpp"
+
 namespace umans {
+
+// every parameter slot indexes CostDesc::p
+template <int N>
+constexpr bool slots_in_range(const PluginParam (&params)[N])
+{
+	for (int k = 0; k < N; ++k)
+		if (params[k].slot < 0 || params[k].slot >= (int)(sizeof(CostDesc::p) / sizeof(float))) return false;
+	return true;
+}
 
 // ExampleRVO: the reference's RVO cost (RVO.cpp:28-44, parameter "w",
 // RVO.h:53) written as a plugin; a policy naming it behaves exactly as one
 // naming "RVO".
-static const PluginParam kExampleRvoParams[] = { { "w", 0, 1.0f } };
+static constexpr PluginParam kExampleRvoParams[] = { { "w", 0, 1.0f } };
+static_assert(slots_in_range(kExampleRvoParams), "ExampleRVO parameter slot outside CostDesc::p");
 
 const PluginInfo kPlugins[] = {
 	{ "ExampleRVO", kExampleRvoParams, 1 },

@@ -25,7 +25,7 @@ namespace umans {
 
 struct PluginParam {
 	const char* attr;   // XML attribute
-	int slot;           // CostDesc::p index
+	int slot;           // CostDesc::p index (0..7, checked at compile time in plugins.cpp)
 	float dflt;         // default value
 };
 
