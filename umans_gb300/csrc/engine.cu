@@ -2063,7 +2063,8 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	bool need_exp = false;
 	for (const auto& p : pols_)
 		for (int c = 0; c < p.ncost; ++c)
-			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE;
+			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE ||
+			            p.cost[c].kind >= K_PLUGIN0;   // a plugin may call ref_expf
 	if (need_exp && !exp_exceptions_for_device(&d_->expx, nullptr, err_)) return false;
 	// kernel groups: scenarios whose policies are all gradient + force-based
 	// costs (k_agent<1>), scenarios with an ORCA cost, the others
@@ -2122,7 +2123,9 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	// rotations of TtcaDca and FOEAvoidance, the segment collision times
 	bool need_trig = need_trig_ || !edges_.empty();
 	for (const auto& p : pols_)
-		for (int c = 0; c < p.ncost; ++c) need_trig |= p.cost[c].kind == K_TTCADCA || p.cost[c].kind == K_FOE;
+		for (int c = 0; c < p.ncost; ++c)
+			need_trig |= p.cost[c].kind == K_TTCADCA || p.cost[c].kind == K_FOE ||
+			             p.cost[c].kind >= K_PLUGIN0;   // a plugin may call host_sinf / host_sincosf
 	if (need_trig && !set_device_sincos(err_)) return false;
 	if (!alloc(std::max(n_, 16))) return false;
 	if (!upload_all()) return false;

@@ -13,7 +13,9 @@
 //                            const CostDesc& c, float2 v);   // GetCost
 //    with the agent (A), its neighbour and obstacle lists (N) and the
 //    candidate velocity v, using the helpers of costs.cuh (time to first
-//    collision, closest approach, ...).
+//    collision, closest approach, ...) and the host-exact libm functions
+//    (ref_expf(A.ex, x), host_sinf, host_sincosf), whose tables the engine
+//    uploads for every scenario with a plugin cost.
 // A plugin cost is evaluated inside the agent kernel like the built-in
 // per-sample costs: on every candidate of the sampling method, through the
 // default sampling of the global method (policy.h:74-86), and through the
