@@ -82,6 +82,13 @@ int umans_create(const char* config_file, umans_sim** out);
  * errors (CrowdSimulator::FromConfigFile, crowdSimulator.cpp:516-647) through
  * umans_last_error(NULL). */
 int umans_scenario_info(const char* config_file, int* agents, int* policies, int* edges);
+/* The loader's warnings for a scenario file (host only), one per line: the
+ * messages the reference writes to standard error while loading (an invalid
+ * sampling attribute, an unknown cost function, an agent without a goal, an
+ * unknown world type; crowdSimulator.cpp:344-400, 516-647).  Writes up to
+ * cap-1 bytes and a terminating NUL into text (may be NULL when cap is 0);
+ * *needed receives the full length plus one. */
+int umans_scenario_warnings(const char* config_file, char* text, int cap, int* needed);
 /* The cost-function names a policy's <costfunction name="..."/> may use: the
  * built-in costs, then the compiled-in plugins (the names registered with
  * CostFunctionFactory, costFunctionFactory.cpp:41-61).  Writes up to cap

@@ -8,7 +8,7 @@ import time
 
 import pytest
 
-from umans_gb300 import UmansError, scenario_info, scenarios as S
+from umans_gb300 import UmansError, scenario_info, scenario_warnings, scenarios as S
 
 
 def test_counts(tmp_path):
@@ -44,6 +44,31 @@ def test_cost_function_plugin_names(tmp_path):
     p.write_text(scen("NoSuchCost"))
     with pytest.raises(UmansError, match="cost function"):
         scenario_info(str(p))
+
+
+def test_loader_warnings(tmp_path):
+    """Recoverable problems load with the reference's defaults and are
+    reported as warnings (crowdSimulator.cpp:344-400)."""
+    p = tmp_path / "w.xml"
+    p.write_text('<?xml version="1.0"?><Simulation delta_time="0.1"><World type="Spherical"/>'
+                 '<Policies><Policy id="3" OptimizationMethod="sampling" SamplingType="jittered">'
+                 '<costfunction name="RVO"/><costfunction name="NoSuchCost"/></Policy></Policies>'
+                 '<Agents><Agent><pos x="0" y="0"/><Policy id="3"/></Agent></Agents></Simulation>')
+    w = scenario_warnings(str(p))
+    assert "Policy 3: sampling type invalid, using default (regular)" in w
+    assert "Policy 3: unknown cost function NoSuchCost ignored" in w
+    assert "agent has no goal element and will not move" in w
+    assert "no valid world type; using Infinite" in w
+    assert scenario_warnings(S.model_crossing("RVO").write(str(tmp_path / "ok.xml"))) == []
+    # a short buffer is filled and terminated, the full size reported
+    import ctypes as C
+    from umans_gb300 import _lib
+    buf, need = C.create_string_buffer(b"\xff" * 8), C.c_int()
+    assert _lib.load().umans_scenario_warnings(str(p).encode(), buf, 6, C.byref(need)) == 0
+    assert buf.raw[:6] == w[0].encode()[:5] + b"\0" and buf.raw[6:8] == b"\xff\xff"
+    assert need.value == len("\n".join(w)) + 2
+    with pytest.raises(UmansError):
+        scenario_warnings(str(tmp_path / "missing.xml"))
 
 
 def test_loader_errors(tmp_path):

@@ -13,7 +13,8 @@ Python host mirror of the reference's interfaces:
 Both call the CUDA engine through the C ABI (include/umans_gb300.h).
 """
 from ._lib import AgentData  # noqa: F401
-from .api import UMANS, Batch, Simulation, UmansError, cost_functions, read_trajectory, scenario_info  # noqa: F401
+from .api import (UMANS, Batch, Simulation, UmansError, cost_functions, read_trajectory,  # noqa: F401
+                  scenario_info, scenario_warnings)
 from .policy import Policy, SamplingParameters  # noqa: F401
 
 __all__ = ["UMANS", "Simulation", "Batch", "UmansError", "AgentData", "read_trajectory"]

@@ -66,6 +66,7 @@ _SIGS = {
     "umans_profile_counters": (C.c_int, [P, P, C.c_int]),
     "umans_scenario_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "umans_cost_functions": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_int)]),
+    "umans_scenario_warnings": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
     "umans_diff_begin": (C.c_int, [P, C.c_int, C.c_int, P, C.c_float]),
     "umans_diff_forward": (C.c_int, [P, C.POINTER(C.c_double)]),
     "umans_diff_backward": (C.c_int, [P, P, P, P]),

@@ -266,6 +266,20 @@ def scenario_info(config_file: str) -> dict:
     return dict(agents=a.value, policies=p.value, edges=e.value)
 
 
+def scenario_warnings(config_file: str) -> list:
+    """The loader's warnings for a scenario file (host only): what the
+    reference reports on standard error while loading it."""
+    lib = _lib.load()
+    need = C.c_int()
+    path = os.fsencode(config_file)
+    if lib.umans_scenario_warnings(path, None, 0, C.byref(need)) != 0:
+        raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+    buf = C.create_string_buffer(need.value)
+    if lib.umans_scenario_warnings(path, buf, need.value, C.byref(need)) != 0:
+        raise UmansError(lib.umans_last_error(None).decode(errors="replace"))
+    return [w for w in buf.value.decode(errors="replace").split("\n") if w]
+
+
 def cost_functions() -> list:
     """Names a policy's cost functions may use: the built-in costs, then the
     compiled-in plugins (the reference's CostFunctionFactory registry)."""

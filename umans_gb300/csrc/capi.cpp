@@ -3,6 +3,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -63,6 +64,24 @@ int umans_scenario_info(const char* config_file, int* agents, int* policies, int
 	if (agents) *agents = (int)sc.agents.size();
 	if (policies) *policies = (int)sc.policies.size();
 	if (edges) *edges = (int)sc.edges.size();
+	return UMANS_OK;
+}
+
+int umans_scenario_warnings(const char* config_file, char* text, int cap, int* needed)
+{
+	if (!config_file || !needed || cap < 0 || (cap > 0 && !text))
+		return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	umans::Scenario sc;
+	std::string err;
+	if (!umans::load_scenario(config_file, sc, err)) return fail(nullptr, UMANS_ERR_LOAD, err);
+	std::string all;
+	for (const auto& w : sc.warnings) all += w + "\n";
+	*needed = (int)all.size() + 1;
+	if (cap > 0) {
+		const size_t k = std::min(all.size(), (size_t)cap - 1);
+		std::memcpy(text, all.data(), k);
+		text[k] = 0;
+	}
 	return UMANS_OK;
 }
 

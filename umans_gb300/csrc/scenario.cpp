@@ -138,24 +138,24 @@ struct Loader {
 			if (const char* a = pe->attr("SamplingType")) {
 				v = a;
 				if (v == "regular") p.s_type = 0; else if (v == "random") p.s_type = 1;
-				else s.warnings.push_back("sampling type invalid, using default (regular)");
+				else s.warnings.push_back("Policy " + std::to_string(pid) + ": sampling type invalid, using default (regular)");
 			}
 			if (const char* a = pe->attr("SamplingBase")) {
 				v = a;
 				if (v == "zero") p.s_base = 0; else if (v == "current velocity") p.s_base = 1;
-				else s.warnings.push_back("sampling base invalid, using default (zero)");
+				else s.warnings.push_back("Policy " + std::to_string(pid) + ": sampling base invalid, using default (zero)");
 			}
 			if (const char* a = pe->attr("SamplingBaseDirection")) {
 				v = a;
 				if (v == "unit") p.s_dir = 0; else if (v == "current velocity") p.s_dir = 1;
 				else if (v == "preferred velocity") p.s_dir = 2;
-				else s.warnings.push_back("sampling base direction invalid, using default");
+				else s.warnings.push_back("Policy " + std::to_string(pid) + ": sampling base direction invalid, using default");
 			}
 			if (const char* a = pe->attr("SamplingRadius")) {
 				v = a;
 				if (v == "preferred speed") p.s_radius = 0; else if (v == "maximum speed") p.s_radius = 1;
 				else if (v == "maximum acceleration") p.s_radius = 2;
-				else s.warnings.push_back("sampling radius type invalid, using default");
+				else s.warnings.push_back("Policy " + std::to_string(pid) + ": sampling radius type invalid, using default");
 			}
 		}
 		p.relax_time = 0;
@@ -176,7 +176,7 @@ struct Loader {
 				parse_cost_params(fe, c);
 				p.ncost++;
 			} else {
-				s.warnings.push_back(std::string("unknown cost function ") + (nm ? nm : "(null)") + " ignored");
+				s.warnings.push_back("Policy " + std::to_string(pid) + ": unknown cost function " + std::string(nm ? nm : "(null)") + " ignored");
 			}
 			fe = pe->next_sibling(fe);
 		}
