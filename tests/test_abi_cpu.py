@@ -47,3 +47,43 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.load()
+
+
+_C_CALLER = r"""
+#include <stdio.h>
+#include "umans_gb300.h"
+int main(int argc, char** argv) {
+    if (argc < 2) return 9;
+    const char* names[64]; int n = 0;
+    if (umans_cost_functions(names, 64, &n) != UMANS_OK) return 1;
+    int a = 0, p = 0, e = 0;
+    if (umans_scenario_info(argv[1], &a, &p, &e) != UMANS_OK) return 2;
+    char w[256]; int need = 0;
+    if (umans_scenario_warnings(argv[1], w, (int)sizeof w, &need) != UMANS_OK) return 3;
+    printf("%d %s %d %d %d %d\n", n, names[0], a, p, e, need);
+    return 0;
+}
+"""
+
+
+def test_header_is_c99_and_links_from_c(tmp_path):
+    """The header compiles as pedantic C99 (what a C or cgo caller sees) and a
+    C program linked against the library makes the host-only calls."""
+    import shutil
+    import subprocess
+    from umans_gb300 import scenarios as S
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no gcc")
+    lib_dir = os.path.dirname(build.build())
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(_C_CALLER)
+    subprocess.check_call([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                           "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                           "-L", lib_dir, "-lumans_gb300", "-Wl,-rpath," + lib_dir])
+    xml = S.model_crossing("RVO").write(str(tmp_path / "c.xml"))
+    r = subprocess.run([str(exe), xml], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    n, first, agents, policies, edges, need = r.stdout.split()
+    assert first == "ORCA" and int(n) >= 15
+    assert (int(agents), int(policies), int(edges), int(need)) == (40, 1, 0, 1)
