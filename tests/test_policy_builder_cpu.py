@@ -83,3 +83,24 @@ def test_builder_errors():
         p.add_cost_function("GoalReachingForce")
     with pytest.raises(ValueError, match="at least one cost function"):
         Policy(1, "global").to_xml()
+
+
+def test_built_policies_simulate_like_templates(tmp_path):
+    """The same crowd under the Karamouzas sampling policy written from its
+    template and built in code: identical oracle trajectories."""
+    from oracle.port import PortSim
+    a = S.model_crossing("RVO")
+    a.policies = [S.KARAMOUZAS_POLICY.format(pid=0)]
+    b = S.model_crossing("RVO")
+    b.policies = [Policy(0, "sampling", SamplingParameters(type="regular", base="zero",
+                                                           base_direction="preferred velocity", angle=180,
+                                                           speed_samples=10, angle_samples=20,
+                                                           include_base_as_sample=True, radius="maximum speed"),
+                         relaxation_time=0).add_cost_function("Karamouzas", range=10)]
+    sa = PortSim(a.write(str(tmp_path / "a.xml")), threads=2)
+    sb = PortSim(b.write(str(tmp_path / "b.xml")), threads=2)
+    sa.step(30)
+    sb.step(30)
+    pa, pb = sa.state()["pos"], sb.state()["pos"]
+    assert np.array_equal(pa, pb)
+    assert float(np.abs(pa - a.pos).max()) > 0.5   # the crowd moved
