@@ -87,3 +87,13 @@ def test_header_is_c99_and_links_from_c(tmp_path):
     n, first, agents, policies, edges, need = r.stdout.split()
     assert first == "ORCA" and int(n) >= 15
     assert (int(agents), int(policies), int(edges), int(need)) == (40, 1, 0, 1)
+
+
+def test_cost_function_listing_respects_capacity():
+    lib = _lib.load()
+    buf, n = (ctypes.c_char_p * 4)(), ctypes.c_int()
+    buf[3] = b"untouched"
+    assert lib.umans_cost_functions(buf, 3, ctypes.byref(n)) == 0
+    assert n.value >= 15 and [buf[k] for k in range(4)] == [b"ORCA", b"RVO", b"SocialForcesAvoidance",
+                                                              b"untouched"]
+    assert lib.umans_cost_functions(None, 1, ctypes.byref(n)) != 0   # names required when cap > 0
