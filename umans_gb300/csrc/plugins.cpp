@@ -24,5 +24,6 @@ const PluginInfo kPlugins[] = {
 	{ "ExampleRVO", kExampleRvoParams, 1 },
 };
 const int kNumPlugins = (int)(sizeof(kPlugins) / sizeof(kPlugins[0]));
+static_assert(sizeof(kPlugins) / sizeof(kPlugins[0]) == kPluginCount, "kPluginCount must count kPlugins");
 
 }  // namespace umans

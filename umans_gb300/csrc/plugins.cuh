@@ -2,6 +2,7 @@
 // entry of kPlugins, dispatched by index.
 #pragma once
 #include "costs.cuh"
+#include "plugins.hpp"
 
 namespace umans {
 
@@ -14,6 +15,8 @@ __device__ __forceinline__ float plugin_example_rvo(const AgentCtx& A, const NbV
 	const float minT = ttc_first(A, N, rv, c.range, true);
 	return c.p[0] / minT + vmag(vd);
 }
+
+static_assert(kPluginCount == 1, "plugin_cost needs one case per plugin: update both");
 
 __device__ __forceinline__ float plugin_cost(int index, const AgentCtx& A, const NbView& N, const CostDesc& c, float2 v)
 {

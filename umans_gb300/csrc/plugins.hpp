@@ -37,6 +37,10 @@ struct PluginInfo {
 	int nparams;
 };
 
+// the number of plugins: the length of kPlugins and the number of cases of
+// plugin_cost (plugins.cuh), both checked against it at compile time
+constexpr int kPluginCount = 1;
+
 extern const PluginInfo kPlugins[];
 extern const int kNumPlugins;
 
