@@ -136,6 +136,28 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def fp32_peak_tflops(sm_mhz: float) -> tuple[float, int]:
+    """Nominal FP32 peak of the device: SMs (read from the device) x 128 FP32
+    lanes x 2 FLOP (FMA) x the SM clock.  MEASURED_PEAKS.json holds no FP32
+    figure, so this is the denominator of the FP32 roofline."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12, sms
+
+
+def port_over_reference():
+    """Speed of the C restatement relative to the compiled reference on the
+    same workload, from the committed CPU measurement (profiles/), if any."""
+    p = os.path.join(ROOT, "profiles", "cpu_port_vs_reference.md")
+    try:
+        for line in open(p):
+            if line.startswith("port_over_reference:"):
+                return json.loads(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def profiled_traffic_per_agent():
     """dram bytes per agent of k_agent from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "k_agent_socialforces_toric.md")
@@ -174,24 +196,32 @@ def batched_leg(tmp: str, steps: int, warmup: int, flush, stream_of):
     t_ms = sum(a.elapsed_time(c) for a, c in evs)
     batched = total * steps / (t_ms / 1e3)
     b.close()
-    # plain path, one scenario after another (every 16th scenario)
+    # plain path, one scenario after another (every 16th scenario), timed
+    # with CUDA events on each simulation's stream like the batch (its steps
+    # are enqueued back to back; the flush of the batch timing is left out,
+    # which favours the plain path)
     sample = list(range(0, len(paths), 16))
-    plain_agent_steps, plain_s = 0, 0.0
+    plain_agent_steps, plain_ms = 0, 0.0
     psteps = 10
     for k in sample:
         sim = Simulation(paths[k])
         sim.step(2)
-        t0 = time.perf_counter()
-        sim.step(psteps)
-        plain_s += time.perf_counter() - t0
+        pst = torch.cuda.ExternalStream(sim.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(pst)
+        sim.step_async(psteps)
+        e1.record(pst)
+        sim.synchronize()
+        plain_ms += e0.elapsed_time(e1)
         plain_agent_steps += int(counts[k]) * psteps
         sim.close()
-    plain = plain_agent_steps / plain_s
+    plain = plain_agent_steps / (plain_ms / 1e3)
     return {"value": batched, "unit": "agent-steps/s", "scenarios": len(paths), "agents": total, "steps": steps,
             "ms_per_step": t_ms / steps, "autotune": tune,
             "plain_per_scenario": {"value": plain, "unit": "agent-steps/s",
                                    "sample": f"{len(sample)} of {len(paths)} scenarios (every 16th), {psteps} steps each, "
-                                             "one Simulation per scenario, sequentially"},
+                                             "one Simulation per scenario, sequentially",
+                                   "timing": "CUDA events on each simulation's stream, the same clock as the batch"},
             "speedup_vs_plain": batched / plain}
 
 
@@ -208,9 +238,14 @@ def diff_leg(tmp: str, sets: int = 256, n: int = 512, steps: int = 100, every: i
     held = S.calibration_set((2.52, 0.255, 1.65, 2.7), n=n).write(os.path.join(tmp, "held.xml"))
     h = Simulation(held)
     tg = np.empty((steps, n, 2), np.float32)
-    for t in range(steps):
-        h.step(1)
-        tg[t] = h.positions()
+    obs = {"pos": [], "vel": [], "viewdir": []}
+    for t in range(steps + 1):
+        st = h.state()
+        for k in obs:
+            obs[k].append(st[k].copy())
+        if t < steps:
+            h.step(1)
+            tg[t] = h.positions()
     h.close()
     paths = [S.calibration_set(params[k], n=n).write(os.path.join(tmp, f"cal_{k}.xml")) for k in range(sets)]
     b = Batch(paths)
@@ -236,7 +271,48 @@ def diff_leg(tmp: str, sets: int = 256, n: int = 512, steps: int = 100, every: i
         b.synchronize()
         if r:
             plain.append(time.perf_counter() - t0)
+    # windowed calibration (multiple shooting): windows of `every` steps, each
+    # from the observed state at its start
+    from umans_gb300.calibration import windowed_gradient
+    tiled = {k: np.ascontiguousarray(np.tile(np.array(v, np.float32), (1, sets, 1))) for k, v in obs.items()}
+    b.synchronize()
+    t0 = time.perf_counter()
+    wloss, wg = windowed_gradient(b, tiled, window=every)
+    wsec = time.perf_counter() - t0
+    params_eng = [b.force_params(k).astype(np.float64) for k in range(sets)]
     b.close()
+    # the first window's gradient of a sample of sets against the float64
+    # tangent along their own trajectories (oracle/calib64.py)
+    check = None
+    try:
+        from oracle import calib64, port as oport
+        sample = [k for k in (0, sets // 4, sets // 2, 3 * sets // 4) if k < sets]
+        b1 = Batch([paths[k] for k in sample])
+        t1 = {k: np.ascontiguousarray(np.tile(np.array(v[:every + 1], np.float32), (1, len(sample), 1)))
+              for k, v in obs.items()}
+        for j, k in enumerate(sample):
+            b1.set_force_params(params_eng[k].astype(np.float32), j)
+        _, g1 = windowed_gradient(b1, t1, window=every)
+        b1.close()
+        errs = []
+        z = np.zeros((n, 2))
+        for j, k in enumerate(sample):
+            s = Simulation(paths[k])
+            st = []
+            for tt in range(every + 1):
+                x = s.state()
+                st.append((x["pos"].copy(), x["vel"].copy()))
+                if tt < every:
+                    s.step(1)
+            s.close()
+            ref = calib64.tangent_gradient(oport.read_scenario(paths[k]), st, np.array(obs["pos"][1:every + 1]),
+                                           1.0 / (every * n), params_eng[k], [(np.eye(4)[q], z, z) for q in range(4)],
+                                           h=1e-8)
+            errs.append(float(np.linalg.norm(g1[j] - ref) / max(np.linalg.norm(ref), 1e-30)))
+        check = {"sets": sample, "window": f"steps 1..{every}", "rel_err_vs_float64_tangent": errs,
+                 "max_rel_err": max(errs), "tolerance": 1e-3}
+    except Exception as e:   # the check is a report, not part of the timing
+        check = {"error": repr(e)}
     finite = np.isfinite(g).all(1)
     f, a, p = statistics.median(fwd), statistics.median(bwd), statistics.median(plain)
     return {"sets": sets, "agents_per_set": n, "steps": steps, "checkpoint_every": every,
@@ -245,9 +321,13 @@ def diff_leg(tmp: str, sets: int = 256, n: int = 512, steps: int = 100, every: i
             "fwd_adjoint_over_forward": (f + a) / f, "fwd_adjoint_over_plain_step": (f + a) / p,
             "agent_steps_per_s_forward": sets * n * steps / f,
             "loss": loss, "sets_with_finite_gradient": int(finite.sum()),
-            "gradient_note": "over 100 steps at this density the pathwise gradient grows ~2.5x per step "
-                             "(the forward map's own divergence rate) and leaves the float range; "
-                             "gradients are checked at short horizons in tests/test_gpu_diff.py",
+            "gradient_note": "over 100 steps at this density the pathwise gradient of one episode grows ~2.5x "
+                             "per step (the forward map's own divergence rate) and leaves the float range; "
+                             "the windowed form below is the one to calibrate with",
+            "windowed": {"windows": (steps + every - 1) // every, "window_steps": every, "seconds": wsec,
+                         "ms_per_step": 1e3 * wsec / steps, "loss": wloss,
+                         "sets_with_finite_gradient": int(np.isfinite(wg).all(1).sum()),
+                         "gradient_check": check},
             "timing": f"median of {reps} after one warm-up, host clock around synchronous calls; "
                       "inputs (tape ~0.7 GB) exceed L2"}
 
@@ -296,8 +376,8 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
         kbar = cn["karamouzas_pair_ttc"] / max(cn["karamouzas_window_samples"], 1)
         flop = KARAMOUZAS_FLOP_PER_TTC * kbar * (1.0 + s_eval)
         kms = pr["agent_kernel_ms"] / max(pr["steps"], 1)
-        fp32_peak = 152 * 128 * 2 * 2070.0 * 1e6 / 1e12
-        work = dict(window_samples_per_agent=s_eval, pairs_per_sample=kbar, flop_per_agent_step=flop,
+        fp32_peak, sms = fp32_peak_tflops(2070.0)
+        work = dict(sms=sms, window_samples_per_agent=s_eval, pairs_per_sample=kbar, flop_per_agent_step=flop,
                     k_agent_ms=kms, achieved_tflops=flop * n / (kms * 1e-3) / 1e12,
                     peak_tflops_nominal=fp32_peak, frac=flop * n / (kms * 1e-3) / 1e12 / fp32_peak)
     sim.close()
@@ -343,6 +423,36 @@ def cpu_baseline(path: str, n_agents: int, seconds: float = 30.0, threads: int |
         t = sim.step(steps)
     return dict(value=n_agents * steps / t, unit="agent-steps/s", cores=threads, kind=kind,
                 sample=f"{steps} steps of the full {n_agents}-agent workload after 1 warm-up step")
+
+
+def parity_leg(path: str, warmup: int, steps: int, threads: int | None = None, checks: int = 5) -> dict:
+    """Maximum per-agent position deviation of the GPU trajectory from the
+    oracle (the C restatement, pinned to the reference by the golden
+    fixtures) over the benchmark's own step range, compared `checks` times."""
+    from oracle.port import PortSim
+    from umans_gb300 import Simulation
+    threads = threads or os.cpu_count() or 1
+    sim = Simulation(path)
+    with native_stdout_to_stderr():
+        port = PortSim(path, threads=threads)
+    sim.step(warmup)
+    port.step(warmup)
+    done, dev, worst_step = warmup, 0.0, warmup
+    left = steps
+    while left > 0:
+        k = min(left, max(1, steps // checks))
+        sim.step(k)
+        port.step(k)
+        done += k
+        left -= k
+        d = float(np.abs(sim.positions() - port.state()["pos"]).max())
+        if d > dev:
+            dev, worst_step = d, done
+    sim.close()
+    port.close()
+    return {"max_dev_m": dev, "at_step": worst_step, "steps_compared": f"{warmup + 1}..{done}",
+            "against": "oracle (C restatement, bit-identical to the compiled reference on the golden fixtures)",
+            "bar_m": 1e-4}
 
 
 def dist_setup(args=None, backend: str | None = None):
@@ -428,6 +538,9 @@ def run_reference(args):
                                  "sample": f"{args.steps} steps of the full workload after {args.warmup} warm-up"},
                 "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
+    por = port_over_reference()
+    if kind == "port" and por is not None:
+        line["cpu_baseline"]["port_over_reference"] = por
     print(json.dumps(line))
 
 
@@ -508,7 +621,7 @@ def run_ours(args):
         flops = (SF_FLOP_PER_PAIR * kbar + SF_FLOP_PER_AGENT) * n
         clocks = clk.summary()
         sm_max = clocks.get("sm_max_mhz") or 2070.0
-        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        fp32_peak, sms = fp32_peak_tflops(sm_max)
         sim.close()
         lap("warm_and_profile")
         # --- e2e through the reference-facing C functions ----------------
@@ -541,7 +654,13 @@ def run_ours(args):
         e2e_value = replica_rate(world, n, args.steps, te)
         lap("e2e")
         cpu = cpu_baseline(path, n, max_steps=args.steps) if (rank == 0 and world == 1 and not args.no_cpu) else None
+        if cpu is not None:
+            por = port_over_reference()
+            if por is not None:
+                cpu["port_over_reference"] = por
         lap("cpu_baseline")
+        parity = parity_leg(path, args.warmup, args.steps) if (rank == 0 and not args.no_parity) else None
+        lap("parity")
         batched = None if args.no_batch else batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
         lap("batched")
         diff = None if args.no_diff else diff_leg(tmp, sets=args.diff_sets)
@@ -567,13 +686,26 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "agent-steps/s", "h2d_bytes_per_step": 28 * n * world,
                 "d2h_bytes_per_step": 28 * n * world,
                 "path": "SetAgentPositions -> DoSimulationSteps(1) -> GetAgentPositions, host buffers"},
-        "roofline": {"bound": "hbm", "kernel": "k_agent", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": (tpa * n if tpa else None), "alg_bytes_per_launch": alg_bytes,
-                     "launch_ms": agent_ms, "step_ms_profiled": step_ms_prof},
-        "fp32_roofline": {"achieved_tflops": flops / (agent_ms * 1e-3) / 1e12, "peak_tflops_nominal": fp32_peak,
-                          "frac": flops / (agent_ms * 1e-3) / 1e12 / fp32_peak,
-                          "flop_per_agent_step": flops / max(n, 1)},
+        # the kernel's bound is min(HBM / bytes, FP32 / FLOPs) per agent-step;
+        # with ~96 B and ~3.3 kFLOP per agent-step the FP32 term is the lower
+        "roofline": {"bound": "fp32", "kernel": "k_agent",
+                     "achieved": flops / (agent_ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": flops / (agent_ms * 1e-3) / 1e12 / fp32_peak,
+                     "peak_source": f"nominal: {sms} SMs (from the device) x 128 FP32 lanes x 2 FLOP x "
+                                    f"{sm_max:.0f} MHz; MEASURED_PEAKS.json has no FP32 figure",
+                     "flop_per_agent_step": flops / max(n, 1),
+                     "flop_count": f"{SF_FLOP_PER_PAIR} per neighbour pair x {kbar:.1f} neighbours + "
+                                   f"{SF_FLOP_PER_AGENT} per agent (counted from the reference source)",
+                     "traffic": (tpa * n if tpa else None), "traffic_unit": "DRAM bytes per launch (ncu)",
+                     "launch_ms": agent_ms, "step_ms_profiled": step_ms_prof,
+                     "agent_steps_roofline": min(peak * 1e9 / K_AGENT_BYTES_PER_AGENT,
+                                                 fp32_peak * 1e12 / (flops / max(n, 1))),
+                     "frac_of_agent_steps_roofline": (n / (agent_ms * 1e-3)) /
+                                                     min(peak * 1e9 / K_AGENT_BYTES_PER_AGENT,
+                                                         fp32_peak * 1e12 / (flops / max(n, 1)))},
+        "hbm_roofline": {"kernel": "k_agent", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
+                         "traffic": (tpa * n if tpa else None)},
         "grid_build": {"kernels": "k_bbox..k_scatter", "ms": grid_ms, "alg_bytes_per_agent": GRID_BYTES_PER_AGENT,
                        "achieved": GRID_BYTES_PER_AGENT * n / (grid_ms * 1e-3) / 1e9 if grid_ms > 0 else None,
                        "peak": peak, "unit": "GB/s",
@@ -584,6 +716,9 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if parity:
+        line["max_dev_m"] = parity["max_dev_m"]
+        line["parity"] = parity
     if batched:
         line["batched"] = batched
     if diff:
@@ -603,6 +738,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="socialforces_toric")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-parity", action="store_true", help="skip the deviation check against the oracle")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form leg")
     ap.add_argument("--no-extra", action="store_true",

@@ -238,11 +238,14 @@ int umans_debug_prod_diff(const float* abcd, float* y, int n);
  * max_accel are float[n]; nbr_index / nbr_dist2 are [n * nbr_cap] (neighbour
  * list index into the same arrays, and PhantomAgent distSqr), nbr_count[n].
  * Limit: nbr_cap <= 128 (lines per agent); larger is rejected with
- * UMANS_ERR_ARGUMENT, and a count above nbr_cap returns UMANS_ERR_DEVICE.
- * The first call on a device looks up the array's device address; make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised.  Waits for `stream` (a
- * cudaStream_t, may be null).  Errors: umans_last_error(NULL). */
+ * UMANS_ERR_ARGUMENT.  A count above nbr_cap (the list is truncated) or a
+ * neighbour index outside [0, n) (the entry is skipped) returns
+ * UMANS_ERR_DEVICE.  The first call on a device looks up the array's device
+ * address.  Every call reads a status word back and synchronises `stream`
+ * (a cudaStream_t, may be null), so it must not be called while that stream
+ * is being captured.  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised.  Errors: umans_last_error(NULL), per
+ * host thread. */
 int umans_orca_velocities_noalloc(int n, const float* pos, const float* vel, const float* pref,
                                   const float* radius, const float* max_speed, const float* max_accel,
                                   const int* nbr_index, const float* nbr_dist2, const int* nbr_count,

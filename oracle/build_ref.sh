@@ -3,19 +3,24 @@
 # with oracle/ref_shim.cpp into oracle/_ref/libumans_ref.so.  Test
 # infrastructure only: the product never links this library.
 #
-# The reference sources are located by $UMANS_REFERENCE (default
-# /root/reference).  When they are absent (e.g. on a machine that only has
-# this repository) the script exits 0 without building anything.
+# The reference sources are located by $UMANS_REFERENCE (the root of a UMANS
+# checkout, the directory holding src/Engine).  When it is unset or does not
+# hold the sources (e.g. on a machine that only has this repository) the
+# script says so and exits 0 without building anything.
 #
 # -ffp-contract=off keeps GCC from fusing a*b+c into an FMA; aarch64 GCC
 # contracts by default, x86-64 without -mfma cannot, so this flag makes the
 # oracle's arithmetic identical on both hosts.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${UMANS_REFERENCE:-/root/reference}"
+REF="${UMANS_REFERENCE:-}"
 OUT="$HERE/_ref"
+if [ -z "$REF" ]; then
+  echo "UMANS_REFERENCE is not set; skipping the oracle/_ref build"
+  exit 0
+fi
 if [ ! -d "$REF/src/Engine" ]; then
-  echo "reference sources not found at $REF; skipping oracle/_ref build"
+  echo "reference sources not found at \$UMANS_REFERENCE=$REF; skipping the oracle/_ref build"
   exit 0
 fi
 mkdir -p "$OUT"

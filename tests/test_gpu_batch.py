@@ -28,6 +28,33 @@ def test_batch_equals_individual_simulations(tmp_path):
         assert np.array_equal(pos[off[k]:off[k + 1]], s.positions()), f"scenario {k}"
 
 
+def test_full_batch_members_equal_their_simulations(tmp_path):
+    """The benchmark's batch of 4096 scenarios (agent counts log-uniform in
+    [8, 2048], ~1.5M agents) stepped 20 steps together: 64 members (every
+    64th, all three policy kinds and both layouts) equal their own
+    simulations exactly."""
+    counts = S.batch_counts()
+    assert len(counts) == 4096
+    paths = [S.batch_member(k, int(n)).write(str(tmp_path / f"b{k}.xml")) for k, n in enumerate(counts)]
+    b = Batch(paths)
+    off = b.offsets
+    b.step(20)
+    pos = b.positions()
+    b.close()
+    sample = list(range(0, 4096, 64))
+    kinds = {k % 3 for k in sample}
+    assert kinds == {0, 1, 2}
+    worst = 0.0
+    for k in sample:
+        s = Simulation(paths[k])
+        s.step(20)
+        d = float(np.abs(pos[off[k]:off[k + 1]] - s.positions()).max())
+        worst = max(worst, d)
+        s.close()
+        assert d == 0.0, f"scenario {k} ({int(counts[k])} agents): {d} m"
+    print(f"4096-scenario batch, 20 steps: {len(sample)} members, max deviation {worst:.3g} m")
+
+
 def test_autotune_keeps_results(tmp_path):
     paths = _mixed(tmp_path, count=12)
     a, b = Batch(paths), Batch(paths)

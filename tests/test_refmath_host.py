@@ -1,10 +1,13 @@
 """Host-side checks of the reference-exact arithmetic shared by host and
 device code (refmath.hpp): the float-float line intersection never disagrees
 with the reference's double pipeline when it decides, and the float-float
-sine/cosine differs from the C library only near rounding midpoints."""
+sine/cosine differs from the C library only near rounding midpoints; the
+tables of the exponential and of the sine/cosine equal what their generators
+print."""
 import os
 import shutil
 import subprocess
+import sys
 
 import pytest
 
@@ -26,3 +29,38 @@ def test_refmath_host_check(tmp_path):
     assert "mismatches=0" in lines["isect"]
     assert "unflagged=0" in lines["sincos"]
     assert "mismatches=0" in lines["gauss"]
+
+
+def _table_rows(header: str, name: str) -> list[str]:
+    i = header.index(name)
+    body = header[header.index("{", i) + 1:header.index("};", i)]
+    return [l.strip() for l in body.strip().splitlines()]
+
+
+def _generated(script: str) -> list[str]:
+    pytest.importorskip("mpmath")
+    out = subprocess.run([sys.executable, script], capture_output=True, text=True,
+                         check=True).stdout
+    return [l.strip() for l in out.strip().splitlines()]
+
+
+def test_exp2_table_matches_its_generator():
+    csrc = os.path.join(HERE, "..", "umans_gb300", "csrc")
+    header = open(os.path.join(csrc, "refmath.hpp")).read()
+    rows = _generated(os.path.join(csrc, "gen_exp2_table.py"))
+    assert len(rows) == 64
+    assert _table_rows(header, "FF_EXP2_TAB_D") == rows
+    assert _table_rows(header, "FF_EXP2_TAB_H") == rows
+
+
+def test_sincos_table_matches_its_generator():
+    csrc = os.path.join(HERE, "..", "umans_gb300", "csrc")
+    header = open(os.path.join(csrc, "refmath.hpp")).read()
+    out = _generated(os.path.join(csrc, "gen_sincos_table.py"))
+    rows = [l for l in out if l.startswith("{")]
+    assert len(rows) == 53
+    assert _table_rows(header, "SC_TAB_D") == rows
+    assert _table_rows(header, "SC_TAB_H") == rows
+    consts = [l for l in out if l.startswith("constexpr float SC_")]
+    for c in consts:
+        assert c in header, c

@@ -22,8 +22,11 @@
 //    the status word: serialise them;
 //  * the host name of the array is not a device address; its device address
 //    is taken once per device with cudaGetSymbolAddress, with that device
-//    current, on the first call on that device.  Make that first call before
-//    any stream capture begins.
+//    current, on the first call on that device;
+//  * every call reads the status word back and synchronises `stream`, so it
+//    must not be called while that stream is being captured into a graph;
+//  * neighbour indices outside [0, n) are skipped and reported (status bit
+//    2), never read;
 //  * infinite worlds only: neighbours are indices into the caller's arrays,
 //    without wrap-around offsets.
 #include <cstdio>
@@ -65,15 +68,20 @@ __global__ void __launch_bounds__(128) k_orca_noalloc(
 			if (lane == 0) atomicOr(status, 1);
 			K = cap;
 		}
+		if (K < 0) K = 0;
 		float2 nv = V(0, 0);
 		if (!viszero(pv)) {
 			int nl = 0;
 			for (int base = 0; base < K; base += 32) {
 				const int k = base + lane;
-				const bool in = k < K && nbr_d2[(size_t)i * cap + k] <= maxDistSq;
+				bool in = k < K && nbr_d2[(size_t)i * cap + k] <= maxDistSq;
+				const int j = in ? nbr_index[(size_t)i * cap + k] : 0;
+				if (in && (j < 0 || j >= n)) {   // a stale or corrupt list: skip the entry
+					atomicOr(status, 2);
+					in = false;
+				}
 				float4 o = make_float4(0, 0, 0, 0);
 				if (in) {
-					const int j = nbr_index[(size_t)i * cap + k];
 					const float2 relPos = vsub(pos[j], p);
 					const float2 relVel = vsub(v, vel[j]);
 					const float distSq = vsq(relPos);
@@ -133,7 +141,7 @@ struct Symbols {
 constexpr int MAX_DEVICES = 64;
 Symbols g_syms[MAX_DEVICES];
 std::mutex g_sym_mutex;
-char g_err[256];
+thread_local char g_err[256];   // per host thread, as the handle API's error flag
 
 int set_error(int code, const char* fmt, ...)
 {
@@ -175,7 +183,11 @@ int orca_velocities_noalloc(int n, const float* pos, const float* vel, const flo
 		}
 	}
 	cudaStream_t st = (cudaStream_t)stream;
-	cudaError_t e = cudaMemsetAsync(S.status, 0, sizeof(int), st);
+	// an error left by the caller's earlier work is reported as such, not as
+	// this call's launch failure
+	cudaError_t e = cudaPeekAtLastError();
+	if (e != cudaSuccess) return set_error(3, "a CUDA error from earlier work is pending: %s", cudaGetErrorString(e));
+	e = cudaMemsetAsync(S.status, 0, sizeof(int), st);
 	if (e != cudaSuccess) return set_error(3, "cudaMemsetAsync: %s", cudaGetErrorString(e));
 	k_orca_noalloc<<<NOALLOC_WARPS / 4, 128, 0, st>>>(
 		n, (const float2*)pos, (const float2*)vel, (const float2*)pref, radius, max_speed, max_accel, nbr_index,
@@ -186,6 +198,7 @@ int orca_velocities_noalloc(int n, const float* pos, const float* vel, const flo
 	e = cudaMemcpyAsync(&hs, S.status, sizeof(int), cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	if (e != cudaSuccess) return set_error(3, "%s", cudaGetErrorString(e));
+	if (hs & 2) return set_error(4, "a neighbour index lies outside [0, n); those entries were skipped");
 	if (hs) return set_error(4, "a neighbour count exceeds nbr_cap; those lists were truncated");
 	return 0;
 }
