@@ -212,6 +212,14 @@ int umans_record_stop(umans_sim* sim);
  * values and reports the size of the exception table.  Errors are reported
  * through umans_last_error(NULL). */
 int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions);
+/* Test hook: checks the short exponential that the force models try first
+ * against the table-backed one, over the float bit patterns
+ * [first, first + count) that lie in [-87, 0]: counts[0] = values it
+ * answered, counts[1] = answered values whose result differs (must be 0),
+ * counts[2] = answered values listed in the exception table (must be 0);
+ * *band (may be null) receives the table's midpoint band in ulps.  Errors
+ * are reported through umans_last_error(NULL). */
+int umans_debug_expf_check(unsigned int first, unsigned int count, unsigned long long* counts, float* band);
 /* Test hook: the device's sinf/cosf, which return exactly the host C
  * library's sinf/cosf for |x| <= 64 (the float sin/cos of
  * costFunction.cpp:33, :104, :321 and FOEAvoidance.cpp:142); evaluates n

@@ -35,6 +35,34 @@ def test_ref_expf_bit_exact_dense_range():
         assert nexc > 0
 
 
+def test_short_exponential_on_every_float_of_the_domain():
+    """The force models try a short FMA exponential first and fall back to
+    the float-float one with the exception table only near rounding
+    midpoints.  On all 1.1e9 floats of [-87, 0] its answers equal the
+    table-backed results and never concern an argument the table lists; on
+    the force models' arguments, [-87, -2^-10], it answers almost always
+    (below that most results round to 1.0, a power of two it leaves to the
+    fallback)."""
+    lib = _lib.load()
+    first = int(np.float32(-0.0).view(np.uint32))
+    count = int(np.float32(-87.0).view(np.uint32)) - first + 1
+    out = np.zeros(3, np.uint64)
+    band = C.c_float()
+    rc = lib.umans_debug_expf_check(first, count, out.ctypes.data_as(C.c_void_p), C.byref(band))
+    assert rc == 0, lib.umans_last_error(None)
+    answered, differing, listed = (int(v) for v in out)
+    print(f"short exponential: answered {answered} of {count} ({answered / count:.5f}), "
+          f"differing {differing}, listed {listed}, table band {band.value:.3g} ulp")
+    assert differing == 0 and listed == 0
+    lo = int(np.float32(-2.0 ** -10).view(np.uint32))
+    count2 = int(np.float32(-87.0).view(np.uint32)) - lo + 1
+    rc = lib.umans_debug_expf_check(lo, count2, out.ctypes.data_as(C.c_void_p), None)
+    assert rc == 0, lib.umans_last_error(None)
+    print(f"on [-87, -2^-10]: answered {int(out[0]) / count2:.5f}")
+    assert int(out[1]) == 0 and int(out[2]) == 0
+    assert int(out[0]) > 0.99 * count2
+
+
 def test_ref_expf_random_and_edges():
     rng = np.random.default_rng(3)
     x = np.concatenate([rng.uniform(-87, 0, 2_000_000), -np.exp(rng.uniform(-100, 4, 500_000)),

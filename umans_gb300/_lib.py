@@ -78,6 +78,7 @@ _SIGS = {
     "umans_record_stop": (C.c_int, [P]),
     "umans_debug_ref_expf": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_size_t)]),
     "umans_debug_ref_sincosf": (C.c_int, [P, P, P, C.c_int, C.POINTER(C.c_size_t)]),
+    "umans_debug_expf_check": (C.c_int, [C.c_uint, C.c_uint, P, C.POINTER(C.c_float)]),
     "umans_debug_prod_diff": (C.c_int, [P, P, C.c_int]),
     "umans_orca_velocities_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, C.c_float,
                                                 C.c_float, C.c_float, C.c_float, P, P]),

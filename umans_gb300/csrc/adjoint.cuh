@@ -62,7 +62,11 @@ UDA SfAdj sf_pair_adj(const AgentCtx& A, const CostDesc& c, float2 np, float2 nv
 	const float2 R2 = sub2(R, Vv);
 	const float magR2 = sqrtf(dot2(R2, R2));
 	const float S = magR + magR2, T = vb * dtp;
-	const float bSq = S * S - T * T;
+	// where S^2 - T^2 cancels, as the forward step: pow(S, 2) - pow(T, 2) in
+	// double, rounded once (SocialForcesAvoidance.cpp:86); a plain float
+	// difference would give a different b there, and the terms below go as 1/b
+	float bSq = S * S - T * T;
+	if (bSq < 0.05f * (S * S)) bSq = sq_diff_d(S, T);
 	if (bSq <= 0) return o;
 	const float b = 0.5f * sqrtf(bSq);
 	if (b < 0.001f) return o;
@@ -133,7 +137,58 @@ struct PlAdj {
 	float lk, ltau0;
 };
 
-// PowerLaw::ComputeAgentInteractionForce (PowerLaw.cpp:28-66)
+// float-float arithmetic for the PowerLaw adjoint (products exact by FMA)
+UDA FF ffa_add(FF p, FF q)
+{
+	FF s = ff_two_sum(p.h, q.h);
+	s.l += p.l + q.l;
+	return ff_fast_two_sum(s.h, s.l);
+}
+UDA FF ffa_mul(FF p, FF q)
+{
+	FF r = ff_two_prod(p.h, q.h);
+	r.l += p.h * q.l + p.l * q.h;
+	return ff_fast_two_sum(r.h, r.l);
+}
+UDA float ffa_f(FF p) { return p.h + p.l; }
+
+// a = v.v, b = -x.v, cc = x.x - R^2, d = b^2 - a cc, x, v and
+// w = x + (cc / (b + sqrt(d))) v of a PowerLaw pair in float-float from the
+// exact differences of the states (taken only for ill-conditioned pairs, off
+// the common path: its registers stay out of the adjoint kernel)
+struct PlExact { float a, b, cc, d; float2 x, v, w; };
+__device__ __noinline__ PlExact pl_exact(float2 pi, float2 pj, float2 vi, float2 vj, float ri, float rj)
+{
+	const FF xx = ff_two_sum(pi.x, -pj.x), xy = ff_two_sum(pi.y, -pj.y);
+	const FF vx = ff_two_sum(vi.x, -vj.x), vy = ff_two_sum(vi.y, -vj.y);
+	const FF Rf = ff_two_sum(rj, ri);
+	const FF aa = ffa_add(ffa_mul(vx, vx), ffa_mul(vy, vy));
+	const FF bb = ffa_add(ffa_mul(xx, vx), ffa_mul(xy, vy));   // -b
+	const FF cf = ffa_add(ffa_add(ffa_mul(xx, xx), ffa_mul(xy, xy)), ffa_mul(Rf, FF{ -Rf.h, -Rf.l }));
+	const FF df = ffa_add(ffa_mul(bb, bb), ffa_mul(aa, FF{ -cf.h, -cf.l }));
+	PlExact e;
+	e.a = ffa_f(aa); e.b = -ffa_f(bb); e.cc = ffa_f(cf); e.d = ffa_f(df);
+	e.x = v2(ffa_f(xx), ffa_f(xy));
+	e.v = v2(ffa_f(vx), ffa_f(vy));
+	const FF tf = FF{ e.d > 0 && e.b > 0 ? e.cc / (e.b + sqrtf(e.d)) : 0.0f, 0.0f };
+	e.w = v2(ffa_f(ffa_add(xx, ffa_mul(tf, vx))), ffa_f(ffa_add(xy, ffa_mul(tf, vy))));
+	return e;
+}
+
+// PowerLaw::ComputeAgentInteractionForce (PowerLaw.cpp:28-66).  The branches
+// are decided on the forward step's own values (tau = (b - sqrt(d)) / a as
+// the reference computes it); the derivative is taken of the same force in
+// a form without cancellation: with u = b + sqrt(d), b - sqrt(d) = a cc / u,
+// so tau = cc / u and comp2 = v - (a x + b v) / sqrt(d) = -a (x + tau v) /
+// sqrt(d), and the force is
+//   f = comp1 comp2 = k E h (x + tau v) / (tau^2 sqrt(d)),
+//   E = exp(-tau / tau0), h = 2 / tau + 1 / tau0.
+// (The written form subtracts nearly equal terms when the relative speed is
+// small, which a float adjoint of it would amplify.)  Where d = b^2 - a cc,
+// cc = x.x - R^2 or b = -x.v cancel, these are evaluated in float-float
+// from the state (pl_exact): near a grazing collision (d << b^2; 4e-5 b^2
+// was seen at the calibration density) the float discriminant keeps only a
+// few bits, and the force goes as 1 / sqrt(d).
 UDA PlAdj pl_pair_adj(const AgentCtx& A, const CostDesc& c, float2 np, float2 nvel, float nr, float2 lf)
 {
 	PlAdj o;
@@ -146,52 +201,61 @@ UDA PlAdj pl_pair_adj(const AgentCtx& A, const CostDesc& c, float2 np, float2 nv
 	if (cc <= 0) return o;
 	const float d = b * b - a * cc;
 	if (d <= 0) return o;
-	const float sd = sqrtf(d);
-	const float tau = (b - sd) / a;
-	if (tau < 0.001f || tau > tau0) return o;
+	const float tau_f = (b - sqrtf(d)) / a;   // the forward step's value: its branches
+	if (tau_f < 0.001f || tau_f > tau0) return o;
+	// the same quantities, from the exact differences where they cancel
+	float ae = a, be = b, ce = cc, de = d;
+	float2 xe = x, ve = v;
+	const float xx2 = dot2(x, x);
+	const bool exact = d < 0.05f * b * b || cc < 0.05f * xx2 || b * b < 0.0025f * xx2 * a;
+	float2 w;
+	if (exact) {
+		const PlExact e = pl_exact(A.pos, np, A.vel, nvel, A.radius, nr);
+		ae = e.a; be = e.b; ce = e.cc; de = e.d; xe = e.x; ve = e.v; w = e.w;
+		if (!(de > 0) || !(ae > 0) || !(be > 0)) return o;
+	}
+	const float sd = sqrtf(de);
+	const float u = be + sd;
+	const float tau = ce / u;
 	const float E = expf(-tau / tau0);
 	const float h = 2 / tau + 1 / tau0;
-	const float comp1 = -k * E * h / (a * tau * tau);
-	const float2 q = add2(mul2(x, a), mul2(v, b));
-	const float2 comp2 = sub2(v, mul2(q, 1.0f / sd));
-	// f = comp1 comp2
-	const float lc1 = dot2(comp2, lf);
-	const float2 lc2 = mul2(lf, comp1);
-	// comp2 = v - q / sd
-	float2 lv = lc2;
-	const float2 lq = mul2(lc2, -1.0f / sd);
-	float lsd = dot2(q, lc2) / (sd * sd);
-	float la = dot2(x, lq);
-	float2 lx = mul2(lq, a);
-	float lb = dot2(v, lq);
-	lv = add2(lv, mul2(lq, b));
-	// comp1 = -k E h / (a tau^2)
-	o.lk = (comp1 / k) * lc1;
-	const float lE = (comp1 / E) * lc1;
-	const float lh = (comp1 / h) * lc1;
-	la += -(comp1 / a) * lc1;
-	float ltau = -2 * (comp1 / tau) * lc1;
-	// h = 2/tau + 1/tau0
-	ltau += -2 / (tau * tau) * lh;
-	float ltau0 = -1 / (tau0 * tau0) * lh;
-	// E = exp(-tau / tau0)
+	// w = x + tau v (|w| = R at the collision)
+	if (!exact) w = add2(x, mul2(v, tau));
+	const float Gk = E * h / (tau * tau * sd);   // f = k Gk w
+	const float G = k * Gk;
+	// f = G w
+	const float lG = dot2(w, lf);
+	const float2 lw = mul2(lf, G);
+	float2 lx = lw;
+	float2 lv = mul2(lw, tau);
+	float ltau = dot2(v, lw);
+	// G = k E h / (tau^2 sd)
+	o.lk = Gk * lG;
+	const float lE = (k * h / (tau * tau * sd)) * lG;
+	const float lh = (k * E / (tau * tau * sd)) * lG;
+	ltau += -2 * (G / tau) * lG;
+	float lsd = -(G / sd) * lG;
+	// E = exp(-tau / tau0); h = 2 / tau + 1 / tau0
 	ltau += -(E / tau0) * lE;
-	ltau0 += (E * tau / (tau0 * tau0)) * lE;
+	float ltau0 = (E * tau / (tau0 * tau0)) * lE;
+	ltau += -2 / (tau * tau) * lh;
+	ltau0 += -1 / (tau0 * tau0) * lh;
 	o.ltau0 = ltau0;
-	// tau = (b - sd) / a
-	lb += ltau / a;
-	lsd += -ltau / a;
-	la += -(tau / a) * ltau;
-	// sd = sqrt(d); d = b^2 - a cc
+	// tau = cc / u, u = b + sd
+	float lcc = ltau / u;
+	const float lu = -(tau / u) * ltau;
+	float lb = lu;
+	lsd += lu;
+	// sd = sqrt(d), d = b^2 - a cc
 	const float ld = lsd / (2 * sd);
-	lb += 2 * b * ld;
-	la += -cc * ld;
-	const float lcc = -a * ld;
+	lb += 2 * be * ld;
+	const float la = -ce * ld;
+	lcc += -ae * ld;
 	// cc = x.x - R^2; b = -x.v; a = v.v
-	lx = add2(lx, mul2(x, 2 * lcc));
-	lx = sub2(lx, mul2(v, lb));
-	lv = sub2(lv, mul2(x, lb));
-	lv = add2(lv, mul2(v, 2 * la));
+	lx = add2(lx, mul2(xe, 2 * lcc));
+	lx = sub2(lx, mul2(ve, lb));
+	lv = sub2(lv, mul2(xe, lb));
+	lv = add2(lv, mul2(ve, 2 * la));
 	o.lx = lx;
 	o.lv = lv;
 	return o;

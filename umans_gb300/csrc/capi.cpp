@@ -394,6 +394,14 @@ int umans_debug_ref_expf(const float* x, float* y, int n, size_t* exceptions)
 	return UMANS_OK;
 }
 
+int umans_debug_expf_check(unsigned int first, unsigned int count, unsigned long long* counts, float* band)
+{
+	if (!counts) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");
+	std::string err;
+	if (!umans::debug_expf_check(first, count, counts, band, err)) return fail(nullptr, UMANS_ERR_CUDA, err);
+	return UMANS_OK;
+}
+
 int umans_debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions)
 {
 	if ((n > 0 && (!x || !s || !c)) || n < 0) return fail(nullptr, UMANS_ERR_ARGUMENT, "bad argument");

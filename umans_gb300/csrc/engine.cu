@@ -1703,6 +1703,59 @@ bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::st
 	return true;
 }
 
+// The short exponential against the table-backed one on the float bit
+// patterns [first, first + count) that lie in [-87, 0].  counts[0]: values
+// where it answered, [1]: of those, results that differ from ff_expf_core,
+// [2]: answered values that the exception table lists.
+__global__ void k_expf_check(ExpExceptions T, uint32_t first, uint32_t count, unsigned long long* counts)
+{
+	unsigned long long dec = 0, bad = 0, listed = 0;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+		const uint32_t b = first + i;
+		const float x = __uint_as_float(b);
+		if (!(x >= FF_EXP_LO && x <= 0.0f)) continue;
+		float y;
+		if (!exp_fast(x, T.band, &y)) continue;
+		++dec;
+		const float z = ff_expf_core(x);
+		bool in_table = false;
+		uint32_t h = ff_hash(b, T.shift);
+		for (;;) {
+			const uint2 e = T.slots[h];
+			if (e.x == 0) break;
+			if (e.x == b) { in_table = true; break; }
+			h = (h + 1) & T.mask;
+		}
+		listed += in_table;
+		bad += __float_as_uint(y) != __float_as_uint(z);
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		dec += __shfl_xor_sync(0xffffffffu, dec, o);
+		bad += __shfl_xor_sync(0xffffffffu, bad, o);
+		listed += __shfl_xor_sync(0xffffffffu, listed, o);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicAdd(&counts[0], dec);
+		atomicAdd(&counts[1], bad);
+		atomicAdd(&counts[2], listed);
+	}
+}
+
+bool debug_expf_check(uint32_t first, uint32_t count, unsigned long long* out, float* band, std::string& err)
+{
+	ExpExceptions T;
+	if (!exp_exceptions_for_device(&T, nullptr, err)) return false;
+	if (band) *band = T.band;
+	unsigned long long* d = nullptr;
+	if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) { err = "cudaMalloc"; return false; }
+	cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+	if (count > 0) k_expf_check<<<1216, 256>>>(T, first, count, d);
+	cudaError_t e = cudaMemcpy(out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+	cudaFree(d);
+	if (e != cudaSuccess) { err = cudaGetErrorString(e); return false; }
+	return true;
+}
+
 // ------------------------------------------------------------------------
 // differentiable form
 // ------------------------------------------------------------------------
@@ -1771,7 +1824,7 @@ __device__ __noinline__ float2 obstacle_adjoint(const DevState& S, const ScenDes
 }
 
 template <bool OBST>
-__global__ void __launch_bounds__(128) k_adjoint(DevState S)
+__global__ void __launch_bounds__(128, 5) k_adjoint(DevState S)   // 5 blocks per SM (the launch)
 {
 	const int lane = threadIdx.x & 31;
 	const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

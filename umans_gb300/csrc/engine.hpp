@@ -20,6 +20,9 @@ struct DevState;   // device pointers (engine.cu)
 
 // device evaluation of the reference-exact expf (refmath.hpp), for tests
 bool debug_ref_expf(const float* x, float* y, int n, size_t* exceptions, std::string& err);
+// the short exponential against the table-backed one over float bit patterns
+// [first, first + count): out[0] answered, out[1] differing, out[2] listed
+bool debug_expf_check(uint32_t first, uint32_t count, unsigned long long* out, float* band, std::string& err);
 bool debug_ref_sincosf(const float* x, float* s, float* c, int n, size_t* exceptions, std::string& err);
 bool set_device_sincos(std::string& err);
 // device evaluation of (float)((double)a*b - (double)c*d) (devmath.cuh), for tests

@@ -31,6 +31,7 @@ struct HostTable {
 	int shift = 32;
 	size_t count = 0;
 	int fast = 0;
+	float band = 0.0f;
 };
 
 std::mutex g_mutex;
@@ -142,11 +143,15 @@ HostTable* build_host_table()
 	T->count = exc.size();
 	// the device may skip the table lookup away from rounding midpoints only
 	// if every exception is a near-midpoint argument
+	// (and the device's short evaluation answers only farther than `band`
+	// from a midpoint, the largest distance of an exception)
 	bool all_near = true;
 	for (const uint2& e : exc) {
 		bool near = false;
-		ff_expf_core(bitsf(e.x), &near);
+		float dist = 0.0f;
+		ff_expf_core(bitsf(e.x), &near, &dist);
 		all_near = all_near && near;
+		T->band = std::max(T->band, dist);
 	}
 	T->fast = all_near ? 1 : 0;
 	return T;
@@ -183,6 +188,7 @@ bool exp_exceptions_for_device(ExpExceptions* out, size_t* count, std::string& e
 	out->mask = g_host->mask;
 	out->shift = g_host->shift;
 	out->fast = g_host->fast;
+	out->band = g_host->band;
 	if (count) *count = g_host->count;
 	return true;
 }

@@ -250,7 +250,8 @@ constexpr float FF_EXP_LO = -87.0f;
 // when the unrounded value lies within 1/256 ulp of a rounding midpoint (the
 // only place where the host library's expf, accurate to 0.502 ulp, and this
 // function can disagree; the host verifies that against its full table).
-RM_HD float ff_expf_core(float x, bool* near = nullptr)
+// *dist receives that distance from the midpoint in ulps of the result.
+RM_HD float ff_expf_core(float x, bool* near = nullptr, float* dist = nullptr)
 {
 	const float INV = 92.33248138427734f;      // 64 / ln 2
 	const float L1 = 0x1.62cp-7f;              // ln2/64 = L1 + L2 + L3, L1 with 11 bits
@@ -278,10 +279,11 @@ RM_HD float ff_expf_core(float x, bool* near = nullptr)
 	const FF m = ff_two_prod(Th, s.h);
 	const float ml = m.l + (Th * sl + Tl * s.h);
 	const float f = m.h + ml;
-	if (near) {
+	if (near || dist) {
 		const float rl = ml - (f - m.h);
 		const float half_ulp = rm_float((rm_bits(f) & 0x7f800000u) - (24u << 23));
-		*near = !(fabsf(rl) < half_ulp * 0.99609375f);
+		if (near) *near = !(fabsf(rl) < half_ulp * 0.99609375f);
+		if (dist) *dist = (half_ulp - fabsf(rl)) / (2.0f * half_ulp);
 	}
 	// 2^kq, kq in [-126, 0]: normal, so the scaling is exact
 	return f * rm_float((uint32_t)(kq + 127) << 23);
@@ -327,15 +329,62 @@ struct ExpExceptions {
 	uint32_t mask;    // size - 1 (size a power of two)
 	int shift;        // 32 - log2(size)
 	int fast;         // 1 when every table entry is a near-midpoint argument
+	float band;       // largest distance of an entry's value from its rounding midpoint, in ulps
 };
 
 RM_HD uint32_t ff_hash(uint32_t bits, int shift) { return (bits * 0x9E3779B1u) >> shift; }
 
 #if defined(__CUDACC__)
+// ln 2 / 64 = EXP_L1 + EXP_L2 (+ 1.4e-18); EXP_L1 is a multiple of 2^-30
+constexpr float EXP_L1 = 0x1.62e43p-7f;
+constexpr float EXP_L2 = -0x1.05c61p-35f;
+
+// e^x for x in [FF_EXP_LO, 0] by a short FMA evaluation: Tang's table method
+// (P. T. P. Tang, "Table-driven implementation of the exponential function
+// in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989), x = k ln2/64 + r
+// with r reduced in two parts (the first, fma(-k, EXP_L1, x), is exact: both
+// terms are multiples of 2^-30 and |r| < 2^-7), e^r - 1 by a degree-4
+// polynomial, and 2^(j/64) from the float-pair table; the unrounded value is
+// within 2^-13 ulp of e^x.  Returns true with *out = e^x rounded to nearest
+// when that rounding is decided and e^x lies farther than `band` + 2^-13 ulp
+// from a rounding midpoint (outside the exception table's reach); false
+// otherwise, for the caller to take ff_expf_core and the table.  Checked
+// against the table-backed result on every float of the domain
+// (umans_debug_expf_check, tests/test_gpu_refmath.py).
+__device__ __forceinline__ bool exp_fast(float x, float band, float* out)
+{
+	const float kf = rintf(x * 92.33248138427734f);   // 64 / ln 2
+	const float r_hi = fmaf(-kf, EXP_L1, x);
+	const float r_lo = -kf * EXP_L2;
+	const float rh = r_hi + r_lo;                       // TwoSum
+	const float bb = rh - r_hi;
+	const float rl = (r_hi - (rh - bb)) + (r_lo - bb);
+	float c = fmaf(rh, 1.0f / 24.0f, 1.0f / 6.0f);
+	c = fmaf(rh, c, 0.5f);
+	const float q = fmaf(rh * rh, c, fmaf(rl, rh, rl));   // e^r - 1 - rh
+	const int k = (int)kf;
+	const int j = k & 63;
+	const int kq = (k - j) / 64;                        // floor(k / 64)
+	const float Th = FF_EXP2_TAB_D[j][0], Tl = FF_EXP2_TAB_D[j][1];
+	const float Ph = Th * rh, Pl = fmaf(Th, rh, -Ph);   // Th rh exactly
+	const float Sh = Th + Ph, Sl = Ph - (Sh - Th);      // Th + Ph exactly (|Ph| < Th)
+	const float tail = Sl + (Pl + fmaf(Th, q, fmaf(Tl, rh, Tl)));
+	const float f = Sh + tail;
+	const float e = (Sh - f) + tail;                    // f's rounding residual
+	const uint32_t fb = __float_as_uint(f);
+	const float ulp = __uint_as_float((fb & 0x7f800000u) - (23u << 23));
+	if ((fb & 0x007fffffu) == 0) return false;          // a power of two: unequal ulps on its two sides
+	if (!(fabsf(e) < ulp * (0.5f - band - 0x1p-12f))) return false;
+	*out = f * __uint_as_float((uint32_t)(kq + 127) << 23);   // kq in [-126, 0]: exact
+	return true;
+}
+
 // The host C library's expf(x), exactly (see the header comment).
 __device__ __forceinline__ float ref_expf(const ExpExceptions& T, float x)
 {
 	if (!(x >= FF_EXP_LO && x <= 0.0f)) return (float)exp((double)x);
+	float yf;
+	if (T.fast && exp_fast(x, T.band, &yf)) return yf;
 	bool near;
 	const float y = ff_expf_core(x, &near);
 	if (T.fast && !near) return y;
