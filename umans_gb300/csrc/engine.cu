@@ -304,6 +304,59 @@ __global__ void k_scan_down(DevState S)
 	if (blockIdx.x == 0 && threadIdx.x == 0) S.start[nc] = S.n;
 }
 
+// The same exclusive scan in one block, for grids of at most
+// SCAN_SINGLE_MAX_CELLS cells (one launch instead of three): each warp scans
+// a contiguous range of cells in coalesced chunks of 32, after a first pass
+// that sums the warps' ranges.
+constexpr int SCAN_SINGLE_MAX_CELLS = 1 << 17;
+__global__ void __launch_bounds__(1024) k_scan_single(DevState S)
+{
+	const int nc = S.cell_base[S.nscen];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	const int per = (((nc + nw - 1) / nw) + 31) & ~31;
+	const int w0 = min(nc, warp * per), w1 = min(nc, w0 + per);
+	int s = 0;
+	for (int c = w0 + lane; c < w1; c += 32) s += S.cnt[c];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	__shared__ int wt[32];
+	if (lane == 0) wt[warp] = s;
+	__syncthreads();
+	if (warp == 0) {
+		const int v = lane < nw ? wt[lane] : 0;
+		int incl = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, incl, o);
+			if (lane >= o) incl += u;
+		}
+		if (lane < nw) wt[lane] = incl - v;
+	}
+	__syncthreads();
+	// the loads do not depend on the running total: distinct arrays, so that
+	// they can be issued ahead of the stores
+	const int* __restrict__ cnt = S.cnt;
+	int* __restrict__ start = S.start;
+	int* __restrict__ fill = S.fill;
+	int run = wt[warp];
+#pragma unroll 4
+	for (int base = w0; base < w1; base += 32) {
+		const int c = base + lane;
+		const int v = c < w1 ? __ldcg(cnt + c) : 0;
+		int incl = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, incl, o);
+			if (lane >= o) incl += u;
+		}
+		if (c < w1) {
+			start[c] = run + incl - v;
+			fill[c] = run + incl - v;
+		}
+		run += __shfl_sync(0xffffffffu, incl, 31);
+	}
+	__syncthreads();
+	for (int c = w0 + lane; c < w1; c += 32) S.cnt[c] = 0;   // histogram is all-zero between steps
+	if (threadIdx.x == 0) S.start[nc] = S.n;
+}
+
 __device__ __forceinline__ void scatter_one(const DevState& S, int i)
 {
 	const int c = S.cell[i];
@@ -2153,6 +2206,9 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		if (!dalloc(scen_order_dev_, scen_order_.size(), err_)) return false;
 		CK(cudaMemcpy(scen_order_dev_, scen_order_.data(), sizeof(int) * scen_order_.size(), cudaMemcpyHostToDevice));
 		d_->scen_order = scen_order_dev_;
+		toric_only_ = !scen_.empty();
+		for (const auto& D : scen_) toric_only_ = toric_only_ && D.world == W_TORIC;
+		static_grid_ready_ = false;
 	}
 	if (!edges_.empty()) {
 		if (!dalloc(edges_dev_, edges_.size(), err_)) return false;
@@ -2540,6 +2596,7 @@ bool Engine::configure()
 	S.total_warps = agent_blocks_ * wpb;
 	S.sched = opt_.schedule;
 	S.cells_per_range = opt_.cells_per_range;
+	static_grid_ready_ = false;   // the cell size may have changed
 	if (!dalloc(S.scratch, std::max<size_t>(scr, 1), err_)) return false;
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
@@ -2596,8 +2653,11 @@ bool Engine::small_world() const
 	return scen_.size() == 1 && n_ <= SMALL_MAX_AGENTS && d_->max_cells <= SMALL_MAX_CELLS;
 }
 
-// The grid build: one block for a small single-scenario world, else the
-// seven grid-wide kernels.
+// The grid build: one block for a small single-scenario world; else the
+// bounding box and grid parameters (every step in infinite worlds; once, by
+// ensure_static_grid, when every world is toric: its grid is the world
+// box), the histogram, the scan (one block up to SCAN_SINGLE_MAX_CELLS
+// cells) and the scatter.
 void Engine::enqueue_grid(const DevState& S)
 {
 	if (small_world()) {
@@ -2606,14 +2666,38 @@ void Engine::enqueue_grid(const DevState& S)
 	}
 	const int threads = 256;
 	const int nb = std::max(1, (n_ + threads - 1) / threads);
-	k_bbox<<<nb, threads, 0, stream_>>>(S);
-	k_grid<<<1, 1024, 0, stream_>>>(S);
+	const bool grid_fixed = toric_only_ && static_grid_ready_;
+	if (!grid_fixed) {
+		k_bbox<<<nb, threads, 0, stream_>>>(S);
+		k_grid<<<1, 1024, 0, stream_>>>(S);
+	}
 	k_count<<<nb, threads, 0, stream_>>>(S);
-	const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
-	k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
-	k_scan_top<<<1, 1024, 0, stream_>>>(S);
-	k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	const int cells_bound = grid_fixed ? static_cells_ : S.max_cells;
+	if (cells_bound <= SCAN_SINGLE_MAX_CELLS) {
+		k_scan_single<<<1, 1024, 0, stream_>>>(S);
+	} else {
+		const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+		k_scan_reduce<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+		k_scan_top<<<1, 1024, 0, stream_>>>(S);
+		k_scan_down<<<sb, SCAN_BLOCK, 0, stream_>>>(S);
+	}
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
+}
+
+// Toric worlds only: the grid parameters and cell ranges, which do not
+// change between steps, computed once outside any graph capture.
+bool Engine::ensure_static_grid()
+{
+	if (!toric_only_ || static_grid_ready_ || small_world()) return true;
+	DevState& S = *d_;
+	S.n = n_;
+	k_grid<<<1, 1024, 0, stream_>>>(S);
+	CK(cudaGetLastError());
+	CK(cudaMemcpyAsync(&static_cells_, S.cell_base + scen_.size(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+	CK(cudaStreamSynchronize(stream_));
+	static_grid_ready_ = true;
+	invalidate_graph();
+	return true;
 }
 
 void Engine::set_profile(bool on)
@@ -2637,7 +2721,13 @@ bool Engine::profile_counters(unsigned long long* out, int n)
 	return true;
 }
 
-int Engine::kernels_per_step() const { return (small_world() ? 1 : 7) + (int)groups_.size(); }
+int Engine::kernels_per_step() const
+{
+	if (small_world()) return 1 + (int)groups_.size();
+	const bool grid_fixed = toric_only_ && static_grid_ready_;
+	const bool single = (grid_fixed ? static_cells_ : d_->max_cells) <= SCAN_SINGLE_MAX_CELLS;
+	return (grid_fixed ? 0 : 2) + 1 + (single ? 1 : 3) + 1 + (int)groups_.size();
+}
 
 bool Engine::capture_graph()
 {
@@ -2715,6 +2805,7 @@ bool Engine::remove_at_goal()
 bool Engine::run_steps(int nsteps, bool record)
 {
 	if (configured_maxnb_ != maxnb_ && !configure()) return false;
+	if (!ensure_static_grid()) return false;
 	steps_pending_ = true;
 	record = record && rec_ != nullptr;
 	if (record && n_ > rec_cap_n_) {
@@ -3127,6 +3218,7 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	float4* scr = nullptr;
 	if (!dalloc(scr, (size_t)T.total_warps * 2 * dump_nb, err_)) return false;
 	T.scratch = scr;
+	if (!ensure_static_grid()) { cudaFree(scr); return false; }
 	enqueue_grid(T);
 	T.t_begin = 0;
 	T.t_end = n_;

@@ -145,6 +145,10 @@ private:
 	bool restore_snapshot();
 	void enqueue_step();
 	void enqueue_grid(const DevState& S);
+	bool ensure_static_grid();
+	bool toric_only_ = false;          // every scenario's world is toric: the grid is fixed
+	bool static_grid_ready_ = false;   // its parameters are on the device
+	int static_cells_ = 0;             // its cell count
 	bool capture_graph();
 	void invalidate_graph();
 	bool apply_pending_agents();
