@@ -32,7 +32,6 @@
 #include "costs.cuh"
 #include "orca.cuh"
 #include "adjoint.cuh"
-#include "plugins.cuh"
 
 namespace umans {
 
@@ -1131,6 +1130,12 @@ __device__ float2 grad_foe(const AgentCtx& A, const NbView& N, const CostDesc& c
 	return V(-Vn.y * w.x + -Vn.x * w.y, -(-Vn.x) * w.x + -Vn.y * w.y);
 }
 
+}  // namespace umans
+// cost-function plugins: their device functions may use the gradient
+// helpers above (grad_foe, ordered_sums, ...)
+#include "plugins.cuh"
+namespace umans {
+
 // ------------------------------------------------------------------------
 // per-cost evaluation (sampling / finite differences)
 // ------------------------------------------------------------------------
@@ -1588,7 +1593,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					else if (c.kind == K_TTCADCA)
 						g = grad_ttcadca(A, N, c, A.vel, lane, fx, fy, reinterpret_cast<float*>(proj));
 					else if (c.kind == K_FOE) g = grad_foe(A, N, c, A.vel, lane, fx, fy);
-					else {
+					else if (c.kind >= K_PLUGIN0 &&
+					         plugin_gradient(c.kind - K_PLUGIN0, A, N, c, A.vel, lane, fx, fy, &g)) {
+						// the plugin's GetGradient
+					} else {
 						// CostFunction::GetGradient default: costFunction.cpp:36-54;
 						// lanes 0..3 evaluate the four probes
 						const float d = 0.1f;
@@ -1616,6 +1624,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				const CostDesc& c0 = pol.cost[0];
 				if (pol.method == M_GLOBAL && pol.ncost == 1 && c0.kind == K_ORCA) best = P.orca_v;
 				else if (pol.method == M_GLOBAL && pol.ncost == 1 && is_force_based(c0.kind)) best = P.target[0];
+				else if (pol.method == M_GLOBAL && pol.ncost == 1 && c0.kind >= K_PLUGIN0 &&
+				         plugin_global_minimum(c0.kind - K_PLUGIN0, A, N, c0, lane, &best)) {
+					// the plugin's GetGlobalMinimum
+				}
 				else {
 					const uint32_t r0 = S.rng[slot];
 					best = sample_min(S, A, N, pol, P, r0, lane, lines, reinterpret_cast<float*>(proj));

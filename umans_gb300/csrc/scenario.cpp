@@ -64,6 +64,7 @@ void cost_defaults(int kind, CostDesc& c)
 		if (kind >= K_PLUGIN0 && kind < K_PLUGIN0 + kNumPlugins) {
 			const PluginInfo& pl = kPlugins[kind - K_PLUGIN0];
 			for (int k = 0; k < pl.nparams; ++k) c.p[pl.params[k].slot] = pl.params[k].dflt;
+			if (pl.range >= 0) c.range = pl.range;
 		}
 		break;
 	}
