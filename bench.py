@@ -619,6 +619,7 @@ def run_ours(args):
         step_ms_prof = prof["step_ms"] / max(prof["steps"], 1)
         grid_ms = prof["grid_build_ms"] / max(prof["steps"], 1)
         kbar = sum(kb) / len(kb)
+        list_cap = sim.max_neighbours
         peak, peak_kind = measured_peaks()
         alg_bytes = K_AGENT_BYTES_PER_AGENT * n
         achieved = alg_bytes / (agent_ms * 1e-3) / 1e9
@@ -682,7 +683,7 @@ def run_ours(args):
     cfg = dict(cfg, l2="flushed (256 MiB write) before every timed step; state ~10 MB would fit in L2",
                timed_steps=f"steps {args.warmup + 1}..{args.warmup + args.steps} of the scenario (the neighbour "
                            f"count grows as the crowd condenses)",
-               neighbours_mean=round(kbar, 2), parallelism=f"replicas x{world}")
+               neighbours_mean=round(kbar, 2), list_capacity=list_cap, parallelism=f"replicas x{world}")
     line = {
         "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,

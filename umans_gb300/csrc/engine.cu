@@ -54,6 +54,7 @@ struct DevState {
 	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces)
 	int *sSlot, *sId;
 	int *cell, *cnt, *start, *fill, *blocksum;
+	unsigned* ticket;       // blocks of k_count_scan done (zero between launches)
 	GridParams* grid;       // [nscen]
 	unsigned* bbox;         // [4 * nscen]
 	// profiling only (else null): Karamouzas samples inside the window, pairs
@@ -303,6 +304,119 @@ __global__ void k_scan_down(DevState S)
 	if (blockIdx.x == 0 && threadIdx.x == 0) S.start[nc] = S.n;
 }
 
+// Exclusive scan of cnt[0..nc) by one block through shared memory (sm holds
+// nc + nc/32 ints; the index is padded by one word per 32 so that per-thread
+// runs of cells fall in different banks): coalesced loads, eight in flight
+// per thread, then per thread a contiguous run of cells summed, a block scan
+// of the run sums, the runs rewritten with their prefixes, and a coalesced
+// write of start and fill, the histogram zeroed for the next step.
+constexpr int SCAN_SMEM_MAX_CELLS = 49152;
+__host__ __device__ constexpr size_t scan_smem_bytes(int cells) { return sizeof(int) * ((size_t)cells + cells / 32 + 1); }
+__device__ __forceinline__ int scan_pad(int c) { return c + (c >> 5); }
+__device__ void block_scan_cells(const DevState& S, int nc, int* sm)
+{
+	const int tid = threadIdx.x, nt = blockDim.x;
+	const int* __restrict__ cnt = S.cnt;
+	for (int c0 = tid; c0 < nc; c0 += 8 * nt) {
+		int v[8];
+#pragma unroll
+		for (int k = 0; k < 8; ++k) {
+			const int c = c0 + k * nt;
+			v[k] = c < nc ? __ldcg(cnt + c) : 0;
+		}
+#pragma unroll
+		for (int k = 0; k < 8; ++k) {
+			const int c = c0 + k * nt;
+			if (c < nc) sm[scan_pad(c)] = v[k];
+		}
+	}
+	__syncthreads();
+	const int L = (nc + nt - 1) / nt;
+	const int c0 = min(nc, tid * L), c1 = min(nc, c0 + L);
+	int s = 0;
+	for (int c = c0; c < c1; ++c) s += sm[scan_pad(c)];
+	const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+	int incl = s;
+	for (int o = 1; o < 32; o <<= 1) {
+		const int u = __shfl_up_sync(0xffffffffu, incl, o);
+		if (lane >= o) incl += u;
+	}
+	__shared__ int wt[32];
+	if (lane == 31) wt[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		const int v = lane < nw ? wt[lane] : 0;
+		int w = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, w, o);
+			if (lane >= o) w += u;
+		}
+		if (lane < nw) wt[lane] = w - v;
+	}
+	__syncthreads();
+	int run = wt[warp] + incl - s;
+	for (int c = c0; c < c1; ++c) {
+		const int v = sm[scan_pad(c)];
+		sm[scan_pad(c)] = run;
+		run += v;
+	}
+	__syncthreads();
+	int* __restrict__ start = S.start;
+	int* __restrict__ fill = S.fill;
+	int* __restrict__ zero = S.cnt;
+	for (int c = tid; c < nc; c += nt) {
+		const int v = sm[scan_pad(c)];
+		start[c] = v;
+		fill[c] = v;
+		zero[c] = 0;   // histogram is all-zero between steps
+	}
+	if (tid == 0) start[nc] = S.n;
+}
+
+// One block, grids of at most `cap` (<= SCAN_SMEM_MAX_CELLS) cells.
+__global__ void __launch_bounds__(1024) k_scan_smem(DevState S, int cap)
+{
+	extern __shared__ int sm[];
+	const int nc = S.cell_base[S.nscen];
+	if (nc > cap) {   // cannot happen: cap bounds every grid the engine builds
+		if (threadIdx.x == 0) atomicOr(S.status, ST_GRID_OVERFLOW);
+		return;
+	}
+	block_scan_cells(S, nc, sm);
+}
+
+// The histogram and, in the last block to finish, the scan: one launch for
+// grids whose cell count is fixed and at most `cap` cells (toric worlds).
+// Each block counts its agents, fences, and takes a ticket; the block that
+// takes the last ticket sees every other block's counts in L2 and scans them
+// (no block waits for another).
+__global__ void __launch_bounds__(1024) k_count_scan(DevState S, int cap)
+{
+	extern __shared__ int sm[];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < S.n) {
+		const int sc = S.agent_scen[i];
+		count_one(S, i, S.grid[sc], S.cell_base[sc]);
+	}
+	__threadfence();
+	__syncthreads();
+	__shared__ bool last;
+	if (threadIdx.x == 0) {
+		const unsigned t = atomicAdd(S.ticket, 1u);
+		last = t == gridDim.x - 1;
+		if (last) *S.ticket = 0u;   // for the next launch
+	}
+	__syncthreads();
+	if (!last) return;
+	__threadfence();
+	const int nc = S.cell_base[S.nscen];
+	if (nc > cap) {
+		if (threadIdx.x == 0) atomicOr(S.status, ST_GRID_OVERFLOW);
+		return;
+	}
+	block_scan_cells(S, nc, sm);
+}
+
 // The same exclusive scan in one block, for grids of at most
 // SCAN_SINGLE_MAX_CELLS cells (one launch instead of three): each warp scans
 // a contiguous range of cells in coalesced chunks of 32, after a first pass
@@ -502,16 +616,13 @@ __device__ void warp_sort(const DevState& S, const WarpLists& L, int s, int len,
 // Sort of [s, s+len), len <= 32 * M (M = 1, 2, 4), in registers: each lane
 // holds M packed keys (float key bits with the low PB bits replaced by the
 // position in the segment; positive floats order like their bit patterns)
-// and a shuffle bitonic network sorts them.  The entries are then permuted
-// through registers holding only the references: the key of an entry is
-// recomputed from its reference exactly as the gather computed it (same
-// expression, same operands).  Keys that agree above the low PB
+// and a shuffle bitonic network sorts them.  The entries (reference and
+// full key) are then permuted through registers.  Keys that agree above the low PB
 // bits may come out in either order: the near-tie pass that follows
 // (relative window 2^(PB-22), twice the 2^(PB-23) truncation) re-orders
 // them with the exact double distance and the id.
 template <int M>
-__device__ __forceinline__ void warp_sort_regs(const DevState& S, const WarpLists& L, int s, int len, int lane,
-                                               float2 q)
+__device__ __forceinline__ void warp_sort_regs(const WarpLists& L, int s, int len, int lane)
 {
 	constexpr int PB = (M == 1) ? 5 : (M == 2) ? 6 : 7;
 	constexpr uint32_t PMASK = (1u << PB) - 1u;
@@ -547,21 +658,21 @@ __device__ __forceinline__ void warp_sort_regs(const DevState& S, const WarpList
 			}
 		}
 	}
+	float k[M];
 #pragma unroll
 	for (int m = 0; m < M; ++m) {
 		const int i = m * 32 + lane;
-		u[m] = (i < len) ? L.ref[s + (int)(u[m] & PMASK)] : 0u;
+		const int from = s + (int)(u[m] & PMASK);
+		k[m] = (i < len) ? L.key[from] : 0.0f;
+		u[m] = (i < len) ? L.ref[from] : 0u;
 	}
 	__syncwarp();
 #pragma unroll
 	for (int m = 0; m < M; ++m) {
 		const int i = m * 32 + lane;
 		if (i < len) {
-			const int tt = (int)(u[m] & 0x0FFFFFFFu);
-			const float2 cp = S.sP[tt];
-			const float dx = q.x - cp.x, dy = q.y - cp.y;
 			L.ref[s + i] = u[m];
-			L.key[s + i] = dx * dx + dy * dy;
+			L.key[s + i] = k[m];
 		}
 	}
 	__syncwarp();
@@ -708,42 +819,56 @@ __device__ int gather(const DevState& S, const GridParams& G, int cb, int world,
 			// nr are empty and start at the total)
 			const int beg = incl - len;
 			const int total = __shfl_sync(0xffffffffu, incl, ROWS - 1);
-			for (int base = 0; base < total; base += 32) {
-				const int c = base + lane;
-				// the last row starting at or before c (binary search over the
-				// ROWS starts, held by lanes 0..ROWS-1)
-				int r = 0;
+			// two chunks of 32 candidates per pass: both chunks' positions are
+			// loaded before either is tested
+			for (int base = 0; base < total; base += 64) {
+				const int nh = base + 32 < total ? 2 : 1;
+				int tt[2];
+				float2 cp[2];
 #pragma unroll
-				for (int step = ROWS / 2; step > 0; step >>= 1)
-					if (__shfl_sync(0xffffffffu, beg, r + step) <= c) r += step;
-				const int tt = __shfl_sync(0xffffffffu, rs, r) + (c - __shfl_sync(0xffffffffu, beg, r));
-				bool ok = false;
-				float d2f = 0;
-				if (c < total && tt != t) {
-					const float2 cp = S.sP[tt];
-					const float dx = q.x - cp.x, dy = q.y - cp.y;
-					d2f = dx * dx + dy * dy;
-					if (d2f < r2lo) ok = true;
-					else if (d2f <= r2hi) ok = exact_key(q, cp) < r2d;
+				for (int h = 0; h < 2; ++h) {
+					if (h >= nh) break;
+					const int c = base + 32 * h + lane;
+					// the last row starting at or before c (binary search over the
+					// ROWS starts, held by lanes 0..ROWS-1)
+					int r = 0;
+#pragma unroll
+					for (int step = ROWS / 2; step > 0; step >>= 1)
+						if (__shfl_sync(0xffffffffu, beg, r + step) <= c) r += step;
+					tt[h] = __shfl_sync(0xffffffffu, rs, r) + (c - __shfl_sync(0xffffffffu, beg, r));
+					cp[h] = (c < total && tt[h] != t) ? S.sP[tt[h]] : V(0, 0);
 				}
-				const unsigned m = __ballot_sync(0xffffffffu, ok);
-				if (ok) {
-					const int idx = K + __popc(m & lt);
-					if (idx < maxnb) {
-						L.ref[idx] = ((uint32_t)g << 28) | (uint32_t)tt;
-						L.key[idx] = d2f;
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					if (h >= nh) break;
+					const int c = base + 32 * h + lane;
+					bool ok = false;
+					float d2f = 0;
+					if (c < total && tt[h] != t) {
+						const float dx = q.x - cp[h].x, dy = q.y - cp[h].y;
+						d2f = dx * dx + dy * dy;
+						if (d2f < r2lo) ok = true;
+						else if (d2f <= r2hi) ok = exact_key(q, cp[h]) < r2d;
 					}
+					const unsigned m = __ballot_sync(0xffffffffu, ok);
+					if (ok) {
+						const int idx = K + __popc(m & lt);
+						if (idx < maxnb) {
+							L.ref[idx] = ((uint32_t)g << 28) | (uint32_t)tt[h];
+							L.key[idx] = d2f;
+						}
+					}
+					K += __popc(m);
 				}
-				K += __popc(m);
 			}
 		}
 		if (K > maxnb) { *overflow = true; K = maxnb; }
 		if (g == 0) K0 = K;
 		__syncwarp();
 		const int len = K - gs;
-		if (len <= 32) warp_sort_regs<1>(S, L, gs, len, lane, q);
-		else if (len <= 64) warp_sort_regs<2>(S, L, gs, len, lane, q);
-		else if (len <= 128) warp_sort_regs<4>(S, L, gs, len, lane, q);
+		if (len <= 32) warp_sort_regs<1>(L, gs, len, lane);
+		else if (len <= 64) warp_sort_regs<2>(L, gs, len, lane);
+		else if (len <= 128) warp_sort_regs<4>(L, gs, len, lane);
 		else warp_sort(S, L, gs, len, lane);
 		fix_near_ties(S, L, gs, K, q, lane, len <= 64 ? 0x1p-16f : (len <= 128 ? 0x1p-15f : 1e-6f));
 	}
@@ -879,6 +1004,29 @@ __device__ __forceinline__ float2 ordered_accumulate(float2 acc, float2 f, bool 
 	return acc;
 }
 
+// fx[0..K) summed by lane 0 and fy[0..K) by lane 1, in list order (the
+// reference's sequential Vector2D sum), eight loads issued ahead of their
+// additions; every lane returns both sums.
+__device__ __forceinline__ float2 list_sum(const float* fx, const float* fy, int K, int lane)
+{
+	float acc = 0.0f;
+	if (lane < 2) {
+		const float* src = lane ? fy : fx;
+		int k = 0;
+		for (; k + 8 <= K; k += 8) {
+			float v[8];
+#pragma unroll
+			for (int j = 0; j < 8; ++j) v[j] = src[k + j];
+#pragma unroll
+			for (int j = 0; j < 8; ++j) acc += v[j];
+		}
+		for (; k < K; ++k) acc += src[k];
+	}
+	return V(__shfl_sync(0xffffffffu, acc, 0), __shfl_sync(0xffffffffu, acc, 1));
+}
+
+__device__ float2 obstacle_force(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane);
+
 // ObjectInteractionForces::ComputeForce: ObjectInteractionForces.cpp:26-48
 // (agents only; obstacles add (0,0)); GoalReachingForce.cpp:26-29.
 // Lanes evaluate one neighbour each into shared memory; lane 0 then adds the
@@ -906,16 +1054,17 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 	}
 	// neighbours beyond the cost's range hold +0.0 (see ordered_sums)
 	__syncwarp();
-	float acc = 0.0f;
-	if (lane < 2) {
-		const float* src = lane ? fy : fx;
-		for (int k = 0; k < N.K; ++k) acc += src[k];
-	}
-	const float ax = __shfl_sync(0xffffffffu, acc, 0);
-	const float ay = __shfl_sync(0xffffffffu, acc, 1);
+	const float2 sum = list_sum(fx, fy, N.K, lane);
 	__syncwarp();
-	// obstacle edges within the cost's range, summed in list order; PowerLaw
-	// has no obstacle force (PowerLaw.cpp:68-72: a zero vector each)
+	return vadd(sum, obstacle_force(A, N, c, lane));
+}
+
+// The obstacle edges within cost c's range, summed in list order
+// (ObjectInteractionForces.cpp:40-45); PowerLaw has no obstacle force
+// (PowerLaw.cpp:68-72: a zero vector each).
+__device__ float2 obstacle_force(const AgentCtx& A, const NbView& N, const CostDesc& c, int lane)
+{
+	const float rs = c.range * c.range;
 	float2 obs = V(0, 0);
 	if (c.kind == K_SOCIALFORCES) {
 		for (int b0 = 0; b0 < N.KO; b0 += 32) {
@@ -930,7 +1079,7 @@ __device__ float2 compute_force(const AgentCtx& A, const NbView& N, const CostDe
 			obs = ordered_accumulate(obs, f, take);
 		}
 	}
-	return vadd(V(ax, ay), obs);
+	return obs;
 }
 
 // ForceBasedFunction::ComputeTargetVelocity: ForceBasedFunction.cpp:48-52
@@ -1420,6 +1569,696 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 // the differentiable form's backward pass
 // OBST: the obstacle-edge gather compiled in (the force-only kernel of
 // obstacle-free groups leaves it out, which keeps its registers)
+// Agent::UpdateVelocityAndPosition (agent.cpp:71-93) for one agent: the
+// contact force over the agent mass (80) added to the policy's velocity nv,
+// the viewing direction, the new position (wrapped in toric worlds:
+// worldToric.cpp:81-108).
+__device__ __forceinline__ void update_agent(const DevState& S, const ScenDesc& sd, int slot, float2 pos,
+                                             float2 pref, float dt, float2 nv, float2 contact)
+{
+	const float2 af = vdiv(contact, 80.0f);
+	const float2 vel = vadd(nv, vmul(af, dt));
+	const float2 vd = vdiv(vadd(vmul(vel, 2), pref), 3);
+	// (double)|vd|^2 > 0.01 <=> |vd|^2 > 0.01f (0.01f is the float just below 0.01)
+	if (vsq(vd) > 0.01f) S.view[slot] = vnorm(vd);
+	float2 p = vadd(pos, vmul(vel, dt));
+	if (sd.world == W_TORIC) {
+		const float hw = 0.5f * sd.width, hh = 0.5f * sd.height;
+		float x = p.x, y = p.y;
+		if (x > hw) x -= sd.width;
+		else if (x < -hw) x += sd.width;
+		if (y > hh) y -= sd.height;
+		else if (y < -hh) y += sd.height;
+		p = V(x, y);
+	}
+	S.pos[slot] = p;
+	S.vel[slot] = vel;
+	S.vwf[slot] = nv;
+}
+
+// ------------------------------------------------------------------------
+// force-only policies
+// ------------------------------------------------------------------------
+// Policies of the gradient method whose costs are all force-based
+// (SocialForces, PowerLaw, GoalReaching) take this path.  Per agent the warp
+// gathers the neighbour list and evaluates the neighbour terms: pair forces
+// and contact forces in one pass over the list, each summed in list order.
+// The per-agent remainder (GoalReachingForce, the cost targets and gradient
+// step of policy.cpp:78-89, the clamps, Agent::UpdateVelocityAndPosition)
+// then runs for up to 32 agents at once, one per lane, from a per-warp
+// record in shared memory: t, the force of each cost (x, y), the contact
+// force (x, y).  The stride is odd, so lane j's record starts in bank j.
+constexpr int STASH_STRIDE = 2 + 2 * MAX_COSTS + 1;
+
+// The neighbour force of cost c (SocialForces or PowerLaw; agents, then
+// obstacle edges), as compute_force.  With contact_scale > 0 the same pass
+// over the list also forms the agents' contact forces (policy.cpp:107-125)
+// and sums them in list order into *contact.
+__device__ float2 force_and_contact(const AgentCtx& A, const NbView& N, const CostDesc& c, float contact_scale,
+                                    int lane, float* fx, float* fy, float2* contact)
+{
+	const float rs = c.range * c.range;
+	const bool sf = c.kind == K_SOCIALFORCES;
+	const SfConst SK = sf_const(A, c);
+	float2 cacc = V(0, 0);
+	for (int b0 = 0; b0 < N.K; b0 += 32) {
+		const int k = b0 + lane;
+		bool take = false;
+		float2 fc = V(0, 0);
+		if (k < N.K) {
+			const float2 np = nb_pos(N, k);
+			const float nr = nb_radius(N, k);
+			const float d2 = N.d2[k];
+			float2 f = V(0, 0);
+			if (d2 <= rs) f = sf ? sf_force(A, SK, np, nb_E(N, k), nr) : pl_force(A, c, np, nb_vel(N, k), nr);
+			fx[k] = f.x;
+			fy[k] = f.y;
+			if (contact_scale > 0) {
+				// d2 is |pos - neighbour|^2 computed exactly as vsq(diff); if it
+				// exceeds (r + r_j)^2 by 1e-5 relative, sqrt(d2) >= r + r_j and
+				// the overlap test is false
+				const float rsum = A.radius + nr;
+				if (!(d2 > rsum * rsum * 1.00001f)) {
+					const float2 diff = vsub(A.pos, np);
+					const float inter = rsum - vmag(diff);
+					if (inter > 0) { take = true; fc = vmul(vnorm(diff), contact_scale * inter); }
+				}
+			}
+		}
+		if (contact_scale > 0) cacc = ordered_accumulate(cacc, fc, take);
+	}
+	if (contact_scale > 0) *contact = cacc;
+	__syncwarp();
+	const float2 sum = list_sum(fx, fy, N.K, lane);
+	__syncwarp();
+	return vadd(sum, obstacle_force(A, N, c, lane));
+}
+
+// The remainder of a batch of nb agents, lane j taking record j.
+template <bool TAPE>
+__device__ void finish_forces(const DevState& S, const float* stash, int nb, int lane)
+{
+	if (lane >= nb) return;
+	const float* rec = stash + lane * STASH_STRIDE;
+	const int t = __float_as_int(rec[0]);
+	const int slot = S.sSlot[t];
+	const float4 sb = S.sB[t];
+	const float4 prm = S.prm[slot];
+	const PolicyDesc& pol = S.pols[S.pol[slot]];
+	const ScenDesc& sd = S.scen[S.agent_scen[slot]];
+	const float2 pos = S.sP[t], vel = S.sV[t], pref = V(sb.x, sb.y);
+	const float dt = sd.dt;
+	float2 nv = V(0, 0);
+	if (!viszero(pref)) {
+		// Policy::getAccelerationFromGradient (policy.cpp:78-89) with
+		// ForceBasedFunction::GetGradient (ForceBasedFunction.cpp:32-36) and
+		// ComputeTargetVelocity (ForceBasedFunction.cpp:48-52)
+		float2 T = V(0, 0);
+		for (int ci = 0; ci < pol.ncost; ++ci) {
+			const CostDesc& c = pol.cost[ci];
+			const float2 F = c.kind == K_GOALREACHING ? vdiv(vsub(pref, vel), fmaxr(pol.relax_time, dt))
+			                                          : V(rec[1 + 2 * ci], rec[2 + 2 * ci]);
+			const float2 target = vadd(vel, vmul(vdiv(F, c.p[5]), dt));
+			T = vadd(T, vmul(vdiv(vsub(vel, target), dt), c.coeff));
+		}
+		const float2 acc = vclamp(vmul(T, -1), prm.w);
+		nv = vclamp(vadd(vel, vmul(acc, dt)), prm.z);
+		if (TAPE) S.tape_acc[slot] = vmul(T, -1);
+	}
+	update_agent(S, sd, slot, pos, pref, dt, nv, V(rec[2 * MAX_COSTS + 1], rec[2 * MAX_COSTS + 2]));
+}
+
+template <bool TAPE, bool OBST>
+__device__ void force_agents(const DevState& S, const WarpLists& L, float* stash, int lane, int gw, bool* overflow)
+{
+	float* fx = reinterpret_cast<float*>(L.nid);
+	float* fy = L.aux;
+	const int span = S.t_end - S.t_begin;
+	const int per = (span + S.total_warps - 1) / S.total_warps;
+	const int t0 = S.t_begin + (S.sched ? gw * per : gw), stride = S.sched ? 1 : S.total_warps;
+	const int tend = S.sched ? min(S.t_end, t0 + per) : S.t_end;
+	int nb = 0;
+	for (int t = t0; t < tend; t += stride) {
+		const int slot = S.sSlot[t];
+		const float4 sb = S.sB[t];
+		const float4 prm = S.prm[slot];
+		const PolicyDesc& pol = S.pols[S.pol[slot]];
+		AgentCtx A;
+		A.pos = S.sP[t]; A.vel = S.sV[t]; A.pref = V(sb.x, sb.y); A.goal = V(0, 0);
+		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
+		const int sc = S.agent_scen[slot];
+		const ScenDesc sd = S.scen[sc];
+		const GridParams G = S.grid[sc];
+		A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
+
+		const int K = gather(S, G, S.cell_base[sc], sd.world, sd.width, sd.height, L, t, A.pos, pol.range, lane, overflow);
+		NbView N;
+		N.ref = L.ref; N.d2 = L.key; N.K = K; N.sP = S.sP; N.sV = S.sV; N.sB = S.sB; N.sE = S.sE;
+		N.W = sd.width; N.H = sd.height;
+		N.edges = S.edges; N.obs = nullptr; N.KO = 0;
+		if (TAPE) {
+			for (int k = lane; k < K; k += 32) {
+				const uint32_t rr = L.ref[k];
+				S.tape_list[(size_t)slot * S.maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
+			}
+			if (lane == 0) S.tape_cnt[slot] = K;
+		}
+		if (OBST && sd.nedges > 0) {
+			uint32_t* ol = S.obs_list + (size_t)gw * S.max_obs;
+			N.KO = gather_obstacles(S, sd, A.pos, pol.range, lane, ol);
+			N.obs = ol;
+		}
+
+		float* rec = stash + nb * STASH_STRIDE;
+		float2 contact = V(0, 0);
+		bool contact_done = !(pol.contact_scale > 0);
+		if (!viszero(A.pref)) {
+			for (int ci = 0; ci < pol.ncost; ++ci) {
+				const CostDesc& c = pol.cost[ci];
+				if (c.kind == K_GOALREACHING) continue;
+				const float2 f = force_and_contact(A, N, c, contact_done ? 0.0f : pol.contact_scale, lane, fx, fy,
+				                                   &contact);
+				contact_done = true;
+				if (lane == 0) { rec[1 + 2 * ci] = f.x; rec[2 + 2 * ci] = f.y; }
+			}
+		}
+		// contact forces (policy.cpp:107-141): the agents, when no cost pass
+		// formed them, then the colliding obstacle edges
+		if (!contact_done) {
+			for (int b0 = 0; b0 < K; b0 += 32) {
+				const int k = b0 + lane;
+				bool take = false;
+				float2 f = V(0, 0);
+				if (k < K) {
+					const float rsum = A.radius + nb_radius(N, k);
+					if (!(N.d2[k] > rsum * rsum * 1.00001f)) {
+						const float2 diff = vsub(A.pos, nb_pos(N, k));
+						const float inter = rsum - vmag(diff);
+						if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
+					}
+				}
+				contact = ordered_accumulate(contact, f, take);
+			}
+		}
+		if (OBST && pol.contact_scale > 0) {
+			for (int b0 = 0; b0 < N.KO; b0 += 32) {
+				const int k = b0 + lane;
+				bool take = false;
+				float2 f = V(0, 0);
+				if (k < N.KO) {
+					float2 a, b;
+					nb_seg(N, k, &a, &b);
+					const float2 diff = vsub(A.pos, nearest_on_segment(A.pos, a, b));
+					const float inter = A.radius - vmag(diff);
+					if (inter > 0) { take = true; f = vmul(vnorm(diff), pol.contact_scale * inter); }
+				}
+				contact = ordered_accumulate(contact, f, take);
+			}
+		}
+		if (lane == 0) {
+			rec[0] = __int_as_float(t);
+			rec[2 * MAX_COSTS + 1] = contact.x;
+			rec[2 * MAX_COSTS + 2] = contact.y;
+		}
+		if (++nb == 32) {
+			__syncwarp();
+			finish_forces<TAPE>(S, stash, nb, lane);
+			__syncwarp();
+			nb = 0;
+		}
+	}
+	if (nb > 0) {
+		__syncwarp();
+		finish_forces<TAPE>(S, stash, nb, lane);
+	}
+}
+
+// ------------------------------------------------------------------------
+// force-only policies, four agents per warp
+// ------------------------------------------------------------------------
+// force_agents with eight lanes per agent: four agents per warp, consecutive
+// in cell order (so that their lists have similar lengths).  Every loop runs
+// warp-uniformly to the largest of the four agents' trip counts, each
+// agent's lanes predicated on their own; shuffles stay within an agent's
+// eight lanes (width 8) and each agent takes its byte of a ballot.  An
+// agent's list is two arrays in shared memory (reference, key); the force
+// pass overwrites each entry in place with its force terms (x over the key,
+// y over the reference).  Worlds without obstacle edges whose policies have
+// at most one neighbour cost (SocialForces or PowerLaw) take this path.
+constexpr int QG = 8, QN = 32 / QG;
+
+struct QLane {
+	int sg, sl;        // agent of this lane in the warp, lane within the agent
+	int shift;         // QG * sg
+	unsigned below;    // the agent's lanes below this one
+};
+__device__ __forceinline__ unsigned q_ballot(bool p, const QLane& q)
+{
+	return (__ballot_sync(0xffffffffu, p) >> q.shift) & 0xFFu;
+}
+template <class T>
+__device__ __forceinline__ T q_shfl(T v, int src) { return __shfl_sync(0xffffffffu, v, src, QG); }
+__device__ __forceinline__ int q_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
+
+// warp_sort_regs for an agent's eight lanes: P = 8 M <= 64 packed keys, M
+// per lane; entry i = 8 m + lane.  Exchanges at distances of 8 and more are
+// between a lane's own registers.  The sorted keys also give the near-tie
+// flags of fix_near_ties (pair (i, i+1) within the relative window win):
+// every lane of the agent returns the first and last flagged pair in *f0,
+// *f1 (*f0 > *f1 when none is flagged).
+template <int M>
+__device__ __forceinline__ void q_sort_regs(const WarpLists& L, int s, int len, const QLane& q, float win, int* f0,
+                                            int* f1)
+{
+	constexpr int P = QG * M;
+	static_assert(P <= 64, "positions take at most 6 bits");
+	constexpr int PB = P <= 32 ? 5 : 6;
+	constexpr uint32_t PMASK = (1u << PB) - 1u;
+	uint32_t u[M];
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * QG + q.sl;
+		u[m] = (i < len) ? ((__float_as_uint(L.key[s + i]) & ~PMASK) | (uint32_t)i) : 0xffffffffu;
+	}
+#pragma unroll
+	for (int size = 2; size <= P; size <<= 1) {
+#pragma unroll
+		for (int j = size >> 1; j > 0; j >>= 1) {
+#pragma unroll
+			for (int m = 0; m < M; ++m) {
+				const int i = m * QG + q.sl;
+				const bool up = (i & size) == 0;
+				if (j >= QG) {
+					const int mm = m ^ (j / QG);
+					if (mm > m) {
+						const uint32_t a = u[m], b = u[mm];
+						if (up ? (a > b) : (a < b)) { u[m] = b; u[mm] = a; }
+					}
+				} else {
+					const uint32_t o = __shfl_xor_sync(0xffffffffu, u[m], j, QG);
+					const bool lower = (q.sl & j) == 0;
+					u[m] = (lower == up) ? min(u[m], o) : max(u[m], o);
+				}
+			}
+		}
+	}
+	float k[M];
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * QG + q.sl;
+		const int from = s + (int)(u[m] & PMASK);
+		k[m] = (i < len) ? L.key[from] : 0.0f;
+		u[m] = (i < len) ? L.ref[from] : 0u;
+	}
+	__syncwarp();
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * QG + q.sl;
+		if (i < len) {
+			L.ref[s + i] = u[m];
+			L.key[s + i] = k[m];
+		}
+	}
+	int lo = 0x7fffffff, hi = -1;
+#pragma unroll
+	for (int m = 0; m < M; ++m) {
+		const int i = m * QG + q.sl;
+		// the key of entry i + 1: the next lane's, or lane 0's next register
+		const float a = __shfl_down_sync(0xffffffffu, k[m], 1, QG);
+		const float b = __shfl_sync(0xffffffffu, k[m + 1 < M ? m + 1 : m], 0, QG);
+		const float nx = q.sl < QG - 1 ? a : b;
+		if (i + 1 < len && nx - k[m] <= win * nx) { lo = min(lo, i); hi = max(hi, i); }
+	}
+#pragma unroll
+	for (int o = 1; o < QG; o <<= 1) {
+		lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o, QG));
+		hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o, QG));
+	}
+	*f0 = lo;
+	*f1 = hi;
+	__syncwarp();
+}
+
+// warp_sort (bitonic in shared memory, by (key, id)) for an agent's eight
+// lanes; the network is sized for the longest of the four lists.
+__device__ void q_sort_smem(const DevState& S, const WarpLists& L, int s, int len, int netlen, const QLane& q)
+{
+	if (netlen <= 1) return;
+	int lp = 0;
+	while ((1 << lp) < netlen) ++lp;
+	const int halfP = 1 << (lp - 1);
+	for (int ls = 1; ls <= lp; ++ls) {
+		const int lh = ls - 1;
+		for (int k = q.sl; k < halfP; k += QG) {
+			const int blk = k >> lh, pos = k & ((1 << lh) - 1);
+			const int lo = (blk << ls) + pos, hi = (blk << ls) + (1 << ls) - 1 - pos;
+			if (hi < len) nb_cmpswap(S, L, s + lo, s + hi);
+		}
+		__syncwarp();
+		for (int lj = lh - 1; lj >= 0; --lj) {
+			for (int k = q.sl; k < halfP; k += QG) {
+				const int lo = ((k >> lj) << (lj + 1)) | (k & ((1 << lj) - 1)), hi = lo + (1 << lj);
+				if (hi < len) nb_cmpswap(S, L, s + lo, s + hi);
+			}
+			__syncwarp();
+		}
+	}
+}
+
+// The first and last pair (i, i+1) of the agent's sorted list [s, e) whose
+// keys are within the relative window win (as fix_near_ties; *f0 > *f1 when
+// none), on every lane of the agent.
+__device__ void q_near_ties(const WarpLists& L, int s, int e, const QLane& q, float win, int* f0, int* f1)
+{
+	const int npairs = e - 1 - s;
+	const int pmax = q_max(npairs);
+	int lo = 0x7fffffff, hi = -1;
+	for (int b = 0; b < pmax; b += QG) {
+		const int i = b + q.sl;
+		if (i < npairs) {
+			const float a = L.key[s + i], c = L.key[s + i + 1];
+			if (c - a <= win * c) { lo = min(lo, i); hi = max(hi, i); }
+		}
+	}
+#pragma unroll
+	for (int o = 1; o < QG; o <<= 1) {
+		lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o, QG));
+		hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o, QG));
+	}
+	*f0 = lo;
+	*f1 = hi;
+}
+
+// fix_near_ties for an agent's eight lanes, given its first and last flagged
+// pairs f0 <= f1 (relative to s): the agent's first lane walks the pairs
+// between them and re-sorts each run of near-equal keys in the reference's
+// order (runs are disjoint, and re-sorting one changes no flag of the pairs
+// after it).
+__device__ void q_fix_near_ties(const DevState& S, const WarpLists& L, int s, int f0, int f1, float2 qp,
+                                const QLane& q, float win)
+{
+	if (!__any_sync(0xffffffffu, f0 <= f1)) return;
+	__syncwarp();
+	if (f0 <= f1 && q.sl == 0) {
+		int k = s + f0;
+		const int kend = s + f1;   // the last flagged pair
+		while (k <= kend) {
+			const float a = L.key[k], c = L.key[k + 1];
+			if (c - a <= win * c) {
+				const int r0 = k;
+				++k;
+				while (k <= kend) {
+					const float a2 = L.key[k], c2 = L.key[k + 1];
+					if (!(c2 - a2 <= win * c2)) break;
+					++k;
+				}
+				sort_run(S, L, r0, k, qp);   // pairs r0 .. k-1 flagged: entries r0 .. k
+			}
+			++k;
+		}
+	}
+	__syncwarp();
+}
+
+// gather for an agent's eight lanes (live false: an empty list).
+__device__ int q_gather(const DevState& S, const GridParams& G, int cb, int world, float W, float H,
+                        const WarpLists& L, int t, float2 p, float r, bool live, const QLane& q, bool* overflow)
+{
+	int K = 0, K0 = 0;
+	const int maxnb = S.maxnb;
+	live = live && r > 0;   // dist < r*r never holds for r = 0
+	const float r2 = r * r;
+	const double r2d = (double)r2;
+	const float r2lo = r2 * 0.999999f, r2hi = r2 * 1.000001f;
+	for (int g = 0; g < 5; ++g) {
+		float2 disp = V(0, 0);
+		bool active = live;
+		if (g > 0) {
+			// worldToric.cpp:64-76 (see gather)
+			if (world != W_TORIC) active = false;
+			else if (g == 1) { active = active && (p.x - r) < -0.5f * W; disp = V(W, 0); }
+			else if (g == 2) { active = active && (p.x + r) > 0.5f * W; disp = V(-W, 0); }
+			else if (g == 3) { active = active && (p.y - r) < -0.5f * H; disp = V(0, H); }
+			else { active = active && (p.y + r) > 0.5f * H; disp = V(0, -H); }
+		}
+		if (__any_sync(0xffffffffu, active)) {
+			const float2 qp = vadd(p, disp);
+			const int gs = K;
+			int cx0 = 0, cx1 = -1, cy0 = 0, nrows = 0;
+			if (active) {
+				cx0 = cell_coord((qp.x - r - G.x0) * G.inv_cs - 0.01f, 0.0f, 1.0f, G.nx);
+				cx1 = cell_coord((qp.x + r - G.x0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.nx);
+				cy0 = cell_coord((qp.y - r - G.y0) * G.inv_cs - 0.01f, 0.0f, 1.0f, G.ny);
+				const int cy1 = cell_coord((qp.y + r - G.y0) * G.inv_cs + 0.01f, 0.0f, 1.0f, G.ny);
+				nrows = cy1 - cy0 + 1;
+			}
+			const int maxrows = q_max(nrows);
+			// QG rows at a time: lane k loads the sorted range of row k, the rows
+			// are concatenated and scanned two chunks of QG candidates per pass
+			for (int r0 = 0; r0 < maxrows; r0 += QG) {
+				const int nr = nrows - r0;
+				int rs = 0, len = 0;
+				if (q.sl < nr) {
+					const int c0 = cb + (cy0 + r0 + q.sl) * G.nx;
+					rs = S.start[c0 + cx0];
+					len = S.start[c0 + cx1 + 1] - rs;
+				}
+				int incl = len;
+#pragma unroll
+				for (int o = 1; o < QG; o <<= 1) {
+					const int v = __shfl_up_sync(0xffffffffu, incl, o, QG);
+					if (q.sl >= o) incl += v;
+				}
+				const int beg = incl - len;
+				const int total = q_shfl(incl, QG - 1);
+				const int maxtotal = q_max(total);
+				for (int base = 0; base < maxtotal; base += 2 * QG) {
+					const int nh = base + QG < maxtotal ? 2 : 1;
+					int tt[2];
+					float2 cp[2];
+#pragma unroll
+					for (int h = 0; h < 2; ++h) {
+						if (h >= nh) break;
+						const int c = base + QG * h + q.sl;
+						int rr = 0;
+#pragma unroll
+						for (int step = QG / 2; step > 0; step >>= 1)
+							if (q_shfl(beg, rr + step) <= c) rr += step;
+						tt[h] = q_shfl(rs, rr) + (c - q_shfl(beg, rr));
+						cp[h] = (c < total && tt[h] != t) ? S.sP[tt[h]] : V(0, 0);
+					}
+#pragma unroll
+					for (int h = 0; h < 2; ++h) {
+						if (h >= nh) break;
+						const int c = base + QG * h + q.sl;
+						bool ok = false;
+						float d2f = 0;
+						if (c < total && tt[h] != t) {
+							const float dx = qp.x - cp[h].x, dy = qp.y - cp[h].y;
+							d2f = dx * dx + dy * dy;
+							if (d2f < r2lo) ok = true;
+							else if (d2f <= r2hi) ok = exact_key(qp, cp[h]) < r2d;
+						}
+						const unsigned m = q_ballot(ok, q);
+						if (ok) {
+							const int idx = K + __popc(m & q.below);
+							if (idx < maxnb) {
+								L.ref[idx] = ((uint32_t)g << 28) | (uint32_t)tt[h];
+								L.key[idx] = d2f;
+							}
+						}
+						K += __popc(m);
+					}
+				}
+			}
+			if (K > maxnb) { *overflow = true; K = maxnb; }
+			__syncwarp();
+			// one register network (64 entries: a single instantiation keeps
+			// the kernel's code small), the shared-memory sort beyond it
+			const int len = K - gs;
+			const int lmax = q_max(len);
+			const float win = lmax <= 64 ? 0x1p-16f : 1e-6f;
+			int f0, f1;
+			if (lmax <= 64) {
+				q_sort_regs<8>(L, gs, len, q, win, &f0, &f1);
+			} else {
+				q_sort_smem(S, L, gs, len, lmax, q);
+				q_near_ties(L, gs, K, q, win, &f0, &f1);
+			}
+			q_fix_near_ties(S, L, gs, f0, f1, qp, q, win);
+		}
+		if (g == 0) K0 = K;
+	}
+	// PhantomAgent::distSqr of the displaced entries (see gather)
+	const int dmax = q_max(K - K0);
+	for (int b = 0; b < dmax; b += QG) {
+		const int k = K0 + b + q.sl;
+		if (k < K) {
+			const uint32_t rr = L.ref[k];
+			const float2 ph = vadd(S.sP[rr & 0x0FFFFFFFu], group_offset(rr >> 28, W, H));
+			L.key[k] = vsq(vsub(p, ph));
+		}
+	}
+	__syncwarp();
+	return K;
+}
+
+// force_and_contact for an agent's eight lanes, writing the force terms in
+// place.  c: the agent's neighbour cost (null: none, or a zero preferred
+// velocity); contact_scale 0: no contact forces.  Returns the cost's force
+// (agents, then the (0, 0) of the absent obstacles), on all of the agent's
+// lanes.
+__device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists& L, int K, const CostDesc* c,
+                          float contact_scale, float W, float H, const QLane& q, float2* contact)
+{
+	const float rs = c ? c->range * c->range : -1.0f;
+	const bool sf = c && c->kind == K_SOCIALFORCES;
+	SfConst SK = {};
+	if (c) SK = sf_const(A, *c);
+	float2 cacc = V(0, 0);
+	const int kmax = q_max(K);
+	for (int b0 = 0; b0 < kmax; b0 += QG) {
+		const int k = b0 + q.sl;
+		bool take = false;
+		float2 fc = V(0, 0);
+		if (k < K) {
+			const uint32_t rr = L.ref[k];
+			const int j = (int)(rr & 0x0FFFFFFFu);
+			const float2 np = vadd(S.sP[j], group_offset(rr >> 28, W, H));
+			const float nr = S.sB[j].z;
+			const float d2 = L.key[k];
+			float2 f = V(0, 0);
+			if (d2 <= rs) f = sf ? sf_force(A, SK, np, S.sE[j], nr) : pl_force(A, *c, np, S.sV[j], nr);
+			L.key[k] = f.x;
+			L.ref[k] = __float_as_uint(f.y);
+			if (contact_scale > 0) {
+				// policy.cpp:107-125 (see force_and_contact)
+				const float rsum = A.radius + nr;
+				if (!(d2 > rsum * rsum * 1.00001f)) {
+					const float2 diff = vsub(A.pos, np);
+					const float inter = rsum - vmag(diff);
+					if (inter > 0) { take = true; fc = vmul(vnorm(diff), contact_scale * inter); }
+				}
+			}
+		}
+		// contact terms added in list order
+		unsigned m = q_ballot(take, q);
+		while (__any_sync(0xffffffffu, m != 0u)) {
+			const int src = m ? __ffs(m) - 1 : 0;
+			const float fx = q_shfl(fc.x, src), fy = q_shfl(fc.y, src);
+			if (m) {
+				cacc.x += fx;
+				cacc.y += fy;
+				m &= m - 1;
+			}
+		}
+	}
+	*contact = cacc;
+	__syncwarp();
+	// the sums in list order: lane 0 the x terms, lane 1 the y terms
+	float acc = 0.0f;
+	if (c && q.sl < 2) {
+		const uint32_t* src = q.sl ? L.ref : reinterpret_cast<const uint32_t*>(L.key);
+		int k = 0;
+		for (; k + 8 <= K; k += 8) {
+			float v[8];
+#pragma unroll
+			for (int jj = 0; jj < 8; ++jj) v[jj] = __uint_as_float(src[k + jj]);
+#pragma unroll
+			for (int jj = 0; jj < 8; ++jj) acc += v[jj];
+		}
+		for (; k < K; ++k) acc += __uint_as_float(src[k]);
+	}
+	const float2 sum = V(q_shfl(acc, 0), q_shfl(acc, 1));
+	__syncwarp();
+	return vadd(sum, V(0, 0));
+}
+
+constexpr int QPAD = 8;
+__host__ __device__ constexpr size_t q_words(int maxnb) { return 2 * (size_t)maxnb + QPAD; }
+
+template <bool TAPE>
+__global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
+{
+	extern __shared__ unsigned char smem[];
+	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
+	const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+	QLane q;
+	q.sg = lane / QG; q.sl = lane % QG; q.shift = QG * q.sg; q.below = (1u << q.sl) - 1u;
+	const int maxnb = S.maxnb;
+	// an agent's arrays start QPAD words (8 banks) after the previous agent's
+	// and its keys QPAD / 2 words after its references, so that the four
+	// agents' lanes, and an agent's two summing lanes, fall in distinct banks
+	uint32_t* lists = reinterpret_cast<uint32_t*>(smem) + ((size_t)wib * QN + q.sg) * q_words(maxnb);
+	const WarpLists L{ lists, reinterpret_cast<float*>(lists + maxnb + QPAD / 2), nullptr, nullptr };
+	float* stash = reinterpret_cast<float*>(smem) + (size_t)(blockDim.x >> 5) * QN * q_words(maxnb) + wib * 32 * STASH_STRIDE;
+	bool overflow = false;
+
+	const int span = S.t_end - S.t_begin;
+	const int nq = (span + QN - 1) / QN;
+	const int per = (nq + S.total_warps - 1) / S.total_warps;
+	const int q0 = S.sched ? gw * per : gw, qstride = S.sched ? 1 : S.total_warps;
+	const int qend = S.sched ? min(nq, q0 + per) : nq;
+	int nb = 0;
+	for (int qi = q0; qi < qend; qi += qstride) {
+		const int t = S.t_begin + qi * QN + q.sg;
+		const bool valid = t < S.t_end;
+		const int tc = valid ? t : S.t_end - 1;   // in-range loads for a missing fourth agent
+		const int slot = S.sSlot[tc];
+		const float4 sb = S.sB[tc];
+		const float4 prm = S.prm[slot];
+		const PolicyDesc& pol = S.pols[S.pol[slot]];
+		AgentCtx A;
+		A.pos = S.sP[tc]; A.vel = S.sV[tc]; A.pref = V(sb.x, sb.y); A.goal = V(0, 0);
+		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
+		const int sc = S.agent_scen[slot];
+		const ScenDesc& sd = S.scen[sc];
+		const GridParams G = S.grid[sc];
+		A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
+		const float W = sd.width, H = sd.height;
+
+		const int K = q_gather(S, G, S.cell_base[sc], sd.world, W, H, L, t, A.pos, pol.range, valid, q, &overflow);
+		if (TAPE) {
+			const int kmax = q_max(K);
+			for (int b = 0; b < kmax; b += QG) {
+				const int k = b + q.sl;
+				if (k < K) {
+					const uint32_t rr = L.ref[k];
+					S.tape_list[(size_t)slot * maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
+				}
+			}
+			if (valid && q.sl == 0) S.tape_cnt[slot] = K;
+			__syncwarp();
+		}
+		int ci = -1;
+		for (int k = 0; k < pol.ncost; ++k)
+			if (pol.cost[k].kind != K_GOALREACHING) ci = k;
+		const CostDesc* cd = (valid && ci >= 0 && !viszero(A.pref)) ? &pol.cost[ci] : nullptr;
+		float2 contact;
+		const float2 f = q_force(S, A, L, K, cd, valid ? pol.contact_scale : 0.0f, W, H, q, &contact);
+		if (valid && q.sl == 0) {
+			float* rec = stash + (nb + q.sg) * STASH_STRIDE;
+			rec[0] = __int_as_float(t);
+			if (ci >= 0) { rec[1 + 2 * ci] = f.x; rec[2 + 2 * ci] = f.y; }
+			rec[2 * MAX_COSTS + 1] = contact.x;
+			rec[2 * MAX_COSTS + 2] = contact.y;
+		}
+		nb += __popc(__ballot_sync(0xffffffffu, valid && q.sl == 0));
+		if (nb > 32 - QN) {
+			__syncwarp();
+			finish_forces<TAPE>(S, stash, nb, lane);
+			__syncwarp();
+			nb = 0;
+		}
+	}
+	if (nb > 0) {
+		__syncwarp();
+		finish_forces<TAPE>(S, stash, nb, lane);
+	}
+	if (__any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
+}
+
 template <int MODE, bool TAPE = false, bool OBST = true>
 __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
 {
@@ -1431,11 +2270,17 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	uint32_t* base = reinterpret_cast<uint32_t*>(smem) + (size_t)wib * 4 * maxnb;
 	WarpLists L{ base, reinterpret_cast<float*>(base + maxnb), reinterpret_cast<int*>(base + 2 * maxnb),
 	             reinterpret_cast<float*>(base + 3 * maxnb) };
+	bool overflow = false;
+	if constexpr (MODE == 1) {
+		float* stash = reinterpret_cast<float*>(smem) + (size_t)(blockDim.x >> 5) * 4 * maxnb + wib * 32 * STASH_STRIDE;
+		force_agents<TAPE, OBST>(S, L, stash, lane, gw, &overflow);
+		if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
+		return;
+	}
 	float* fx = reinterpret_cast<float*>(L.nid);   // per-neighbour terms
 	float* fy = L.aux;
 	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
 	float4* proj = lines + maxnb;
-	bool overflow = false;
 
 	const int span = S.t_end - S.t_begin;
 	const int per = (span + S.total_warps - 1) / S.total_warps;
@@ -1524,25 +2369,13 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		float2 nv = V(0, 0);
 		uint32_t rng_next = 0;
 		bool rng_used = false;
-		if (MODE == 1 && !viszero(A.pref)) {
-			// Policy::getAccelerationFromGradient (policy.cpp:78-89) with
-			// ForceBasedFunction::GetGradient (ForceBasedFunction.cpp:32-36)
-			float2 T = V(0, 0);
-			for (int ci = 0; ci < pol.ncost; ++ci) {
-				const CostDesc& c = pol.cost[ci];
-				const float2 target = target_velocity(A, N, c, lane, fx, fy);
-				T = vadd(T, vmul(vdiv(vsub(A.vel, target), A.dt), c.coeff));
-			}
-			const float2 acc = vclamp(vmul(T, -1), A.maxacc);
-			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
-			if (TAPE && lane == 0) S.tape_acc[slot] = vmul(T, -1);
-		} else if (MODE == 0 && !viszero(A.pref)) {
+		if (!viszero(A.pref)) {
 			CostPrep P;
 			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
 			for (int ci = 0; ci < pol.ncost; ++ci) {
 				const CostDesc& c = pol.cost[ci];
 				if (is_force_based(c.kind)) P.target[ci] = target_velocity(A, N, c, lane, fx, fy);
-				else if (MODE == 0 && c.kind == K_KARAMOUZAS) {
+				else if (c.kind == K_KARAMOUZAS) {
 					// TTC at the preferred velocity: a min, so lanes split the neighbours
 					float m = MAXF;
 					const float md2 = c.range * c.range;
@@ -1567,7 +2400,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					P.ttcp[ci] = m;
 					P.maxdev[ci] = karamouzas_maxdev(m);
 					P.cosdev[ci] = cosf(P.maxdev[ci]);
-				} else if (MODE == 0 && c.kind == K_ORCA) {
+				} else if (c.kind == K_ORCA) {
 					P.orca_v = orca_solve(A, N, c, lines, proj, &P.nlines, lane);
 				}
 			}
@@ -1579,7 +2412,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 				for (int ci = 0; ci < pol.ncost; ++ci) {
 					const CostDesc& c = pol.cost[ci];
 					float2 g;
-					if (MODE == 1 || is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
+					if (is_force_based(c.kind)) g = vdiv(vsub(A.vel, P.target[ci]), A.dt);
 					else if (c.kind == K_RANDOM) {
 						// RandomFunction::GetGradient (RandomFunction.cpp:30-33): two
 						// numbers in [-1, 1]; the reference build evaluates the
@@ -1619,7 +2452,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					rng_used = true;
 					rng_next = mulmod(S.lcgpow[grad_draws], S.rng[slot]);
 				}
-			} else if (MODE == 0) {
+			} else {
 				float2 best;
 				const CostDesc& c0 = pol.cost[0];
 				if (pol.method == M_GLOBAL && pol.ncost == 1 && c0.kind == K_ORCA) best = P.orca_v;
@@ -1637,8 +2470,6 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 					}
 				}
 				acc = vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt));
-			} else {
-				acc = V(0, 0);
 			}
 			acc = vclamp(acc, A.maxacc);
 			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
@@ -1646,24 +2477,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 
 		// phase 6: Agent::UpdateVelocityAndPosition (agent.cpp:71-93)
 		if (lane == 0) {
-			const float2 af = vdiv(contact, 80.0f);
-			const float2 vel = vadd(nv, vmul(af, A.dt));
-			const float2 vd = vdiv(vadd(vmul(vel, 2), A.pref), 3);
-			// (double)|vd|^2 > 0.01 <=> |vd|^2 > 0.01f (0.01f is the float just below 0.01)
-			if (vsq(vd) > 0.01f) S.view[slot] = vnorm(vd);
-			float2 p = vadd(A.pos, vmul(vel, A.dt));
-			if (sd.world == W_TORIC) {   // worldToric.cpp:81-108
-				const float hw = 0.5f * sd.width, hh = 0.5f * sd.height;
-				float x = p.x, y = p.y;
-				if (x > hw) x -= sd.width;
-				else if (x < -hw) x += sd.width;
-				if (y > hh) y -= sd.height;
-				else if (y < -hh) y += sd.height;
-				p = V(x, y);
-			}
-			S.pos[slot] = p;
-			S.vel[slot] = vel;
-			S.vwf[slot] = nv;
+			update_agent(S, sd, slot, A.pos, A.pref, A.dt, nv, contact);
 			if (rng_used) S.rng[slot] = rng_next;
 		}
 		__syncwarp();
@@ -2126,6 +2940,8 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	int dev = 0;
 	CK(cudaGetDevice(&dev));
 	CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+	CK(cudaFuncSetAttribute(k_scan_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes(SCAN_SMEM_MAX_CELLS)));
+	CK(cudaFuncSetAttribute(k_count_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes(SCAN_SMEM_MAX_CELLS)));
 	CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
 	CK(cudaMallocHost(&status_host_, sizeof(int)));
 	for (cudaEvent_t* e : { &ev0_, &ev1_, &pa0_, &pa1_, &ps0_, &ps1_ }) CK(cudaEventCreate(e));
@@ -2212,6 +3028,15 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			if ((int)scen_order_.size() > j0) {
 				KGroup g{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 };
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
+				g.quad = g.mode == 1 && !g.obst;
+				for (size_t pi = 0; pi < pols_.size(); ++pi) {
+					bool in_group = false;
+					for (int j = j0; j < g.j1; ++j) in_group |= pol_scen_[pi] == scen_order_[j];
+					if (!in_group) continue;
+					int nbc = 0;
+					for (int c2 = 0; c2 < pols_[pi].ncost; ++c2) nbc += pols_[pi].cost[c2].kind != K_GOALREACHING;
+					if (nbc > 1) g.quad = false;
+				}
 				groups_.push_back(g);
 			}
 		}
@@ -2392,8 +3217,10 @@ bool Engine::alloc(int cap)
 	    !dalloc(S.sB, cap, err_) || !dalloc(S.sE, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
 	    !dalloc(S.cell, cap, err_) || !dalloc(S.agent_scen, cap, err_) || !dalloc(S.cnt, mc + 1, err_) ||
 	    !dalloc(S.start, mc + 1, err_) || !dalloc(S.fill, mc + 1, err_) ||
-	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 2, err_))
+	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 3, err_))
 		return false;
+	S.ticket = reinterpret_cast<unsigned*>(S.blocksum + mc / SCAN_PER_BLOCK + 2);
+	CK(cudaMemset(S.ticket, 0, sizeof(unsigned)));
 	if (!S.grid && !dalloc(S.grid, ns, err_)) return false;
 	if (!S.bbox && !dalloc(S.bbox, 4 * ns, err_)) return false;
 	if (!S.cell_base && !dalloc(S.cell_base, ns + 1, err_)) return false;
@@ -2528,10 +3355,12 @@ bool Engine::download_mutable()
 	return true;
 }
 
-// The neighbour-list capacity is sized from the initial state: twice the
-// largest list, rounded up to a power of two (at least 128).  A list that
-// later outgrows it sets ST_NEIGHBOUR_OVERFLOW; sync() then re-runs the batch
-// from its snapshot with the capacity doubled (up to 3072 entries).
+// The neighbour-list capacity is sized from the initial state: one and a
+// half times the largest list plus 16, rounded up to a multiple of 32 (at
+// least 64), which keeps the lists of four agents per warp within shared
+// memory at full occupancy.  A list that later outgrows it sets
+// ST_NEIGHBOUR_OVERFLOW; sync() then re-runs the batch from its snapshot with
+// the capacity doubled (up to 3072 entries).
 bool Engine::choose_maxnb()
 {
 	int want = opt_.max_neighbours;
@@ -2543,8 +3372,7 @@ bool Engine::choose_maxnb()
 		if (!neighbours(0, nullptr, nullptr, cnt.data())) { maxnb_ = saved; return false; }
 		int mx = 0;
 		for (int i = 0; i < n_; ++i) mx = std::max(mx, cnt[i]);
-		want = 128;
-		while (want < 2 * mx) want <<= 1;
+		want = std::max(64, std::min(3072, (mx + mx / 2 + 16 + 31) / 32 * 32));
 	}
 	if (want != maxnb_) {
 		maxnb_ = want;
@@ -2560,6 +3388,29 @@ void Engine::invalidate_graph()
 	graph_exec_ = nullptr;
 	graph_ = nullptr;
 	graph_valid_ = false;
+}
+
+// Dynamic shared memory of a k_agent launch: per warp the four neighbour
+// lists, and for the force-only kernel its per-lane agent records.
+static size_t agent_smem(int warps_per_block, int maxnb, int mode)
+{
+	size_t b = (size_t)warps_per_block * maxnb * 16;
+	if (mode == 1) b += (size_t)warps_per_block * 32 * STASH_STRIDE * sizeof(float);
+	return b;
+}
+
+// k_force_quad: per warp four agents' lists (reference, key) and the agent records
+static size_t quad_smem(int warps_per_block, int maxnb)
+{
+	return (size_t)warps_per_block * (QN * q_words(maxnb) + 32 * STASH_STRIDE) * sizeof(float);
+}
+
+static int quad_blocks_for(int num_sms, int warps_per_block, size_t smem)
+{
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_quad<false>, warps_per_block * 32, smem);
+	if (per_sm < 1) per_sm = 1;
+	return num_sms * per_sm;
 }
 
 static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int mode = 0, bool obst = true)
@@ -2579,14 +3430,21 @@ bool Engine::configure()
 {
 	DevState& S = *d_;
 	const int wpb = opt_.warps_per_block;
-	const size_t smem = (size_t)wpb * maxnb_ * 16;
-	if (smem > 48 * 1024) {
-		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		CK(cudaFuncSetAttribute(k_agent<1, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		CK(cudaFuncSetAttribute(k_agent<1, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	const size_t smem0 = agent_smem(wpb, maxnb_, 0), smem1 = agent_smem(wpb, maxnb_, 1);
+	const size_t smemq = quad_smem(wpb, maxnb_);
+	if (smemq > 48 * 1024) {
+		CK(cudaFuncSetAttribute(k_force_quad<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+	}
+	if (smem0 > 48 * 1024) {
+		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+	}
+	if (smem1 > 48 * 1024) {
+		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+		CK(cudaFuncSetAttribute(k_agent<1, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+		CK(cudaFuncSetAttribute(k_agent<1, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
 	}
 	mode_ = 1;
 	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
@@ -2596,7 +3454,8 @@ bool Engine::configure()
 	for (const auto& D : scen_) maxe = std::max(maxe, D.nedges);
 	S.max_obs = 5 * maxe;   // every edge, once per displacement group
 	for (auto& g : groups_) {
-		g.blocks = agent_blocks_for(num_sms_, wpb, smem, g.mode, g.obst);
+		g.blocks = g.quad ? quad_blocks_for(num_sms_, wpb, smemq)
+		                  : agent_blocks_for(num_sms_, wpb, g.mode == 1 ? smem1 : smem0, g.mode, g.obst);
 		if (opt_.occupancy < 1.0f) g.blocks = std::max(num_sms_, (int)(g.blocks * opt_.occupancy));
 		g.scratch_off = scr;
 		scr += (size_t)g.blocks * wpb * 2 * maxnb_;
@@ -2621,7 +3480,8 @@ void Engine::enqueue_step()
 	S.n = n_;
 	S.maxnb = maxnb_;
 	const int wpb = opt_.warps_per_block;
-	const size_t smem = (size_t)wpb * maxnb_ * 16;
+	const size_t smem0 = agent_smem(wpb, maxnb_, 0), smem1 = agent_smem(wpb, maxnb_, 1);
+	const size_t smemq = quad_smem(wpb, maxnb_);
 	S.counters = profile_ ? counters_ : nullptr;
 	enqueue_grid(S);
 	if (profile_) cudaEventRecord(pa0_, stream_);
@@ -2642,17 +3502,21 @@ void Engine::enqueue_step()
 		DevState A = S;
 		A.t_begin = tb[k]; A.t_end = te[k];
 		// no more blocks than the group has agents for (small worlds)
-		const int blocks = std::min(g.blocks, std::max(1, (te[k] - tb[k] + wpb - 1) / wpb));
+		const int per_block = g.quad ? wpb * QN : wpb;
+		const int blocks = std::min(g.blocks, std::max(1, (te[k] - tb[k] + per_block - 1) / per_block));
 		A.total_warps = blocks * wpb;
 		A.scratch = S.scratch + g.scratch_off;
 		A.obs_list = S.obs_list + g.obs_off;
-		if (S.tape_list) {
-			if (g.mode == 1 && g.obst) k_agent<1, true, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
-			else if (g.mode == 1) k_agent<1, true, false><<<blocks, wpb * 32, smem, st>>>(A, 0);
-			else k_agent<0, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
-		} else if (g.mode == 1 && g.obst) k_agent<1, false, true><<<blocks, wpb * 32, smem, st>>>(A, 0);
-		else if (g.mode == 1) k_agent<1, false, false><<<blocks, wpb * 32, smem, st>>>(A, 0);
-		else k_agent<0><<<blocks, wpb * 32, smem, st>>>(A, 0);
+		if (g.quad) {
+			if (S.tape_list) k_force_quad<true><<<blocks, wpb * 32, smemq, st>>>(A);
+			else k_force_quad<false><<<blocks, wpb * 32, smemq, st>>>(A);
+		} else if (S.tape_list) {
+			if (g.mode == 1 && g.obst) k_agent<1, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
+			else if (g.mode == 1) k_agent<1, true, false><<<blocks, wpb * 32, smem1, st>>>(A, 0);
+			else k_agent<0, true><<<blocks, wpb * 32, smem0, st>>>(A, 0);
+		} else if (g.mode == 1 && g.obst) k_agent<1, false, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
+		else if (g.mode == 1) k_agent<1, false, false><<<blocks, wpb * 32, smem1, st>>>(A, 0);
+		else k_agent<0><<<blocks, wpb * 32, smem0, st>>>(A, 0);
 	};
 	// one after the other: each launch fills the GPU (measured: running the
 	// groups on concurrent streams was no faster)
@@ -2683,9 +3547,16 @@ void Engine::enqueue_grid(const DevState& S)
 		k_bbox<<<nb, threads, 0, stream_>>>(S);
 		k_grid<<<1, 1024, 0, stream_>>>(S);
 	}
-	k_count<<<nb, threads, 0, stream_>>>(S);
 	const int cells_bound = grid_fixed ? static_cells_ : S.max_cells;
-	if (cells_bound <= SCAN_SINGLE_MAX_CELLS) {
+	if (grid_fixed && cells_bound <= SCAN_SMEM_MAX_CELLS) {
+		k_count_scan<<<std::max(1, (n_ + 1023) / 1024), 1024, scan_smem_bytes(cells_bound), stream_>>>(S, cells_bound);
+		k_scatter<<<nb, threads, 0, stream_>>>(S);
+		return;
+	}
+	k_count<<<nb, threads, 0, stream_>>>(S);
+	if (cells_bound <= SCAN_SMEM_MAX_CELLS) {
+		k_scan_smem<<<1, 1024, scan_smem_bytes(cells_bound), stream_>>>(S, cells_bound);
+	} else if (cells_bound <= SCAN_SINGLE_MAX_CELLS) {
 		k_scan_single<<<1, 1024, 0, stream_>>>(S);
 	} else {
 		const int sb = (S.max_cells + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
@@ -2737,7 +3608,9 @@ int Engine::kernels_per_step() const
 {
 	if (small_world()) return 1 + (int)groups_.size();
 	const bool grid_fixed = toric_only_ && static_grid_ready_;
-	const bool single = (grid_fixed ? static_cells_ : d_->max_cells) <= SCAN_SINGLE_MAX_CELLS;
+	const int cells_bound = grid_fixed ? static_cells_ : d_->max_cells;
+	if (grid_fixed && cells_bound <= SCAN_SMEM_MAX_CELLS) return 2 + (int)groups_.size();
+	const bool single = cells_bound <= SCAN_SINGLE_MAX_CELLS;
 	return (grid_fixed ? 0 : 2) + 1 + (single ? 1 : 3) + 1 + (int)groups_.size();
 }
 

@@ -209,6 +209,7 @@ private:
 		int blocks;
 		size_t scratch_off, obs_off;
 		bool obst = false;   // a scenario of the group has obstacle edges
+		bool quad = false;   // k_force_quad: force-only, no obstacle edges, at most one neighbour cost per policy
 	};
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
