@@ -159,8 +159,8 @@ def port_over_reference():
 
 
 def profiled_traffic_per_agent():
-    """dram bytes per agent of k_agent from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_agent_socialforces_toric.md")
+    """dram bytes per agent of k_force_quad from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_force_quad_socialforces_toric.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_agent:"):
@@ -556,6 +556,16 @@ def run_ours(args):
     import torch
     torch.cuda.set_device(local)
     with tempfile.TemporaryDirectory() as tmp:
+        if args.only_leg:
+            # one leg alone (a short command for profiling its kernels)
+            if args.only_leg == "batched":
+                flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+                out = batched_leg(tmp, min(args.steps, 20), args.warmup, flush, None)
+            else:
+                out = diff_leg(tmp, sets=args.diff_sets)
+            if rank == 0:
+                print(json.dumps({"leg": args.only_leg, "result": out}))
+            return
         legs = {}
         tl = time.perf_counter()
 
@@ -602,7 +612,7 @@ def run_ours(args):
         sim.synchronize()
         warm_ms = t0.elapsed_time(t1)
         sim.close()
-        # --- dominant kernel: k_agent, CUDA events on the engine's stream,
+        # --- dominant kernel: k_force_quad, CUDA events on the engine's stream,
         # over the same step range (fresh state); mean neighbour count sampled
         sim = Simulation(path)
         sim.step(args.warmup)
@@ -694,7 +704,7 @@ def run_ours(args):
                 "path": "SetAgentPositions -> DoSimulationSteps(1) -> GetAgentPositions, host buffers"},
         # the kernel's bound is min(HBM / bytes, FP32 / FLOPs) per agent-step;
         # with ~96 B and ~3.3 kFLOP per agent-step the FP32 term is the lower
-        "roofline": {"bound": "fp32", "kernel": "k_agent",
+        "roofline": {"bound": "fp32", "kernel": "k_force_quad",
                      "achieved": flops / (agent_ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": flops / (agent_ms * 1e-3) / 1e12 / fp32_peak,
                      "peak_source": f"nominal: {sms} SMs (from the device) x 128 FP32 lanes x 2 FLOP x "
@@ -709,14 +719,17 @@ def run_ours(args):
                      "frac_of_agent_steps_roofline": (n / (agent_ms * 1e-3)) /
                                                      min(peak * 1e9 / K_AGENT_BYTES_PER_AGENT,
                                                          fp32_peak * 1e12 / (flops / max(n, 1)))},
-        "hbm_roofline": {"kernel": "k_agent", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "hbm_roofline": {"kernel": "k_force_quad", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
                          "traffic": (tpa * n if tpa else None)},
-        "grid_build": {"kernels": "k_bbox..k_scatter", "ms": grid_ms, "alg_bytes_per_agent": GRID_BYTES_PER_AGENT,
+        "grid_build": {"kernels": "k_count_scan, k_scatter (static toric grid)", "ms": grid_ms,
+                       "ms_in_graph": t_ms / args.steps - agent_ms,
+                       "alg_bytes_per_agent": GRID_BYTES_PER_AGENT,
                        "achieved": GRID_BYTES_PER_AGENT * n / (grid_ms * 1e-3) / 1e9 if grid_ms > 0 else None,
                        "peak": peak, "unit": "GB/s",
                        "frac": GRID_BYTES_PER_AGENT * n / (grid_ms * 1e-3) / 1e9 / peak if grid_ms > 0 else None,
-                       "note": "state of 100k agents (~13 MB) is L2-resident within a step; time includes launch gaps"},
+                       "note": "ms: profiled steps (separate launches, with their launch gaps); ms_in_graph: the "
+                               "graph-replayed step minus the agent kernel (grid build and graph launch)"},
         "clocks": clocks,
         "gpu_launches": prof["kernels_per_step"] * args.steps,
     }
@@ -752,6 +765,8 @@ def main():
     ap.add_argument("--agents", type=int, default=0,
                     help="agents of the SocialForces workload at the same density (default 100000)")
     ap.add_argument("--diff-sets", type=int, default=256, help="parameter sets of the differentiable leg")
+    ap.add_argument("--only-leg", choices=["batched", "diff"], default=None,
+                    help="run one leg alone and print its record (for profiling; not a bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

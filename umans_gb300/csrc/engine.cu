@@ -53,7 +53,7 @@ struct DevState {
 	float4* sB;
 	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces)
 	int *sSlot, *sId;
-	int *cell, *cnt, *start, *fill, *blocksum;
+	int *cell, *cnt, *start, *blocksum;   // cnt: per-cell histogram, zero between steps
 	unsigned* ticket;       // blocks of k_count_scan done (zero between launches)
 	GridParams* grid;       // [nscen]
 	unsigned* bbox;         // [4 * nscen]
@@ -222,7 +222,8 @@ __global__ void k_count(DevState S)
 	count_one(S, i, S.grid[sc], S.cell_base[sc]);
 }
 
-// exclusive scan of cnt[0..ncells) in 3 passes; 1024 cells per block
+// exclusive scan of cnt[0..ncells) into start in 3 passes; 1024 cells per
+// block (k_scatter takes the counts back to zero)
 constexpr int SCAN_BLOCK = 256, SCAN_PER_BLOCK = 1024;
 
 __global__ void k_scan_reduce(DevState S)
@@ -296,8 +297,6 @@ __global__ void k_scan_down(DevState S)
 		const int c = c0 + k;
 		if (c < nc) {
 			S.start[c] = run;
-			S.fill[c] = run;
-			S.cnt[c] = 0;   // histogram is all-zero between steps
 			run += v[k];
 		}
 	}
@@ -309,7 +308,8 @@ __global__ void k_scan_down(DevState S)
 // runs of cells fall in different banks): coalesced loads, eight in flight
 // per thread, then per thread a contiguous run of cells summed, a block scan
 // of the run sums, the runs rewritten with their prefixes, and a coalesced
-// write of start and fill, the histogram zeroed for the next step.
+// write of start.  (The histogram itself is left as it is: k_scatter counts
+// every cell back down to zero.)
 constexpr int SCAN_SMEM_MAX_CELLS = 49152;
 __host__ __device__ constexpr size_t scan_smem_bytes(int cells) { return sizeof(int) * ((size_t)cells + cells / 32 + 1); }
 __device__ __forceinline__ int scan_pad(int c) { return c + (c >> 5); }
@@ -362,14 +362,7 @@ __device__ void block_scan_cells(const DevState& S, int nc, int* sm)
 	}
 	__syncthreads();
 	int* __restrict__ start = S.start;
-	int* __restrict__ fill = S.fill;
-	int* __restrict__ zero = S.cnt;
-	for (int c = tid; c < nc; c += nt) {
-		const int v = sm[scan_pad(c)];
-		start[c] = v;
-		fill[c] = v;
-		zero[c] = 0;   // histogram is all-zero between steps
-	}
+	for (int c = tid; c < nc; c += nt) start[c] = sm[scan_pad(c)];
 	if (tid == 0) start[nc] = S.n;
 }
 
@@ -448,7 +441,6 @@ __global__ void __launch_bounds__(1024) k_scan_single(DevState S)
 	// they can be issued ahead of the stores
 	const int* __restrict__ cnt = S.cnt;
 	int* __restrict__ start = S.start;
-	int* __restrict__ fill = S.fill;
 	int run = wt[warp];
 #pragma unroll 4
 	for (int base = w0; base < w1; base += 32) {
@@ -459,14 +451,9 @@ __global__ void __launch_bounds__(1024) k_scan_single(DevState S)
 			const int u = __shfl_up_sync(0xffffffffu, incl, o);
 			if (lane >= o) incl += u;
 		}
-		if (c < w1) {
-			start[c] = run + incl - v;
-			fill[c] = run + incl - v;
-		}
+		if (c < w1) start[c] = run + incl - v;
 		run += __shfl_sync(0xffffffffu, incl, 31);
 	}
-	__syncthreads();
-	for (int c = w0 + lane; c < w1; c += 32) S.cnt[c] = 0;   // histogram is all-zero between steps
 	if (threadIdx.x == 0) S.start[nc] = S.n;
 }
 
@@ -477,10 +464,12 @@ __device__ __forceinline__ void scatter_one(const DevState& S, int i)
 	const unsigned peers = __match_any_sync(act, c);
 	const int lane = threadIdx.x & 31;
 	const int leader = __ffs(peers) - 1;
-	int base = 0;
-	if (lane == leader) base = atomicAdd(&S.fill[c], __popc(peers));
-	base = __shfl_sync(peers, base, leader);
-	const int t = base + __popc(peers & ((1u << lane) - 1u));
+	// the cell is filled from its top down: the histogram count is taken back
+	// by each agent placed, so it is all-zero again for the next step
+	int top = 0;
+	if (lane == leader) top = atomicSub(&S.cnt[c], __popc(peers));
+	top = __shfl_sync(peers, top, leader);
+	const int t = S.start[c] + top - __popc(peers) + __popc(peers & ((1u << lane) - 1u));
 	const float2 p = S.pos[i];
 	const float2 g = S.goal[i];
 	const float4 prm = S.prm[i];
@@ -550,8 +539,6 @@ __global__ void __launch_bounds__(1024) k_build_small(DevState S)
 	for (int c = c0; c < c1; ++c) {
 		const int v = __ldcg(&S.cnt[c]);
 		S.start[c] = run;
-		S.fill[c] = run;
-		S.cnt[c] = 0;   // histogram is all-zero between steps
 		run += v;
 	}
 	if (tid == 0) S.start[nc] = n;
@@ -3216,7 +3203,7 @@ bool Engine::alloc(int cap)
 	    !dalloc(S.rng, cap, err_) || !dalloc(S.sP, cap, err_) || !dalloc(S.sV, cap, err_) ||
 	    !dalloc(S.sB, cap, err_) || !dalloc(S.sE, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
 	    !dalloc(S.cell, cap, err_) || !dalloc(S.agent_scen, cap, err_) || !dalloc(S.cnt, mc + 1, err_) ||
-	    !dalloc(S.start, mc + 1, err_) || !dalloc(S.fill, mc + 1, err_) ||
+	    !dalloc(S.start, mc + 1, err_) ||
 	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 3, err_))
 		return false;
 	S.ticket = reinterpret_cast<unsigned*>(S.blocksum + mc / SCAN_PER_BLOCK + 2);
@@ -4475,7 +4462,7 @@ Engine::~Engine()
 	if (d_) {
 		DevState& S = *d_;
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,
-		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.fill, S.blocksum, S.grid, S.bbox, S.status,
+		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.blocksum, S.grid, S.bbox, S.status,
 		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io,
 		                 S.agent_scen, S.cell_base, scen_dev_, S.obs_list,
 		                 snap_pos_, snap_vel_, snap_view_, snap_vwf_, snap_rng_ };
