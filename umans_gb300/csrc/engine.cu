@@ -1548,10 +1548,11 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 // ------------------------------------------------------------------------
 // the fused per-agent step
 // ------------------------------------------------------------------------
-// MODE 0: any policy.  MODE 1: every policy uses the gradient method with
-// force-based costs only (SocialForcesAvoidance, PowerLaw,
-// GoalReachingForce); the sampling, ORCA and finite-difference code is
-// compiled out, which lowers register use and raises occupancy.
+// MODE 0: any policy.  MODE 1: every policy has force-based costs only
+// (SocialForcesAvoidance, PowerLaw, GoalReachingForce), whatever its method
+// (the velocity comes from the cost targets, finish_forces); the generic
+// sampling, ORCA and finite-difference code is compiled out, which lowers
+// register use and raises occupancy.
 // TAPE: also record the neighbour lists and the pre-clamp acceleration for
 // the differentiable form's backward pass
 // OBST: the obstacle-edge gather compiled in (the force-only kernel of
@@ -1586,12 +1587,12 @@ __device__ __forceinline__ void update_agent(const DevState& S, const ScenDesc& 
 // ------------------------------------------------------------------------
 // force-only policies
 // ------------------------------------------------------------------------
-// Policies of the gradient method whose costs are all force-based
-// (SocialForces, PowerLaw, GoalReaching) take this path.  Per agent the warp
+// Policies whose costs are all force-based (SocialForces, PowerLaw,
+// GoalReaching), whatever their method, take this path.  Per agent the warp
 // gathers the neighbour list and evaluates the neighbour terms: pair forces
 // and contact forces in one pass over the list, each summed in list order.
-// The per-agent remainder (GoalReachingForce, the cost targets and gradient
-// step of policy.cpp:78-89, the clamps, Agent::UpdateVelocityAndPosition)
+// The per-agent remainder (GoalReachingForce, the cost targets and the
+// method's choice of velocity, the clamps, Agent::UpdateVelocityAndPosition)
 // then runs for up to 32 agents at once, one per lane, from a per-warp
 // record in shared memory: t, the force of each cost (x, y), the contact
 // force (x, y).  The stride is odd, so lane j's record starts in bank j.
@@ -1641,8 +1642,39 @@ __device__ float2 force_and_contact(const AgentCtx& A, const NbView& N, const Co
 	return vadd(sum, obstacle_force(A, N, c, lane));
 }
 
-// The remainder of a batch of nb agents, lane j taking record j.
-template <bool TAPE>
+// Candidate velocity i of a sampling policy (costFunction.cpp:99-158): the
+// regular schedule from its table, or random sampling with the agent's
+// minstd_rand0 stream jumped ahead to the sample's draws.
+__device__ __forceinline__ float2 sample_velocity(const DevState& S, const PolicyDesc& pol, float2 base, float2 dir,
+                                                  float dL, float radius, uint32_t rng0, int i)
+{
+	if (pol.table_random) {
+		const float ma = pol.max_angle;
+		const uint32_t x1 = mulmod(S.lcgpow[i * pol.draws + 1], rng0);
+		const uint32_t x2 = mulmod(S.lcgpow[i * pol.draws + 2], rng0);
+		const float ra = rng_uniform(x1, -ma, ma);
+		const float rl = rng_uniform(x2, 0, radius);
+		float sn, cs;
+		host_sincosf(ra, &sn, &cs);
+		return vadd(base, vmul(vrot_cs(dir, cs, sn), rl));
+	}
+	const SampleEntry e = S.table[pol.table_offset + i];
+	return vadd(base, vmul(vrot_cs(dir, e.c, e.s), dL * e.mult));
+}
+
+// The remainder of a batch of nb agents, lane j taking record j.  The
+// policy's method picks the new velocity from the cost targets
+// (ForceBasedFunction::ComputeTargetVelocity, ForceBasedFunction.cpp:48-52):
+// - gradient: the gradient step of policy.cpp:78-89;
+// - global with one cost: its target, the cost's global minimum
+//   (ForceBasedFunction::GetGlobalMinimum);
+// - sampling, or global with several costs (the default schedule of
+//   SamplingParameters::ApproximateGlobalOptimization): the first sample of
+//   least summed cost 0.5 |v - target|^2 / dt (ForceBasedFunction.cpp:26-30,
+//   costFunction.cpp:60-95), one lane running the agent's samples in order.
+// SAMP false: every policy of the group uses the gradient method (the
+// other methods' code is compiled out).
+template <bool TAPE, bool SAMP>
 __device__ void finish_forces(const DevState& S, const float* stash, int nb, int lane)
 {
 	if (lane >= nb) return;
@@ -1657,25 +1689,68 @@ __device__ void finish_forces(const DevState& S, const float* stash, int nb, int
 	const float dt = sd.dt;
 	float2 nv = V(0, 0);
 	if (!viszero(pref)) {
-		// Policy::getAccelerationFromGradient (policy.cpp:78-89) with
-		// ForceBasedFunction::GetGradient (ForceBasedFunction.cpp:32-36) and
-		// ComputeTargetVelocity (ForceBasedFunction.cpp:48-52)
-		float2 T = V(0, 0);
-		for (int ci = 0; ci < pol.ncost; ++ci) {
-			const CostDesc& c = pol.cost[ci];
-			const float2 F = c.kind == K_GOALREACHING ? vdiv(vsub(pref, vel), fmaxr(pol.relax_time, dt))
-			                                          : V(rec[1 + 2 * ci], rec[2 + 2 * ci]);
-			const float2 target = vadd(vel, vmul(vdiv(F, c.p[5]), dt));
-			T = vadd(T, vmul(vdiv(vsub(vel, target), dt), c.coeff));
+		float2 acc;
+		if (!SAMP || pol.method == M_GRADIENT) {
+			float2 T = V(0, 0);
+			for (int ci = 0; ci < pol.ncost; ++ci) {
+				const CostDesc& c = pol.cost[ci];
+				const float2 F = c.kind == K_GOALREACHING ? vdiv(vsub(pref, vel), fmaxr(pol.relax_time, dt))
+				                                          : V(rec[1 + 2 * ci], rec[2 + 2 * ci]);
+				const float2 target = vadd(vel, vmul(vdiv(F, c.p[5]), dt));
+				T = vadd(T, vmul(vdiv(vsub(vel, target), dt), c.coeff));
+			}
+			acc = vmul(T, -1);
+			if (TAPE) S.tape_acc[slot] = acc;
+		} else {
+			float2 tg[MAX_COSTS];
+#pragma unroll
+			for (int ci = 0; ci < MAX_COSTS; ++ci) {
+				if (ci >= pol.ncost) break;
+				const CostDesc& c = pol.cost[ci];
+				const float2 F = c.kind == K_GOALREACHING ? vdiv(vsub(pref, vel), fmaxr(pol.relax_time, dt))
+				                                          : V(rec[1 + 2 * ci], rec[2 + 2 * ci]);
+				tg[ci] = vadd(vel, vmul(vdiv(F, c.p[5]), dt));
+			}
+			float2 best = V(0, 0);
+			if (!pol.use_sampling) {
+				best = tg[0];
+			} else {
+				// sample_min's schedule (base, direction, length step)
+				float2 base = V(0, 0);
+				if (pol.table_base == 1) base = vel;
+				float radius;
+				if (pol.table_radius == 0) radius = prm.y;
+				else if (pol.table_radius == 1) radius = prm.z;
+				else radius = fminr(2.0f * prm.z, prm.w * dt);
+				float2 dir = V(1, 0);
+				if (pol.table_dir == 1) dir = vnorm(vel);
+				else if (pol.table_dir == 2) dir = vnorm(pref);
+				const float dL = radius / (float)pol.len_divisor;
+				const uint32_t r0 = S.rng[slot];
+				float bestC = MAXF;
+				int bestI = -1;
+				for (int i = 0; i < pol.nsamples; ++i) {
+					const float2 v = sample_velocity(S, pol, base, dir, dL, radius, r0, i);
+					float tc = 0;
+#pragma unroll
+					for (int ci = 0; ci < MAX_COSTS; ++ci) {
+						if (ci >= pol.ncost) break;
+						tc += pol.cost[ci].coeff * (0.5f * vsq(vsub(v, tg[ci])) / dt);
+					}
+					if (tc < bestC) { bestC = tc; bestI = i; }
+				}
+				if (bestI >= 0) best = sample_velocity(S, pol, base, dir, dL, radius, r0, bestI);
+				if (pol.draws > 0) S.rng[slot] = mulmod(S.lcgpow[pol.nsamples * pol.draws], r0);
+			}
+			acc = vdiv(vsub(best, vel), fmaxr(pol.relax_time, dt));
 		}
-		const float2 acc = vclamp(vmul(T, -1), prm.w);
+		acc = vclamp(acc, prm.w);
 		nv = vclamp(vadd(vel, vmul(acc, dt)), prm.z);
-		if (TAPE) S.tape_acc[slot] = vmul(T, -1);
 	}
 	update_agent(S, sd, slot, pos, pref, dt, nv, V(rec[2 * MAX_COSTS + 1], rec[2 * MAX_COSTS + 2]));
 }
 
-template <bool TAPE, bool OBST>
+template <bool TAPE, bool OBST, bool SAMP>
 __device__ void force_agents(const DevState& S, const WarpLists& L, float* stash, int lane, int gw, bool* overflow)
 {
 	float* fx = reinterpret_cast<float*>(L.nid);
@@ -1769,14 +1844,14 @@ __device__ void force_agents(const DevState& S, const WarpLists& L, float* stash
 		}
 		if (++nb == 32) {
 			__syncwarp();
-			finish_forces<TAPE>(S, stash, nb, lane);
+			finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 			__syncwarp();
 			nb = 0;
 		}
 	}
 	if (nb > 0) {
 		__syncwarp();
-		finish_forces<TAPE>(S, stash, nb, lane);
+		finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 	}
 }
 
@@ -1807,16 +1882,18 @@ template <class T>
 __device__ __forceinline__ T q_shfl(T v, int src) { return __shfl_sync(0xffffffffu, v, src, QG); }
 __device__ __forceinline__ int q_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
 
-// warp_sort_regs for an agent's eight lanes: P = 8 M <= 64 packed keys, M
-// per lane; entry i = 8 m + lane.  Exchanges at distances of 8 and more are
-// between a lane's own registers.  The sorted keys also give the near-tie
-// flags of fix_near_ties (pair (i, i+1) within the relative window win):
-// every lane of the agent returns the first and last flagged pair in *f0,
-// *f1 (*f0 > *f1 when none is flagged).
-template <int M>
-__device__ __forceinline__ void q_sort_regs(const WarpLists& L, int s, int len, const QLane& q, float win, int* f0,
-                                            int* f1)
+// warp_sort_regs for a group of G lanes (sl: the lane in the group): P = G M
+// <= 64 packed keys, M per lane; entry i = G m + sl.  Exchanges at distances
+// of G and more are between a lane's own registers.  The sorted keys also
+// give the near-tie flags of fix_near_ties (pair (i, i+1) within the relative
+// window win): every lane of the group returns the first and last flagged
+// pair in *f0, *f1 (*f0 > *f1 when none is flagged).
+template <int G, int M>
+__device__ __forceinline__ void group_sort_regs(const WarpLists& L, int s, int len, int sl, float win, int* f0,
+                                                int* f1)
 {
+	constexpr int QG = G;
+	struct { int sl; } q{ sl };
 	constexpr int P = QG * M;
 	static_assert(P <= 64, "positions take at most 6 bits");
 	constexpr int PB = P <= 32 ? 5 : 6;
@@ -2067,7 +2144,7 @@ __device__ int q_gather(const DevState& S, const GridParams& G, int cb, int worl
 			const float win = lmax <= 64 ? 0x1p-16f : 1e-6f;
 			int f0, f1;
 			if (lmax <= 64) {
-				q_sort_regs<8>(L, gs, len, q, win, &f0, &f1);
+				group_sort_regs<QG, 8>(L, gs, len, q.sl, win, &f0, &f1);
 			} else {
 				q_sort_smem(S, L, gs, len, lmax, q);
 				q_near_ties(L, gs, K, q, win, &f0, &f1);
@@ -2164,7 +2241,7 @@ __device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists&
 constexpr int QPAD = 8;
 __host__ __device__ constexpr size_t q_words(int maxnb) { return 2 * (size_t)maxnb + QPAD; }
 
-template <bool TAPE>
+template <bool TAPE, bool SAMP = false>
 __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 {
 	extern __shared__ unsigned char smem[];
@@ -2234,19 +2311,19 @@ __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 		nb += __popc(__ballot_sync(0xffffffffu, valid && q.sl == 0));
 		if (nb > 32 - QN) {
 			__syncwarp();
-			finish_forces<TAPE>(S, stash, nb, lane);
+			finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 			__syncwarp();
 			nb = 0;
 		}
 	}
 	if (nb > 0) {
 		__syncwarp();
-		finish_forces<TAPE>(S, stash, nb, lane);
+		finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 	}
 	if (__any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 }
 
-template <int MODE, bool TAPE = false, bool OBST = true>
+template <int MODE, bool TAPE = false, bool OBST = true, bool SAMP = false>
 __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
 {
 	extern __shared__ unsigned char smem[];
@@ -2260,7 +2337,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	bool overflow = false;
 	if constexpr (MODE == 1) {
 		float* stash = reinterpret_cast<float*>(smem) + (size_t)(blockDim.x >> 5) * 4 * maxnb + wib * 32 * STASH_STRIDE;
-		force_agents<TAPE, OBST>(S, L, stash, lane, gw, &overflow);
+		force_agents<TAPE, OBST, SAMP>(S, L, stash, lane, gw, &overflow);
 		if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 		return;
 	}
@@ -2987,9 +3064,9 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			need_exp |= p.cost[c].kind == K_SOCIALFORCES || p.cost[c].kind == K_POWERLAW || p.cost[c].kind == K_FOE ||
 			            p.cost[c].kind >= K_PLUGIN0;   // a plugin may call ref_expf
 	if (need_exp && !exp_exceptions_for_device(&d_->expx, nullptr, err_)) return false;
-	// kernel groups: scenarios whose policies are all gradient + force-based
-	// costs (k_agent<1>), scenarios with an ORCA cost, the others
-	// (k_agent<0>); cell space orders scenarios by group
+	// kernel groups: scenarios whose policies have force-based costs only
+	// (k_force_quad or k_agent<1>, whatever the method), scenarios with an
+	// ORCA cost, the others (k_agent<0>); cell space orders scenarios by group
 	{
 		std::vector<int> cls(scen_.size(), 0);
 		for (size_t k = 0; k < scen_.size(); ++k) {
@@ -2997,7 +3074,8 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			for (size_t pi = 0; pi < pols_.size(); ++pi) {
 				if (pol_scen_[pi] != (int)k) continue;
 				const PolicyDesc& P = pols_[pi];
-				if (P.method != M_GRADIENT) force_only = false;
+				// any method: the force-only kernels pick the velocity from the
+				// cost targets (gradient step, global minimum or sample argmin)
 				for (int c = 0; c < P.ncost; ++c) {
 					const int kd = P.cost[c].kind;
 					if (!(kd == K_SOCIALFORCES || kd == K_POWERLAW || kd == K_GOALREACHING)) force_only = false;
@@ -3016,6 +3094,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 				KGroup g{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 };
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
 				g.quad = g.mode == 1 && !g.obst;
+				g.samp = false;
 				for (size_t pi = 0; pi < pols_.size(); ++pi) {
 					bool in_group = false;
 					for (int j = j0; j < g.j1; ++j) in_group |= pol_scen_[pi] == scen_order_[j];
@@ -3023,6 +3102,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 					int nbc = 0;
 					for (int c2 = 0; c2 < pols_[pi].ncost; ++c2) nbc += pols_[pi].cost[c2].kind != K_GOALREACHING;
 					if (nbc > 1) g.quad = false;
+					if (pols_[pi].method != M_GRADIENT) g.samp = true;
 				}
 				groups_.push_back(g);
 			}
@@ -3422,6 +3502,7 @@ bool Engine::configure()
 	if (smemq > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_force_quad<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 		CK(cudaFuncSetAttribute(k_force_quad<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 	}
 	if (smem0 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
@@ -3432,6 +3513,8 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_agent<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
 		CK(cudaFuncSetAttribute(k_agent<1, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
 		CK(cudaFuncSetAttribute(k_agent<1, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+		CK(cudaFuncSetAttribute(k_agent<1, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+		CK(cudaFuncSetAttribute(k_agent<1, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
 	}
 	mode_ = 1;
 	for (const auto& g : groups_) if (g.mode != 1) mode_ = 0;
@@ -3495,8 +3578,13 @@ void Engine::enqueue_step()
 		A.scratch = S.scratch + g.scratch_off;
 		A.obs_list = S.obs_list + g.obs_off;
 		if (g.quad) {
+			// taped runs are gradient-only (diff_begin checks)
 			if (S.tape_list) k_force_quad<true><<<blocks, wpb * 32, smemq, st>>>(A);
+			else if (g.samp) k_force_quad<false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			else k_force_quad<false><<<blocks, wpb * 32, smemq, st>>>(A);
+		} else if (g.mode == 1 && g.samp && !S.tape_list) {
+			if (g.obst) k_agent<1, false, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
+			else k_agent<1, false, false, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
 		} else if (S.tape_list) {
 			if (g.mode == 1 && g.obst) k_agent<1, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
 			else if (g.mode == 1) k_agent<1, true, false><<<blocks, wpb * 32, smem1, st>>>(A, 0);

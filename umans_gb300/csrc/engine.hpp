@@ -210,6 +210,7 @@ private:
 		size_t scratch_off, obs_off;
 		bool obst = false;   // a scenario of the group has obstacle edges
 		bool quad = false;   // k_force_quad: force-only, no obstacle edges, at most one neighbour cost per policy
+		bool samp = false;   // a force-only group with a policy of the sampling or global method
 	};
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
