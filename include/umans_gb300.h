@@ -109,11 +109,18 @@ int umans_batch_create(const char* const* config_files, int n, umans_sim** out);
 /* offsets[0..nscenarios] (cap >= nscenarios + 1), either pointer may be null */
 int umans_batch_offsets(umans_sim* sim, int* offsets, int cap, int* nscenarios);
 /* Times the step's launch-shape candidates (cell size per interaction range,
- * warps per block, occupancy, agent-to-warp schedule) for trial_steps each
- * from the current state, which is restored, and keeps the fastest; reports
- * the choice (any pointer may be null). */
+ * warps per block, occupancy, agent-to-warp schedule, and lanes per agent,
+ * 8 or 32, for force-only scenarios without obstacle edges) for trial_steps
+ * each from the current state, which is restored, and keeps the fastest;
+ * reports the choice (any pointer may be null). */
 int umans_autotune(umans_sim* sim, int trial_steps, float* cells_per_range, int* warps_per_block,
-                   float* occupancy, int* schedule);
+                   float* occupancy, int* schedule, int* agent_lanes);
+/* Applies a launch shape, such as one umans_autotune chose: cells per
+ * interaction range (> 0), warps per block (1..8), occupancy (0, 1],
+ * schedule (0 interleaved, 1 contiguous, 2 work list), lanes per agent (8 or
+ * 32).  Results do not depend on it.  UMANS_ERR_ARGUMENT when out of range. */
+int umans_set_launch(umans_sim* sim, float cells_per_range, int warps_per_block, float occupancy, int schedule,
+                     int agent_lanes);
 /* CrowdSimulator::RunSimulationSteps (crowdSimulator.cpp:77-95): n steps,
  * waits for them, reports device-side errors */
 int umans_step(umans_sim* sim, int nsteps);

@@ -62,8 +62,25 @@ def test_autotune_keeps_results(tmp_path):
     b.step(3)
     choice = b.autotune(trial_steps=2)
     assert choice["cells_per_range"] > 0 and choice["warps_per_block"] in (2, 4)
+    assert choice["agent_lanes"] in (8, 32)
     a.step(10)
     b.step(10)
+    assert np.array_equal(a.positions(), b.positions())
+
+
+def test_work_list_schedule_keeps_results(tmp_path):
+    """The work-list schedule (warps taking agent tiles from a counter) and
+    32 lanes per agent give the batch the same trajectories."""
+    paths = _mixed(tmp_path, count=12)
+    a, b = Batch(paths), Batch(paths)
+    b.set_launch(schedule=2, agent_lanes=32)
+    for _ in range(3):
+        a.step(4)
+        b.step(4)
+        assert np.array_equal(a.positions(), b.positions())
+    b.set_launch(schedule=2, agent_lanes=8)
+    a.step(4)
+    b.step(4)
     assert np.array_equal(a.positions(), b.positions())
 
 

@@ -105,3 +105,30 @@ def test_batch_powerlaw_sampling_members_match_oracle(tmp_path):
         n = min(n, 400)
         path = S.batch_member(k, n).write(str(tmp_path / f"b{k}.xml"))
         _same_as_oracle(path, steps=30)
+
+
+@pytest.mark.parametrize("lanes,schedule", [(8, 0), (8, 1), (8, 2), (32, 0), (32, 2)])
+def test_launch_shapes_match_oracle(lanes, schedule, tmp_path):
+    """Lanes per agent and the agent-to-warp schedule (interleaved,
+    contiguous, work list) change no result."""
+    n = 48
+    pid = np.arange(n) % 2
+    path = _crossing([S.SF_POLICY, PL_SAMPLING], n=n, seed=23, pid=pid).write(str(tmp_path / "shape.xml"))
+    sim = Simulation(path)
+    sim.set_launch(cells_per_range=2.0, warps_per_block=4, occupancy=1.0, schedule=schedule, agent_lanes=lanes)
+    port = PortSim(path, threads=THREADS)
+    for _ in range(6):
+        sim.step(5)
+        port.step(5)
+        assert np.array_equal(sim.positions(), port.state()["pos"])
+    sim.close()
+
+
+def test_launch_shape_rejects_out_of_range(tmp_path):
+    path = _crossing([S.SF_POLICY]).write(str(tmp_path / "bad.xml"))
+    sim = Simulation(path)
+    for kw in (dict(agent_lanes=16), dict(schedule=3), dict(occupancy=0.0), dict(warps_per_block=0)):
+        with pytest.raises(Exception):
+            sim.set_launch(**kw)
+    sim.step(2)   # still usable
+    sim.close()

@@ -111,10 +111,17 @@ class Simulation:
 
     def autotune(self, trial_steps: int = 3) -> dict:
         cpr, occ = C.c_float(), C.c_float()
-        wpb, sched = C.c_int(), C.c_int()
+        wpb, sched, lanes = C.c_int(), C.c_int(), C.c_int()
         self._check(self._lib.umans_autotune(self._h, int(trial_steps), C.byref(cpr), C.byref(wpb), C.byref(occ),
-                                             C.byref(sched)))
-        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value)
+                                             C.byref(sched), C.byref(lanes)))
+        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value,
+                    agent_lanes=lanes.value)
+
+    def set_launch(self, cells_per_range: float = 2.0, warps_per_block: int = 4, occupancy: float = 1.0,
+                   schedule: int = 0, agent_lanes: int = 8):
+        """Applies a launch shape (as autotune reports one); results do not depend on it."""
+        self._check(self._lib.umans_set_launch(self._h, float(cells_per_range), int(warps_per_block),
+                                               float(occupancy), int(schedule), int(agent_lanes)))
 
     def profile(self, enable: bool = True):
         self._check(self._lib.umans_profile(self._h, int(bool(enable))))
@@ -344,10 +351,17 @@ class Batch(Simulation):
 
     def autotune(self, trial_steps: int = 3) -> dict:
         cpr, occ = C.c_float(), C.c_float()
-        wpb, sched = C.c_int(), C.c_int()
+        wpb, sched, lanes = C.c_int(), C.c_int(), C.c_int()
         self._check(self._lib.umans_autotune(self._h, int(trial_steps), C.byref(cpr), C.byref(wpb), C.byref(occ),
-                                             C.byref(sched)))
-        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value)
+                                             C.byref(sched), C.byref(lanes)))
+        return dict(cells_per_range=cpr.value, warps_per_block=wpb.value, occupancy=occ.value, schedule=sched.value,
+                    agent_lanes=lanes.value)
+
+    def set_launch(self, cells_per_range: float = 2.0, warps_per_block: int = 4, occupancy: float = 1.0,
+                   schedule: int = 0, agent_lanes: int = 8):
+        """Applies a launch shape (as autotune reports one); results do not depend on it."""
+        self._check(self._lib.umans_set_launch(self._h, float(cells_per_range), int(warps_per_block),
+                                               float(occupancy), int(schedule), int(agent_lanes)))
 
 
 class UMANS:

@@ -124,8 +124,22 @@ int umans_batch_offsets(umans_sim* s, int* offsets, int cap, int* nscenarios)
 	return UMANS_OK;
 }
 
+int umans_set_launch(umans_sim* s, float cells_per_range, int warps_per_block, float occupancy, int schedule,
+                     int agent_lanes)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	umans::EngineOptions o;
+	o.cells_per_range = cells_per_range;
+	o.warps_per_block = warps_per_block;
+	o.occupancy = occupancy;
+	o.schedule = schedule;
+	o.agent_lanes = agent_lanes;
+	if (!s->eng->set_launch(o)) return fail(s, UMANS_ERR_ARGUMENT, s->eng->error());
+	return UMANS_OK;
+}
+
 int umans_autotune(umans_sim* s, int trial_steps, float* cells_per_range, int* warps_per_block, float* occupancy,
-                   int* schedule)
+                   int* schedule, int* agent_lanes)
 {
 	if (!s) return UMANS_ERR_ARGUMENT;
 	umans::EngineOptions o;
@@ -134,6 +148,7 @@ int umans_autotune(umans_sim* s, int trial_steps, float* cells_per_range, int* w
 	if (warps_per_block) *warps_per_block = o.warps_per_block;
 	if (occupancy) *occupancy = o.occupancy;
 	if (schedule) *schedule = o.schedule;
+	if (agent_lanes) *agent_lanes = o.agent_lanes;
 	return UMANS_OK;
 }
 

@@ -74,7 +74,8 @@ struct DevState {
 	uint32_t* obs_list;   // per warp: max_obs entries of the agent's obstacle list
 	int max_obs;
 	const int* scen_order;   // [nscen]: scenarios in cell-space order (grouped by kernel)
-	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks
+	int sched;            // agent-to-warp schedule: 0 interleaved, 1 contiguous blocks, 2 work list
+	unsigned* work;       // schedule 2: this launch's tile counter and finished-warp count (zero between launches)
 	float cells_per_range;
 	ExpExceptions expx;   // host-expf exception table
 	// differentiable form: neighbour lists recorded during a forward step
@@ -1585,6 +1586,63 @@ __device__ __forceinline__ void update_agent(const DevState& S, const ScenDesc& 
 }
 
 // ------------------------------------------------------------------------
+// agents to warps
+// ------------------------------------------------------------------------
+// Items [0, n) (agents, or groups of four agents) handed to the warps of a
+// launch.  Schedule 0: warp w takes w, w + W, w + 2W, ... (W warps).
+// Schedule 1: warp w a contiguous range.  Schedule 2, a work list: tiles of
+// TILE items, each warp taking the next tile from the launch's counter
+// when it has finished one; work_end then counts the warp out, and the last
+// warp to finish resets the counter for the next launch (no warp waits).
+struct WorkIter {
+	int end, step;
+};
+// (WL false: the launch never uses the work list; its code is left out)
+template <int TILE, bool WL>
+__device__ __forceinline__ int work_take(const DevState& S, WorkIter& w, int lane, int n)
+{
+	unsigned k = 0;
+	if (lane == 0) k = atomicAdd(S.work, 1u);
+	k = __shfl_sync(0xffffffffu, k, 0);
+	const long long b = (long long)k * TILE;
+	if (b >= n) return -1;
+	w.end = (int)min((long long)n, b + TILE);
+	w.step = 1;
+	return (int)b;
+}
+// the first item of the warp, the same on every lane; -1 when none
+template <int TILE, bool WL = true>
+__device__ __forceinline__ int work_first(const DevState& S, WorkIter& w, int n, int gw, int lane)
+{
+	if (WL && S.sched == 2) return work_take<TILE, WL>(S, w, lane, n);
+	int i;
+	if (S.sched == 1) {
+		const int per = (n + S.total_warps - 1) / S.total_warps;
+		i = gw * per; w.end = min(n, i + per); w.step = 1;
+	} else { i = gw; w.end = n; w.step = S.total_warps; }
+	return i < w.end ? i : -1;
+}
+// the item after i; -1 when none is left
+template <int TILE, bool WL = true>
+__device__ __forceinline__ int work_after(const DevState& S, WorkIter& w, int i, int lane, int n)
+{
+	i += w.step;
+	if (i < w.end) return i;
+	if (!WL || S.sched != 2) return -1;
+	return work_take<TILE, WL>(S, w, lane, n);
+}
+template <bool WL = true>
+__device__ __forceinline__ void work_end(const DevState& S, int lane)
+{
+	if (!WL || S.sched != 2 || lane != 0) return;
+	const unsigned d = atomicAdd(S.work + 1, 1u);
+	if (d == (unsigned)S.total_warps - 1u) {   // every warp has taken its last ticket
+		S.work[0] = 0u;
+		S.work[1] = 0u;
+	}
+}
+
+// ------------------------------------------------------------------------
 // force-only policies
 // ------------------------------------------------------------------------
 // Policies whose costs are all force-based (SocialForces, PowerLaw,
@@ -1755,12 +1813,11 @@ __device__ void force_agents(const DevState& S, const WarpLists& L, float* stash
 {
 	float* fx = reinterpret_cast<float*>(L.nid);
 	float* fy = L.aux;
-	const int span = S.t_end - S.t_begin;
-	const int per = (span + S.total_warps - 1) / S.total_warps;
-	const int t0 = S.t_begin + (S.sched ? gw * per : gw), stride = S.sched ? 1 : S.total_warps;
-	const int tend = S.sched ? min(S.t_end, t0 + per) : S.t_end;
+	WorkIter w;
+	const int n_items = S.t_end - S.t_begin;
 	int nb = 0;
-	for (int t = t0; t < tend; t += stride) {
+	for (int it = work_first<32>(S, w, n_items, gw, lane); it >= 0; it = work_after<32>(S, w, it, lane, n_items)) {
+		const int t = S.t_begin + it;
 		const int slot = S.sSlot[t];
 		const float4 sb = S.sB[t];
 		const float4 prm = S.prm[slot];
@@ -1853,6 +1910,7 @@ __device__ void force_agents(const DevState& S, const WarpLists& L, float* stash
 		__syncwarp();
 		finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 	}
+	work_end(S, lane);
 }
 
 // ------------------------------------------------------------------------
@@ -2241,7 +2299,68 @@ __device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists&
 constexpr int QPAD = 8;
 __host__ __device__ constexpr size_t q_words(int maxnb) { return 2 * (size_t)maxnb + QPAD; }
 
-template <bool TAPE, bool SAMP = false>
+// One group of four agents (qi: its index in the launch's range) of
+// k_force_quad: the gather, the force pass, the agents' records; every 32
+// records, the per-agent remainder.
+template <bool TAPE, bool SAMP>
+__device__ __forceinline__ void quad_step(const DevState& S, const QLane& q, const WarpLists& L, float* stash,
+                                          int lane, int qi, int& nb, bool& overflow)
+{
+	const int maxnb = S.maxnb;
+	const int t = S.t_begin + qi * QN + q.sg;
+	const bool valid = t < S.t_end;
+	const int tc = valid ? t : S.t_end - 1;   // in-range loads for a missing fourth agent
+	const int slot = S.sSlot[tc];
+	const float4 sb = S.sB[tc];
+	const float4 prm = S.prm[slot];
+	const PolicyDesc& pol = S.pols[S.pol[slot]];
+	AgentCtx A;
+	A.pos = S.sP[tc]; A.vel = S.sV[tc]; A.pref = V(sb.x, sb.y); A.goal = V(0, 0);
+	A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
+	const int sc = S.agent_scen[slot];
+	const ScenDesc& sd = S.scen[sc];
+	const GridParams G = S.grid[sc];
+	A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
+	const float W = sd.width, H = sd.height;
+
+	const int K = q_gather(S, G, S.cell_base[sc], sd.world, W, H, L, t, A.pos, pol.range, valid, q, &overflow);
+	if (TAPE) {
+		const int kmax = q_max(K);
+		for (int b = 0; b < kmax; b += QG) {
+			const int k = b + q.sl;
+			if (k < K) {
+				const uint32_t rr = L.ref[k];
+				S.tape_list[(size_t)slot * maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
+			}
+		}
+		if (valid && q.sl == 0) S.tape_cnt[slot] = K;
+		__syncwarp();
+	}
+	int ci = -1;
+	for (int k = 0; k < pol.ncost; ++k)
+		if (pol.cost[k].kind != K_GOALREACHING) ci = k;
+	const CostDesc* cd = (valid && ci >= 0 && !viszero(A.pref)) ? &pol.cost[ci] : nullptr;
+	float2 contact;
+	const float2 f = q_force(S, A, L, K, cd, valid ? pol.contact_scale : 0.0f, W, H, q, &contact);
+	if (valid && q.sl == 0) {
+		float* rec = stash + (nb + q.sg) * STASH_STRIDE;
+		rec[0] = __int_as_float(t);
+		if (ci >= 0) { rec[1 + 2 * ci] = f.x; rec[2 + 2 * ci] = f.y; }
+		rec[2 * MAX_COSTS + 1] = contact.x;
+		rec[2 * MAX_COSTS + 2] = contact.y;
+	}
+	nb += __popc(__ballot_sync(0xffffffffu, valid && q.sl == 0));
+	if (nb > 32 - QN) {
+		__syncwarp();
+		finish_forces<TAPE, SAMP>(S, stash, nb, lane);
+		__syncwarp();
+		nb = 0;
+	}
+}
+
+// WL: compiled for the work-list schedule (schedule 2), which it then
+// requires; the other schedules use the variant without it.
+template <bool TAPE, bool SAMP = false, bool WL = false>
 __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 {
 	extern __shared__ unsigned char smem[];
@@ -2258,68 +2377,23 @@ __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 	const WarpLists L{ lists, reinterpret_cast<float*>(lists + maxnb + QPAD / 2), nullptr, nullptr };
 	float* stash = reinterpret_cast<float*>(smem) + (size_t)(blockDim.x >> 5) * QN * q_words(maxnb) + wib * 32 * STASH_STRIDE;
 	bool overflow = false;
-
-	const int span = S.t_end - S.t_begin;
-	const int nq = (span + QN - 1) / QN;
-	const int per = (nq + S.total_warps - 1) / S.total_warps;
-	const int q0 = S.sched ? gw * per : gw, qstride = S.sched ? 1 : S.total_warps;
-	const int qend = S.sched ? min(nq, q0 + per) : nq;
+	const int nq = (S.t_end - S.t_begin + QN - 1) / QN;
 	int nb = 0;
-	for (int qi = q0; qi < qend; qi += qstride) {
-		const int t = S.t_begin + qi * QN + q.sg;
-		const bool valid = t < S.t_end;
-		const int tc = valid ? t : S.t_end - 1;   // in-range loads for a missing fourth agent
-		const int slot = S.sSlot[tc];
-		const float4 sb = S.sB[tc];
-		const float4 prm = S.prm[slot];
-		const PolicyDesc& pol = S.pols[S.pol[slot]];
-		AgentCtx A;
-		A.pos = S.sP[tc]; A.vel = S.sV[tc]; A.pref = V(sb.x, sb.y); A.goal = V(0, 0);
-		A.radius = prm.x; A.prefspeed = prm.y; A.maxspeed = prm.z; A.maxacc = prm.w;
-		const int sc = S.agent_scen[slot];
-		const ScenDesc& sd = S.scen[sc];
-		const GridParams G = S.grid[sc];
-		A.dt = sd.dt; A.relax = pol.relax_time; A.ex = S.expx;
-		const float W = sd.width, H = sd.height;
-
-		const int K = q_gather(S, G, S.cell_base[sc], sd.world, W, H, L, t, A.pos, pol.range, valid, q, &overflow);
-		if (TAPE) {
-			const int kmax = q_max(K);
-			for (int b = 0; b < kmax; b += QG) {
-				const int k = b + q.sl;
-				if (k < K) {
-					const uint32_t rr = L.ref[k];
-					S.tape_list[(size_t)slot * maxnb + k] = (rr & 0xF0000000u) | (uint32_t)S.sSlot[rr & 0x0FFFFFFFu];
-				}
-			}
-			if (valid && q.sl == 0) S.tape_cnt[slot] = K;
-			__syncwarp();
-		}
-		int ci = -1;
-		for (int k = 0; k < pol.ncost; ++k)
-			if (pol.cost[k].kind != K_GOALREACHING) ci = k;
-		const CostDesc* cd = (valid && ci >= 0 && !viszero(A.pref)) ? &pol.cost[ci] : nullptr;
-		float2 contact;
-		const float2 f = q_force(S, A, L, K, cd, valid ? pol.contact_scale : 0.0f, W, H, q, &contact);
-		if (valid && q.sl == 0) {
-			float* rec = stash + (nb + q.sg) * STASH_STRIDE;
-			rec[0] = __int_as_float(t);
-			if (ci >= 0) { rec[1 + 2 * ci] = f.x; rec[2 + 2 * ci] = f.y; }
-			rec[2 * MAX_COSTS + 1] = contact.x;
-			rec[2 * MAX_COSTS + 2] = contact.y;
-		}
-		nb += __popc(__ballot_sync(0xffffffffu, valid && q.sl == 0));
-		if (nb > 32 - QN) {
-			__syncwarp();
-			finish_forces<TAPE, SAMP>(S, stash, nb, lane);
-			__syncwarp();
-			nb = 0;
-		}
+	if constexpr (WL) {
+		WorkIter w;
+		for (int qi = work_first<32 / QN>(S, w, nq, gw, lane); qi >= 0; qi = work_after<32 / QN>(S, w, qi, lane, nq))
+			quad_step<TAPE, SAMP>(S, q, L, stash, lane, qi, nb, overflow);
+	} else {
+		const int per = (nq + S.total_warps - 1) / S.total_warps;
+		const int q0 = S.sched ? gw * per : gw, qstride = S.sched ? 1 : S.total_warps;
+		const int qend = S.sched ? min(nq, q0 + per) : nq;
+		for (int qi = q0; qi < qend; qi += qstride) quad_step<TAPE, SAMP>(S, q, L, stash, lane, qi, nb, overflow);
 	}
 	if (nb > 0) {
 		__syncwarp();
 		finish_forces<TAPE, SAMP>(S, stash, nb, lane);
 	}
+	work_end<WL>(S, lane);
 	if (__any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 }
 
@@ -2346,11 +2420,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
 	float4* proj = lines + maxnb;
 
-	const int span = S.t_end - S.t_begin;
-	const int per = (span + S.total_warps - 1) / S.total_warps;
-	const int t0 = S.t_begin + (S.sched ? gw * per : gw), stride = S.sched ? 1 : S.total_warps;
-	const int tend = S.sched ? min(S.t_end, t0 + per) : S.t_end;
-	for (int t = t0; t < tend; t += stride) {
+	WorkIter w;
+	const int n_items = S.t_end - S.t_begin;
+	for (int it = work_first<8>(S, w, n_items, gw, lane); it >= 0; it = work_after<8>(S, w, it, lane, n_items)) {
+		const int t = S.t_begin + it;
 		const int slot = S.sSlot[t];
 		const float4 sb = S.sB[t];
 		const float4 prm = S.prm[slot];
@@ -2546,6 +2619,7 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		}
 		__syncwarp();
 	}
+	work_end(S, lane);
 	if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 }
 
@@ -3093,7 +3167,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			if ((int)scen_order_.size() > j0) {
 				KGroup g{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 };
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
-				g.quad = g.mode == 1 && !g.obst;
+				g.quad_ok = g.mode == 1 && !g.obst;
 				g.samp = false;
 				for (size_t pi = 0; pi < pols_.size(); ++pi) {
 					bool in_group = false;
@@ -3101,7 +3175,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 					if (!in_group) continue;
 					int nbc = 0;
 					for (int c2 = 0; c2 < pols_[pi].ncost; ++c2) nbc += pols_[pi].cost[c2].kind != K_GOALREACHING;
-					if (nbc > 1) g.quad = false;
+					if (nbc > 1) g.quad_ok = false;
 					if (pols_[pi].method != M_GRADIENT) g.samp = true;
 				}
 				groups_.push_back(g);
@@ -3503,6 +3577,9 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_force_quad<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 		CK(cudaFuncSetAttribute(k_force_quad<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 		CK(cudaFuncSetAttribute(k_force_quad<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 	}
 	if (smem0 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
@@ -3524,6 +3601,7 @@ bool Engine::configure()
 	for (const auto& D : scen_) maxe = std::max(maxe, D.nedges);
 	S.max_obs = 5 * maxe;   // every edge, once per displacement group
 	for (auto& g : groups_) {
+		g.quad = g.quad_ok && opt_.agent_lanes == 8;
 		g.blocks = g.quad ? quad_blocks_for(num_sms_, wpb, smemq)
 		                  : agent_blocks_for(num_sms_, wpb, g.mode == 1 ? smem1 : smem0, g.mode, g.obst);
 		if (opt_.occupancy < 1.0f) g.blocks = std::max(num_sms_, (int)(g.blocks * opt_.occupancy));
@@ -3539,6 +3617,9 @@ bool Engine::configure()
 	S.cells_per_range = opt_.cells_per_range;
 	static_grid_ready_ = false;   // the cell size may have changed
 	if (!dalloc(S.scratch, std::max<size_t>(scr, 1), err_)) return false;
+	// work-list counters: a pair per kernel group, and one for the list dump
+	if (!dalloc(S.work, 2 * (groups_.size() + 1), err_)) return false;
+	CK(cudaMemset(S.work, 0, sizeof(unsigned) * 2 * (groups_.size() + 1)));
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
 	return true;
@@ -3575,12 +3656,19 @@ void Engine::enqueue_step()
 		const int per_block = g.quad ? wpb * QN : wpb;
 		const int blocks = std::min(g.blocks, std::max(1, (te[k] - tb[k] + per_block - 1) / per_block));
 		A.total_warps = blocks * wpb;
+		A.work = S.work + 2 * k;
 		A.scratch = S.scratch + g.scratch_off;
 		A.obs_list = S.obs_list + g.obs_off;
 		if (g.quad) {
 			// taped runs are gradient-only (diff_begin checks)
-			if (S.tape_list) k_force_quad<true><<<blocks, wpb * 32, smemq, st>>>(A);
-			else if (g.samp) k_force_quad<false, true><<<blocks, wpb * 32, smemq, st>>>(A);
+			const bool wl = S.sched == 2;
+			if (S.tape_list) {
+				if (wl) k_force_quad<true, false, true><<<blocks, wpb * 32, smemq, st>>>(A);
+				else k_force_quad<true><<<blocks, wpb * 32, smemq, st>>>(A);
+			} else if (g.samp) {
+				if (wl) k_force_quad<false, true, true><<<blocks, wpb * 32, smemq, st>>>(A);
+				else k_force_quad<false, true><<<blocks, wpb * 32, smemq, st>>>(A);
+			} else if (wl) k_force_quad<false, false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			else k_force_quad<false><<<blocks, wpb * 32, smemq, st>>>(A);
 		} else if (g.mode == 1 && g.samp && !S.tape_list) {
 			if (g.obst) k_agent<1, false, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
@@ -4175,6 +4263,7 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 	if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	const int blocks = agent_blocks_for(num_sms_, wpb, smem);
 	T.total_warps = blocks * wpb;
+	T.work = S.work + 2 * groups_.size();
 	float4* scr = nullptr;
 	if (!dalloc(scr, (size_t)T.total_warps * 2 * dump_nb, err_)) return false;
 	T.scratch = scr;
@@ -4201,6 +4290,22 @@ bool Engine::neighbours(int cap, int* ids, float* d2, int* counts)
 // candidate from the current state, which is restored afterwards.  Every
 // candidate computes bit-identical results: the cell size changes which
 // cells are scanned, not which neighbours are found or their order.
+bool Engine::set_launch(const EngineOptions& o)
+{
+	if (!(o.cells_per_range > 0) || o.warps_per_block < 1 || o.warps_per_block > 8 || !(o.occupancy > 0) ||
+	    o.occupancy > 1 || o.schedule < 0 || o.schedule > 2 || (o.agent_lanes != 8 && o.agent_lanes != 32)) {
+		err_ = "launch shape out of range";
+		return false;
+	}
+	if (!sync()) return false;
+	opt_.cells_per_range = o.cells_per_range;
+	opt_.warps_per_block = o.warps_per_block;
+	opt_.occupancy = o.occupancy;
+	opt_.schedule = o.schedule;
+	opt_.agent_lanes = o.agent_lanes;
+	return configure();
+}
+
 bool Engine::autotune(int trial_steps, EngineOptions* chosen)
 {
 	if (!sync()) return false;
@@ -4211,12 +4316,17 @@ bool Engine::autotune(int trial_steps, EngineOptions* chosen)
 	const bool prof = profile_;
 	profile_ = false;
 	if (!take_snapshot()) return false;
+	bool any_quad = false;
+	for (const auto& g : groups_) any_quad |= g.quad_ok;
+	const std::vector<int> lanes = any_quad ? std::vector<int>{ 8, 32 } : std::vector<int>{ base.agent_lanes };
+	for (int ln : lanes)
 	for (float cpr : { 1.0f, 2.0f, 3.0f })
 		for (int wpb : { 2, 4 })
 			for (float occ : { 1.0f, 0.5f })
-				for (int sched : { 0, 1 }) {
+				for (int sched : { 0, 1, 2 }) {
 					opt_ = base;
 					opt_.cells_per_range = cpr; opt_.warps_per_block = wpb; opt_.occupancy = occ; opt_.schedule = sched;
+					opt_.agent_lanes = ln;
 					if (!configure()) return false;
 					if (!restore_snapshot()) return false;
 					if (!run_steps(1)) return false;   // graph capture, warm-up
@@ -4552,7 +4662,7 @@ Engine::~Engine()
 		void* ptrs[] = { S.pos, S.vel, S.goal, S.view, S.vwf, S.pref, S.prm, S.pol, S.id, S.rng, S.sP, S.sV, S.sB, S.sE,
 		                 S.sSlot, S.sId, S.cell, S.cnt, S.start, S.blocksum, S.grid, S.bbox, S.status,
 		                 (void*)S.pols, (void*)S.table, (void*)S.lcgpow, S.scratch, S.dump_ids, S.dump_cnt, S.dump_d2, S.slot_of_id, S.io,
-		                 S.agent_scen, S.cell_base, scen_dev_, S.obs_list,
+		                 S.agent_scen, S.cell_base, scen_dev_, S.obs_list, S.work,
 		                 snap_pos_, snap_vel_, snap_view_, snap_vwf_, snap_rng_ };
 		for (void* p : ptrs)
 			if (p) cudaFree(p);

@@ -33,7 +33,8 @@ struct EngineOptions {
 	float cells_per_range = 2.0f;  // grid cell size = range / cells_per_range
 	int warps_per_block = 4;
 	float occupancy = 1.0f;   // fraction of the resident blocks per SM that the agent kernel launches
-	int schedule = 0;         // agents to warps: 0 interleaved, 1 contiguous blocks
+	int schedule = 0;         // agents to warps: 0 interleaved, 1 contiguous blocks, 2 work list of agent tiles
+	int agent_lanes = 8;      // lanes per agent in the force-only groups that allow 8 (else 32)
 	bool use_graph = true;
 };
 
@@ -80,6 +81,8 @@ public:
 	// times the launch-shape candidates from the current state (restored
 	// afterwards) and keeps the fastest
 	bool autotune(int trial_steps, EngineOptions* chosen);
+	// applies a launch shape (the fields autotune chooses); results do not depend on it
+	bool set_launch(const EngineOptions& o);
 	const EngineOptions& options() const { return opt_; }
 
 	// device pointers of the raw state for callers that keep data on the GPU
@@ -209,7 +212,8 @@ private:
 		int blocks;
 		size_t scratch_off, obs_off;
 		bool obst = false;   // a scenario of the group has obstacle edges
-		bool quad = false;   // k_force_quad: force-only, no obstacle edges, at most one neighbour cost per policy
+		bool quad_ok = false;   // k_force_quad allowed: force-only, no obstacle edges, <= 1 neighbour cost per policy
+		bool quad = false;      // k_force_quad chosen (quad_ok and EngineOptions::agent_lanes == 8)
 		bool samp = false;   // a force-only group with a policy of the sampling or global method
 	};
 	std::vector<KGroup> groups_;
