@@ -104,7 +104,9 @@ int umans_destroy(umans_sim* sim);
  * process): n independent scenarios stepped together, their agents
  * concatenated in list order, scenario k at slots [offsets[k], offsets[k+1]).
  * Each scenario is simulated exactly as by umans_create on its own file.
- * Timed insertion and removal at the goal are not supported in a batch. */
+ * Agents with a start time join the end of their scenario's agents when its
+ * clock reaches it, and agents removed at their goal leave their scenario
+ * (each scenario as its own simulation would), so the offsets move. */
 int umans_batch_create(const char* const* config_files, int n, umans_sim** out);
 /* offsets[0..nscenarios] (cap >= nscenarios + 1), either pointer may be null */
 int umans_batch_offsets(umans_sim* sim, int* offsets, int cap, int* nscenarios);

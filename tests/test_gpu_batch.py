@@ -4,7 +4,7 @@ golden fixtures, the reference's)."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden
+from conftest import assert_same_population, dynamic_golden_names, dynamic_snapshots, golden_names, load_golden
 from umans_gb300 import Batch, Simulation, scenarios as S
 
 pytestmark = pytest.mark.gpu
@@ -66,6 +66,48 @@ def test_autotune_keeps_results(tmp_path):
     a.step(10)
     b.step(10)
     assert np.array_equal(a.positions(), b.positions())
+
+
+def test_batch_with_dynamic_population_matches_reference(tmp_path):
+    """Timed insertion and removal at the goal (worldBase.cpp:82-86, 122-127)
+    in a batch.  The eleven arrivals fixtures are interleaved with static
+    members.  At every snapshot each member holds the fixture's agents at
+    bit-identical positions, and the static members equal their own
+    simulations."""
+    names = dynamic_golden_names()
+    fixtures = [load_golden(n) for n in names]
+    paths, members = [], []
+    for k, (name, g) in enumerate(zip(names, fixtures)):
+        p = tmp_path / (name + ".xml")
+        p.write_bytes(g["xml"].tobytes())
+        paths.append(str(p))
+        members.append(("fixture", g, name))
+        if k % 3 == 0:
+            q = S.batch_member(k, 30).write(str(tmp_path / f"static{k}.xml"))
+            paths.append(q)
+            members.append(("static", Simulation(q), q))
+    b = Batch(paths)
+    snaps = [dict((s, (ids, pos)) for s, ids, pos in dynamic_snapshots(g)) if kind == "fixture" else None
+             for kind, g, _ in members]
+    steps = sorted({s for d in snaps if d for s in d})
+    done = 0
+    for s in steps:
+        b.step(s - done)
+        for kind, obj, _ in members:
+            if kind == "static":
+                obj.step(s - done)
+        done = s
+        off = b.offsets
+        st = b.state()
+        for m, (kind, obj, what) in enumerate(members):
+            ids, pos = st["ids"][off[m]:off[m + 1]], st["pos"][off[m]:off[m + 1]]
+            if kind == "fixture":
+                if s in snaps[m]:
+                    want_ids, want_pos = snaps[m][s]
+                    assert_same_population(ids, pos, want_ids, want_pos, f"{what} step {s}")
+            else:
+                ref = obj.state()
+                assert np.array_equal(ids, ref["ids"]) and np.array_equal(pos, ref["pos"]), f"{what} step {s}"
 
 
 def test_work_list_schedule_keeps_results(tmp_path):

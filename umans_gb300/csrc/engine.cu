@@ -3066,13 +3066,6 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 			for (int c = 0; c < p.ncost; ++c) norca += p.cost[c].kind == K_ORCA;
 			if (norca > 1) { err_ = "a policy with more than one ORCA cost function is not supported"; return false; }
 		}
-		if (xmls.size() > 1) {
-			for (const auto& a : scs_[k].agents)
-				if (a.start_time > 0 || a.remove_at_goal) {
-					err_ = xmls[k] + ": timed insertion and removal at the goal are not supported in a batch";
-					return false;
-				}
-		}
 	}
 	sc_ = scs_[0];
 	int dev = 0;
@@ -3105,7 +3098,13 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 		D.max_range = mr;
 		D.agent_off = (int)id_.size();
 		for (const auto& a : sc.agents) {
-			if (a.start_time > 0) { pending_.push_back(a); continue; }
+			if (a.start_time > 0) {
+				AgentInit p = a;
+				p.scen = (int)k;
+				p.policy += pbase;
+				pending_.push_back(p);
+				continue;
+			}
 			if (k == 0) slot_of_[a.id] = (int)id_.size();
 			id_.push_back(a.id); pol_.push_back(pbase + a.policy);
 			agent_scen_.push_back((int)k);
@@ -3789,64 +3788,149 @@ bool Engine::capture_graph()
 	return true;
 }
 
+// Host copy of the per-agent arrays in list order, rebuilt scenario by
+// scenario when agents join or leave (order within a scenario as the
+// reference's agent list).
+struct Engine::AgentLists {
+	std::vector<int> id, pol, scen;
+	std::vector<unsigned char> remove;
+	std::vector<float2> pos, vel, goal, view, vwf;
+	std::vector<float4> prm;
+	std::vector<uint32_t> rng;
+};
+
+void Engine::take_lists(AgentLists& L)
+{
+	L.id.swap(id_); L.pol.swap(pol_); L.scen.swap(agent_scen_); L.remove.swap(remove_);
+	L.pos.swap(pos_); L.vel.swap(vel_); L.goal.swap(goal_); L.view.swap(view_); L.vwf.swap(vwf_);
+	L.prm.swap(prm_); L.rng.swap(rng_);
+	for (auto* v : { &id_, &pol_, &agent_scen_ }) v->clear();
+	remove_.clear();
+	for (auto* v : { &pos_, &vel_, &goal_, &view_, &vwf_ }) v->clear();
+	prm_.clear();
+	rng_.clear();
+}
+
+void Engine::append_agent(const AgentLists& L, int i)
+{
+	id_.push_back(L.id[i]); pol_.push_back(L.pol[i]); agent_scen_.push_back(L.scen[i]); remove_.push_back(L.remove[i]);
+	pos_.push_back(L.pos[i]); vel_.push_back(L.vel[i]); goal_.push_back(L.goal[i]); view_.push_back(L.view[i]);
+	vwf_.push_back(L.vwf[i]); prm_.push_back(L.prm[i]); rng_.push_back(L.rng[i]);
+}
+
+void Engine::append_new_agent(const AgentInit& a)
+{
+	id_.push_back(a.id); pol_.push_back(a.policy);
+	agent_scen_.push_back(a.scen);
+	pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
+	goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
+	prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
+	rng_.push_back(minstd_seed((unsigned int)a.id));
+	remove_.push_back(a.remove_at_goal ? 1 : 0);
+	// Agent::setGoal: agent.cpp:108-115
+	float2 v0 = make_float2(0, 0);
+	if (a.gx != a.x || a.gy != a.y) {
+		float dx = a.gx - a.x, dy = a.gy - a.y, m = sqrtf(dx * dx + dy * dy);
+		if (m > 0) { dx = dx / m; dy = dy / m; }
+		v0 = make_float2(dx, dy);
+	}
+	view_.push_back(v0);
+}
+
+// The clock of scenario k (a single simulation's own time)
+double Engine::scen_time(int k) const { return scen_.size() == 1 ? time_ : times_[k]; }
+
+bool Engine::agents_due() const
+{
+	for (const auto& a : pending_)
+		if ((double)a.start_time <= scen_time(a.scen)) return true;
+	return false;
+}
+
+// After a change of the agent list: scenario 0's id -> slot map (the single
+// simulation's id lookups), the count, the capacity, the device copy.
+bool Engine::finish_list_change()
+{
+	n_ = (int)id_.size();
+	slot_of_.clear();
+	const int n0 = scen_.size() == 1 ? n_ : scen_[0].n;
+	for (int i = 0; i < n0; ++i) slot_of_[id_[i]] = i;
+	bool grow = n_ > cap_;
+	if (scen_.size() > 1) {
+		// a batch scenario's cell capacity follows its population
+		int64_t mc = 0;
+		for (auto& D : scen_) {
+			D.max_cells = std::max(D.max_cells, 4 * D.n + 256);
+			mc += D.max_cells;
+		}
+		grow |= mc > d_->max_cells;
+	}
+	if (grow && !alloc(n_ > cap_ ? std::max(n_, 2 * cap_) : cap_)) return false;
+	return upload_all();
+}
+
 bool Engine::apply_pending_agents()
 {
 	// WorldBase::DoStep: agents whose start time has come (worldBase.cpp:82-86)
-	if (pending_.empty() || (double)pending_.front().start_time > time_) return true;
+	// join the end of their scenario's agent list, in start order
+	if (!agents_due()) return true;
 	if (!download_mutable()) return false;
-	size_t k = 0;
-	while (k < pending_.size() && (double)pending_[k].start_time <= time_) {
-		const AgentInit& a = pending_[k];
-		slot_of_[a.id] = (int)id_.size();
-		id_.push_back(a.id); pol_.push_back(a.policy);
-		agent_scen_.push_back(0);
-		pos_.push_back(make_float2(a.x, a.y)); vel_.push_back(make_float2(0, 0));
-		goal_.push_back(make_float2(a.gx, a.gy)); vwf_.push_back(make_float2(0, 0));
-		prm_.push_back(make_float4(a.radius, a.pref_speed, a.max_speed, a.max_accel));
-		rng_.push_back(minstd_seed((unsigned int)a.id));
-		remove_.push_back(a.remove_at_goal ? 1 : 0);
-		float2 v0 = make_float2(0, 0);
-		if (a.gx != a.x || a.gy != a.y) {
-			float dx = a.gx - a.x, dy = a.gy - a.y, m = sqrtf(dx * dx + dy * dy);
-			if (m > 0) { dx = dx / m; dy = dy / m; }
-			v0 = make_float2(dx, dy);
-		}
-		view_.push_back(v0);
-		++k;
+	AgentLists L;
+	take_lists(L);
+	std::vector<AgentInit> later;
+	std::vector<std::vector<AgentInit>> due(scen_.size());
+	for (const auto& a : pending_) {
+		if ((double)a.start_time <= scen_time(a.scen)) due[a.scen].push_back(a);
+		else later.push_back(a);
 	}
-	pending_.erase(pending_.begin(), pending_.begin() + k);
-	n_ = (int)id_.size();
-	if (n_ > cap_ && !alloc(std::max(n_, 2 * cap_))) return false;
-	return upload_all();
+	for (size_t k = 0; k < scen_.size(); ++k) {
+		ScenDesc& D = scen_[k];
+		const int off = scen_.size() == 1 ? 0 : D.agent_off, n = scen_.size() == 1 ? (int)L.id.size() : D.n;
+		D.agent_off = (int)id_.size();
+		for (int i = off; i < off + n; ++i) append_agent(L, i);
+		for (const auto& a : due[k]) append_new_agent(a);
+		D.n = (int)id_.size() - D.agent_off;
+	}
+	pending_.swap(later);
+	return finish_list_change();
 }
 
 bool Engine::remove_at_goal()
 {
-	// WorldBase::DoStep tail: worldBase.cpp:122-127, removeAgentAtListIndex :207-235
+	// WorldBase::DoStep tail (worldBase.cpp:122-127): each scenario's agents
+	// from the last to the first; an agent at its goal that is removed there
+	// takes the place of its scenario's last agent (removeAgentAtListIndex
+	// :207-235)
 	if (!download_mutable()) return false;
+	std::vector<std::vector<int>> keep(scen_.size());
 	bool changed = false;
-	for (int i = n_ - 1; i >= 0; --i) {
-		if (!remove_[i]) continue;
-		const float dx = goal_[i].x - pos_[i].x, dy = goal_[i].y - pos_[i].y;
-		const float r = prm_[i].x;
-		if (dx * dx + dy * dy <= r * r) {
-			if (!changed && !rec_flush_async()) return false;   // the ring's agents are the old list
-			const int last = n_ - 1;
-			slot_of_.erase(id_[i]);
-			if (i != last) {
-				id_[i] = id_[last]; pol_[i] = pol_[last]; pos_[i] = pos_[last]; vel_[i] = vel_[last];
-				goal_[i] = goal_[last]; view_[i] = view_[last]; vwf_[i] = vwf_[last]; prm_[i] = prm_[last];
-				rng_[i] = rng_[last]; remove_[i] = remove_[last];
-				slot_of_[id_[i]] = i;
+	for (size_t k = 0; k < scen_.size(); ++k) {
+		const int off = scen_.size() == 1 ? 0 : scen_[k].agent_off, n = scen_.size() == 1 ? n_ : scen_[k].n;
+		std::vector<int>& idx = keep[k];
+		idx.resize(n);
+		for (int i = 0; i < n; ++i) idx[i] = off + i;
+		for (int i = n - 1; i >= 0; --i) {
+			const int a = idx[i];
+			if (!remove_[a]) continue;
+			const float dx = goal_[a].x - pos_[a].x, dy = goal_[a].y - pos_[a].y;
+			const float r = prm_[a].x;
+			if (dx * dx + dy * dy <= r * r) {
+				if (!changed && !rec_flush_async()) return false;   // the ring's agents are the old list
+				idx[i] = idx.back();
+				idx.pop_back();
+				changed = true;
 			}
-			id_.pop_back(); pol_.pop_back(); pos_.pop_back(); vel_.pop_back(); goal_.pop_back();
-			view_.pop_back(); vwf_.pop_back(); prm_.pop_back(); rng_.pop_back(); remove_.pop_back();
-			agent_scen_.pop_back();
-			--n_;
-			changed = true;
 		}
 	}
-	return changed ? upload_all() : true;
+	if (!changed) return true;
+	AgentLists L;
+	take_lists(L);
+	for (size_t k = 0; k < scen_.size(); ++k) {
+		scen_[k].agent_off = (int)id_.size();
+		for (int i : keep[k]) append_agent(L, i);
+		scen_[k].n = (int)id_.size() - scen_[k].agent_off;
+	}
+	return finish_list_change();
 }
 
 // Enqueues n steps (no host work in between).
@@ -4048,7 +4132,7 @@ bool Engine::restore_snapshot()
 bool Engine::step(int nsteps)
 {
 	if (nsteps <= 0) return true;
-	const bool dynamic = !pending_.empty() || any_remove_at_goal_;
+	const bool dynamic = !pending_.empty() || any_remove_at_goal_;   // agents join or leave between steps
 	if (time_kernels) CK(cudaEventRecord(ev0_, stream_));
 	if (!dynamic) {
 		// with trajectory output, batches stop where the ring is full; the
@@ -4070,7 +4154,7 @@ bool Engine::step(int nsteps)
 		// every step before the host-side changes
 		for (int s = 0; s < nsteps; ++s) {
 			if (rec_ && rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
-			if (!pending_.empty() && (double)pending_.front().start_time <= time_ && !rec_before_change()) return false;
+			if (agents_due() && !rec_before_change()) return false;
 			if (!pending_.empty() && !apply_pending_agents()) return false;
 			if (!take_snapshot()) return false;
 			if (!run_steps(1, true)) return false;

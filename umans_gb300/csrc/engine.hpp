@@ -155,6 +155,13 @@ private:
 	bool capture_graph();
 	void invalidate_graph();
 	bool apply_pending_agents();
+	struct AgentLists;
+	void take_lists(AgentLists& L);
+	void append_agent(const AgentLists& L, int i);
+	void append_new_agent(const AgentInit& a);
+	double scen_time(int k) const;
+	bool agents_due() const;
+	bool finish_list_change();
 	bool remove_at_goal();
 	bool download_mutable();
 

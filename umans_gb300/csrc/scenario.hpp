@@ -17,6 +17,7 @@ struct AgentInit {
 	int policy;          // index into Scenario::policies
 	float start_time;
 	bool remove_at_goal;
+	int scen = 0;        // the scenario of a batch it belongs to (set by the engine)
 };
 
 struct Scenario {
