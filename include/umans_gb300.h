@@ -210,7 +210,8 @@ int umans_get_force_params(umans_sim* sim, int scenario, float* params4);
  * lines appended, at full float precision (9 significant digits; the
  * reference writes 6); binary = 1: one file trajectory.bin of chunks (see
  * umans_gb300.read_trajectory).  Changes of the agent list flush the ring
- * first.  Single simulations only.  umans_record_flush writes everything
+ * first.  A batch writes scenario k into directory/scenario_k, as a
+ * simulation of that scenario alone would.  umans_record_flush writes everything
  * recorded so far and waits; umans_record_stop flushes and ends recording
  * (also done by umans_destroy). */
 int umans_record_start(umans_sim* sim, const char* directory, int ring_steps, int binary);

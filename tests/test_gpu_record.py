@@ -87,3 +87,54 @@ def test_agent_list_changes_flush_the_ring(tmp_path):
     assert len(per[1][0]) == 9
     for aid, p in final.items():
         assert np.array_equal(per[aid][1][-1], p)
+
+
+def test_batch_records_each_scenario_as_its_own_simulation(tmp_path):
+    """A batch writes scenario k into <dir>/scenario_k, the same files its own
+    simulation writes: binary chunks through ring wrap-arounds, and CSV
+    with a member whose agents arrive and leave (the list changes flush the
+    ring) and a member with another time step."""
+    from conftest import load_golden
+    from umans_gb300 import Batch
+    arr = load_golden("arrivals40_SocialForces")
+    p_arr = tmp_path / "arrivals.xml"
+    p_arr.write_bytes(arr["xml"].tobytes())
+    slow = S.model_crossing("PowerLaw", n=24)
+    slow.dt = 0.05
+    paths = [S.model_crossing("SocialForces", n=30).write(str(tmp_path / "a.xml")), str(p_arr),
+             slow.write(str(tmp_path / "c.xml"))]
+    for fmt in (True, False):
+        out = str(tmp_path / ("bbin" if fmt else "bcsv"))
+        b = Batch(paths)
+        b.record_start(out, ring_steps=7, binary=fmt)
+        b.step(9)
+        b.step(8)
+        b.record_stop()
+        b.close()
+        for k, p in enumerate(paths):
+            own = str(tmp_path / f"own{k}_{fmt}")
+            s = Simulation(p)
+            s.record_start(own, ring_steps=64, binary=fmt)
+            s.step(17)
+            s.record_stop()
+            s.close()
+            got_dir = os.path.join(out, f"scenario_{k}")
+            if fmt:
+                got = _per_agent(read_trajectory(os.path.join(got_dir, "trajectory.bin")))
+                want = _per_agent(read_trajectory(os.path.join(own, "trajectory.bin")))
+            else:
+                got, want = _read_csv(got_dir), _read_csv(own)
+            assert sorted(got) == sorted(want), f"scenario {k}"
+            for aid in want:
+                assert np.array_equal(got[aid][1], want[aid][1]), f"scenario {k} agent {aid}"
+                assert np.array_equal(got[aid][0], want[aid][0])
+
+
+def _per_agent(chunks):
+    """Binary chunks as {id: (times, xy)} (agents may join or leave between chunks)."""
+    per = {}
+    for ids, times, xy in chunks:
+        for j, aid in enumerate(ids.tolist()):
+            t, p = per.get(aid, ([], []))
+            per[aid] = (t + list(times), p + [xy[:, j]])
+    return {a: (np.array(t), np.concatenate(p)) for a, (t, p) in per.items()}

@@ -3939,7 +3939,7 @@ bool Engine::run_steps(int nsteps, bool record)
 	if (configured_maxnb_ != maxnb_ && !configure()) return false;
 	if (!ensure_static_grid()) return false;
 	steps_pending_ = true;
-	record = record && rec_ != nullptr;
+	record = record && !recs_.empty();
 	if (record && n_ > rec_cap_n_) {
 		// the population grew since the ring was sized (it was flushed then)
 		CK(cudaStreamSynchronize(stream_));
@@ -3972,10 +3972,15 @@ bool Engine::run_steps(int nsteps, bool record)
 		if (record && n_ > 0) {
 			// RunSimulationSteps hands the writer every agent's position after
 			// each step with the world's time (crowdSimulator.cpp:81-93)
-			if (rec_head_ == 0) rec_ids_ = id_;
+			if (rec_head_ == 0) {
+				rec_ids_ = id_;
+				rec_off_.resize(scen_.size() + 1);
+				for (size_t k = 0; k < scen_.size(); ++k) rec_off_[k] = scen_.size() == 1 ? 0 : scen_[k].agent_off;
+				rec_off_[scen_.size()] = n_;
+			}
 			CK(cudaMemcpyAsync(rec_ring_ + (size_t)rec_head_ * n_, d_->pos, sizeof(float2) * n_,
 			                   cudaMemcpyDeviceToDevice, stream_));
-			rec_times_.push_back(time_);
+			for (size_t k = 0; k < scen_.size(); ++k) rec_times_[k].push_back(scen_time((int)k));
 			++rec_head_;
 		}
 	}
@@ -3988,12 +3993,23 @@ bool Engine::run_steps(int nsteps, bool record)
 bool Engine::record_start(const std::string& dir, int ring_steps, int format)
 {
 	if (!sync()) return false;
-	if (rec_ && !record_stop()) return false;
+	if (!recs_.empty() && !record_stop()) return false;
 	if (ring_steps < 1) { err_ = "ring_steps must be positive"; return false; }
-	if (scen_.size() > 1) { err_ = "trajectory output is for single simulations"; return false; }
-	rec_ = new TrajWriter(dir, format);
-	const std::string e = rec_->error();
-	if (!e.empty()) { err_ = e; rec_free(); return false; }
+	if (scen_.size() == 1) {
+		recs_.push_back(new TrajWriter(dir, format));
+	} else {
+		// a batch: scenario k into dir/scenario_k
+		TrajWriter parent(dir, format);
+		std::string e = parent.error();
+		if (!e.empty()) { err_ = e; return false; }
+		std::string base = dir;
+		if (base.empty() || base.back() != '/') base += '/';
+		for (size_t k = 0; k < scen_.size(); ++k) recs_.push_back(new TrajWriter(base + "scenario_" + std::to_string(k), format));
+	}
+	for (TrajWriter* w : recs_) {
+		const std::string e = w->error();
+		if (!e.empty()) { err_ = e; rec_free(); return false; }
+	}
 	rec_R_ = ring_steps;
 	rec_cap_n_ = std::max(n_, 1);
 	if (!dalloc(rec_ring_, (size_t)rec_R_ * rec_cap_n_, err_)) { rec_free(); return false; }
@@ -4002,15 +4018,16 @@ bool Engine::record_start(const std::string& dir, int ring_steps, int format)
 		if (!rec_ev_[b]) CK(cudaEventCreateWithFlags(&rec_ev_[b], cudaEventDisableTiming));
 	}
 	rec_head_ = rec_snap_head_ = 0;
-	rec_times_.clear();
+	rec_times_.assign(scen_.size(), {});
 	return true;
 }
 
 bool Engine::rec_flush_async()
 {
-	if (!rec_ || rec_head_ == 0) return true;
+	if (recs_.empty() || rec_head_ == 0) return true;
 	const int b = rec_next_;
-	if (rec_busy_[b].load()) rec_->drain();
+	if (rec_busy_[b].load())
+		for (TrajWriter* w : recs_) w->drain();
 	const size_t floats = (size_t)rec_head_ * n_ * 2;
 	if (rec_host_cap_[b] < floats) {
 		if (rec_host_[b]) cudaFreeHost(rec_host_[b]);
@@ -4021,10 +4038,16 @@ bool Engine::rec_flush_async()
 	}
 	CK(cudaMemcpyAsync(rec_host_[b], rec_ring_, sizeof(float) * floats, cudaMemcpyDeviceToHost, stream_));
 	CK(cudaEventRecord(rec_ev_[b], stream_));
-	rec_busy_[b].store(1);
-	rec_->push(n_, rec_head_, rec_ids_, rec_times_, rec_host_[b], rec_ev_[b], &rec_busy_[b]);
+	// the ring's agents and times, scenario by scenario (the offsets of the
+	// ring's first step: the list does not change while the ring fills)
+	rec_busy_[b].store((int)recs_.size());
+	for (size_t k = 0; k < recs_.size(); ++k) {
+		const int o = rec_off_[k], m = rec_off_[k + 1] - o;
+		recs_[k]->push(m, rec_head_, std::vector<int>(rec_ids_.begin() + o, rec_ids_.begin() + o + m), rec_times_[k],
+		               rec_host_[b], rec_ev_[b], &rec_busy_[b], (int)rec_ids_.size(), o);
+	}
 	rec_head_ = rec_snap_head_ = 0;
-	rec_times_.clear();
+	rec_times_.assign(scen_.size(), {});
 	rec_next_ ^= 1;
 	// a grown population needs a larger ring before the next step is recorded
 	if (n_ > rec_cap_n_) {
@@ -4037,25 +4060,27 @@ bool Engine::rec_flush_async()
 
 bool Engine::rec_before_change()
 {
-	if (!rec_ || rec_head_ == 0) return true;
+	if (recs_.empty() || rec_head_ == 0) return true;
 	if (!sync()) return false;
 	return rec_flush_async();
 }
 
 bool Engine::record_flush()
 {
-	if (!rec_) return true;
+	if (recs_.empty()) return true;
 	if (!sync()) return false;
 	if (!rec_flush_async()) return false;
-	rec_->drain();
-	const std::string e = rec_->error();
-	if (!e.empty()) { err_ = e; return false; }
+	for (TrajWriter* w : recs_) {
+		w->drain();
+		const std::string e = w->error();
+		if (!e.empty()) { err_ = e; return false; }
+	}
 	return true;
 }
 
 bool Engine::record_stop()
 {
-	if (!rec_) return true;
+	if (recs_.empty()) return true;
 	const bool ok = record_flush();
 	rec_free();
 	return ok;
@@ -4063,8 +4088,8 @@ bool Engine::record_stop()
 
 void Engine::rec_free()
 {
-	delete rec_;   // drains and joins the writer
-	rec_ = nullptr;
+	for (TrajWriter* w : recs_) delete w;   // drains and joins the writers
+	recs_.clear();
 	if (rec_ring_) cudaFree(rec_ring_);
 	rec_ring_ = nullptr;
 	for (int b = 0; b < 2; ++b) {
@@ -4125,7 +4150,7 @@ bool Engine::restore_snapshot()
 	time_ = snap_time_;
 	times_ = snap_times_;
 	rec_head_ = rec_snap_head_;
-	rec_times_.resize(rec_head_);
+	for (auto& t : rec_times_) t.resize(rec_head_);
 	return true;
 }
 
@@ -4140,7 +4165,7 @@ bool Engine::step(int nsteps)
 		int left = nsteps;
 		while (left > 0) {
 			int k = left;
-			if (rec_) {
+			if (!recs_.empty()) {
 				if (rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
 				k = std::min(left, rec_R_ - rec_head_);
 			}
@@ -4153,7 +4178,7 @@ bool Engine::step(int nsteps)
 		// insertions and removals change the agent list between steps: settle
 		// every step before the host-side changes
 		for (int s = 0; s < nsteps; ++s) {
-			if (rec_ && rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
+			if (!recs_.empty() && rec_head_ == rec_R_ && (!sync() || !rec_flush_async())) return false;
 			if (agents_due() && !rec_before_change()) return false;
 			if (!pending_.empty() && !apply_pending_agents()) return false;
 			if (!take_snapshot()) return false;

@@ -269,10 +269,11 @@ private:
 	void diff_free();
 
 	// trajectory output state
-	TrajWriter* rec_ = nullptr;
+	std::vector<TrajWriter*> recs_;      // one per scenario (a batch writes each into its own folder)
+	std::vector<int> rec_off_;           // scenario offsets of the ring's agents
 	int rec_R_ = 0, rec_head_ = 0, rec_snap_head_ = 0, rec_cap_n_ = 0, rec_next_ = 0;
 	float2* rec_ring_ = nullptr;
-	std::vector<double> rec_times_;
+	std::vector<std::vector<double>> rec_times_;   // per scenario, each recorded step's time
 	std::vector<int> rec_ids_;
 	float* rec_host_[2] = { nullptr, nullptr };
 	size_t rec_host_cap_[2] = { 0, 0 };

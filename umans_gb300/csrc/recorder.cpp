@@ -34,11 +34,11 @@ std::string TrajWriter::error()
 }
 
 void TrajWriter::push(int n, int steps, std::vector<int> ids, std::vector<double> times, const float* xy,
-                      cudaEvent_t ready, std::atomic<int>* busy)
+                      cudaEvent_t ready, std::atomic<int>* busy, int stride, int offset)
 {
 	{
 		std::lock_guard<std::mutex> g(mu_);
-		jobs_.push_back(Job{ n, steps, std::move(ids), std::move(times), xy, ready, busy });
+		jobs_.push_back(Job{ n, steps, stride, offset, std::move(ids), std::move(times), xy, ready, busy });
 		++pending_;
 	}
 	cv_.notify_all();
@@ -63,7 +63,7 @@ void TrajWriter::run()
 		}
 		cudaEventSynchronize(j.ready);
 		write(j);
-		j.busy->store(0);
+		j.busy->fetch_sub(1);
 		{
 			std::lock_guard<std::mutex> g(mu_);
 			--pending_;
@@ -84,7 +84,8 @@ void TrajWriter::write(const Job& j)
 			std::fwrite(hdr, sizeof(int), 2, f);
 			std::fwrite(j.ids.data(), sizeof(int), (size_t)j.n, f);
 			std::fwrite(j.times.data(), sizeof(double), (size_t)j.steps, f);
-			std::fwrite(j.xy, sizeof(float), (size_t)j.steps * j.n * 2, f);
+			for (int s = 0; s < j.steps; ++s)
+				std::fwrite(j.xy + ((size_t)s * j.stride + j.offset) * 2, sizeof(float), (size_t)j.n * 2, f);
 			if (std::fclose(f) != 0) err = "write error in " + dir_ + "trajectory.bin";
 		}
 	} else {
@@ -94,7 +95,7 @@ void TrajWriter::write(const Job& j)
 			buf.clear();
 			char line[96];
 			for (int s = 0; s < j.steps; ++s) {
-				const float* p = j.xy + ((size_t)s * j.n + k) * 2;
+				const float* p = j.xy + ((size_t)s * j.stride + j.offset + k) * 2;
 				const int m = std::snprintf(line, sizeof(line), "%.10g,%.9g,%.9g\n", j.times[s], (double)p[0],
 				                            (double)p[1]);
 				buf.insert(buf.end(), line, line + m);

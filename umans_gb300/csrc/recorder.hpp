@@ -35,16 +35,18 @@ public:
 	~TrajWriter();
 	// error of the directory or of a write, empty when none
 	std::string error();
-	// Appends steps x n positions (xy, host memory valid once `ready` has
-	// completed); *busy is cleared when the writer no longer needs `xy`.
+	// Appends steps x n positions: agent k of step s at xy[(s * stride +
+	// offset + k) * 2] (host memory valid once `ready` has completed; a batch
+	// hands each scenario's writer its columns of one buffer).  *busy is
+	// decremented when the writer no longer needs `xy`.
 	void push(int n, int steps, std::vector<int> ids, std::vector<double> times, const float* xy,
-	          cudaEvent_t ready, std::atomic<int>* busy);
+	          cudaEvent_t ready, std::atomic<int>* busy, int stride, int offset);
 	// waits until every chunk pushed so far is written
 	void drain();
 
 private:
 	struct Job {
-		int n, steps;
+		int n, steps, stride, offset;
 		std::vector<int> ids;
 		std::vector<double> times;
 		const float* xy;
