@@ -3500,7 +3500,13 @@ bool Engine::download_mutable()
 // least 64), which keeps the lists of four agents per warp within shared
 // memory at full occupancy.  A list that later outgrows it sets
 // ST_NEIGHBOUR_OVERFLOW; sync() then re-runs the batch from its snapshot with
-// the capacity doubled (up to 3072 entries).
+// the capacity grown by half (up to 3072 entries): shared memory per block,
+// and so occupancy, follows the capacity.
+static int grown_capacity(int c)
+{
+	return std::min(3072, std::max(c + 32, (c + c / 2 + 31) / 32 * 32));
+}
+
 bool Engine::choose_maxnb()
 {
 	int want = opt_.max_neighbours;
@@ -4219,7 +4225,7 @@ bool Engine::sync()
 		if ((st & ST_NEIGHBOUR_OVERFLOW) && snap_valid_ && maxnb_ < 3072) {
 			const int steps = snap_steps_;
 			if (!restore_snapshot()) return false;
-			maxnb_ = std::min(3072, maxnb_ * 2);
+			maxnb_ = grown_capacity(maxnb_);
 			invalidate_graph();
 			if (!run_steps(steps, true)) return false;
 			continue;
@@ -4449,7 +4455,7 @@ bool Engine::autotune(int trial_steps, EngineOptions* chosen)
 					CK(cudaMemcpy(&st, d_->status, sizeof(int), cudaMemcpyDeviceToHost));
 					if (st) {   // a trial overflowed the neighbour capacity: grow it, discard the trial
 						CK(cudaMemset(d_->status, 0, sizeof(int)));
-						if (st & ST_NEIGHBOUR_OVERFLOW) maxnb_ = std::min(3072, maxnb_ * 2);
+						if (st & ST_NEIGHBOUR_OVERFLOW) maxnb_ = grown_capacity(maxnb_);
 						continue;
 					}
 					if (ms < best_ms) { best_ms = ms; best = opt_; }
@@ -4597,7 +4603,7 @@ bool Engine::diff_restore_start()
 
 // Waits for the stream; true when no device condition was raised.  A
 // neighbour-capacity overflow is reported through *overflow (the caller
-// re-runs with a doubled capacity).
+// re-runs with a grown capacity).
 bool Engine::diff_check_status()
 {
 	CK(cudaStreamSynchronize(stream_));
@@ -4606,7 +4612,7 @@ bool Engine::diff_check_status()
 	if (st == 0) return true;
 	CK(cudaMemset(d_->status, 0, sizeof(int)));
 	if ((st & ST_NEIGHBOUR_OVERFLOW) && maxnb_ < 3072) {
-		maxnb_ = std::min(3072, maxnb_ * 2);
+		maxnb_ = grown_capacity(maxnb_);
 		invalidate_graph();
 		err_ = "overflow";
 		return false;
