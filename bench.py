@@ -723,7 +723,8 @@ def run_ours(args):
                          "frac": achieved / peak, "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
                          "traffic": (tpa * n if tpa else None)},
         "grid_build": {"kernels": "k_count_scan, k_scatter (static toric grid)", "ms": grid_ms,
-                       "ms_in_graph": t_ms / args.steps - agent_ms,
+                       # null when the two legs' kernels differ (e.g. a capacity change in one leg)
+                       "ms_in_graph": (t_ms / args.steps - agent_ms) if t_ms / args.steps > agent_ms else None,
                        "alg_bytes_per_agent": GRID_BYTES_PER_AGENT,
                        "achieved": GRID_BYTES_PER_AGENT * n / (grid_ms * 1e-3) / 1e9 if grid_ms > 0 else None,
                        "peak": peak, "unit": "GB/s",
