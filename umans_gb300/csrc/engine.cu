@@ -2991,30 +2991,53 @@ __global__ void k_inject(int n, const float2* pos, const float2* target, float w
 }
 
 // GetAgentPositions (APIFunctions.cpp:90-115): one record per agent
-__global__ void k_pack(DevState S)
+// The AgentData records (28 bytes: id, position, velocity, viewing
+// direction) move through shared memory, so that the block's stretch of
+// records is read or written as consecutive 4-byte words: coalesced, also
+// when the buffer is page-locked host memory that the kernel accesses
+// directly.
+constexpr int PACK_BLOCK = 256, REC_WORDS = (int)(sizeof(AgentRecord) / 4);
+static_assert(sizeof(AgentRecord) == 28, "AgentData layout");
+
+// GetAgentPositions (APIFunctions.cpp:88-115): the records of slots [0, n)
+__global__ void __launch_bounds__(PACK_BLOCK) k_pack(DevState S, AgentRecord* dst)
 {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= S.n) return;
-	const float2 p = S.pos[i], v = S.vel[i], w = S.view[i];
-	AgentRecord r;
-	r.id = S.id[i]; r.px = p.x; r.py = p.y; r.vx = v.x; r.vy = v.y; r.wx = w.x; r.wy = w.y;
-	S.io[i] = r;
+	__shared__ uint32_t w[PACK_BLOCK * REC_WORDS];
+	const int i0 = blockIdx.x * PACK_BLOCK, i = i0 + threadIdx.x;
+	const int cnt = min(PACK_BLOCK, S.n - i0);
+	if (i < S.n) {
+		const float2 p = S.pos[i], v = S.vel[i], vw = S.view[i];
+		uint32_t* r = w + threadIdx.x * REC_WORDS;
+		r[0] = (uint32_t)S.id[i];
+		r[1] = __float_as_uint(p.x); r[2] = __float_as_uint(p.y);
+		r[3] = __float_as_uint(v.x); r[4] = __float_as_uint(v.y);
+		r[5] = __float_as_uint(vw.x); r[6] = __float_as_uint(vw.y);
+	}
+	__syncthreads();
+	uint32_t* out = reinterpret_cast<uint32_t*>(dst) + (size_t)i0 * REC_WORDS;
+	for (int k = threadIdx.x; k < cnt * REC_WORDS; k += PACK_BLOCK) out[k] = w[k];
 }
 
 // SetAgentPositions (APIFunctions.cpp:117-137): Agent::setPosition and
 // Agent::setVelocity_ExternalApplication for every listed id that exists
-__global__ void k_unpack(DevState S, int m)
+__global__ void __launch_bounds__(PACK_BLOCK) k_unpack(DevState S, const AgentRecord* src, int m)
 {
-	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	__shared__ uint32_t w[PACK_BLOCK * REC_WORDS];
+	const int k0 = blockIdx.x * PACK_BLOCK, k = k0 + threadIdx.x;
+	const int cnt = min(PACK_BLOCK, m - k0);
+	const uint32_t* in = reinterpret_cast<const uint32_t*>(src) + (size_t)k0 * REC_WORDS;
+	for (int j = threadIdx.x; j < cnt * REC_WORDS; j += PACK_BLOCK) w[j] = in[j];
+	__syncthreads();
 	if (k >= m) return;
-	const AgentRecord r = S.io[k];
-	if (r.id < 0 || r.id >= S.id_bound) return;
-	const int i = S.slot_of_id[r.id];
+	const uint32_t* r = w + threadIdx.x * REC_WORDS;
+	const int id = (int)r[0];
+	if (id < 0 || id >= S.id_bound) return;
+	const int i = S.slot_of_id[id];
 	if (i < 0) return;
-	S.pos[i] = V(r.px, r.py);
-	S.vel[i] = V(r.vx, r.vy);
-	S.vwf[i] = V(r.vx, r.vy);
-	S.view[i] = V(r.wx, r.wy);
+	S.pos[i] = V(__uint_as_float(r[1]), __uint_as_float(r[2]));
+	S.vel[i] = V(__uint_as_float(r[3]), __uint_as_float(r[4]));
+	S.vwf[i] = V(__uint_as_float(r[3]), __uint_as_float(r[4]));
+	S.view[i] = V(__uint_as_float(r[5]), __uint_as_float(r[6]));
 }
 
 // ------------------------------------------------------------------------
@@ -3425,6 +3448,18 @@ static bool is_pinned(const void* p)
 	return a.type == cudaMemoryTypeHost;
 }
 
+// The device's address of page-locked host memory (kernels read and write it
+// directly), or null for other memory
+static void* host_device_view(const void* p)
+{
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Page-locked staging for AgentData exchange with pageable caller buffers:
 // a host copy into it plus a page-locked transfer beats the driver's
 // pageable path.
@@ -3445,15 +3480,24 @@ bool Engine::get_agent_data(void* out)
 	if (!sync()) return false;
 	if (n_ == 0) return true;
 	S.n = n_;
-	k_pack<<<(n_ + 255) / 256, 256, 0, stream_>>>(S);
+	const int nb = (n_ + PACK_BLOCK - 1) / PACK_BLOCK;
 	const size_t bytes = sizeof(AgentRecord) * n_;
-	if (is_pinned(out)) {
-		CK(cudaMemcpyAsync(out, S.io, bytes, cudaMemcpyDeviceToHost, stream_));
+	// page-locked output: the kernel writes it directly
+	if (AgentRecord* dv = static_cast<AgentRecord*>(host_device_view(out))) {
+		k_pack<<<nb, PACK_BLOCK, 0, stream_>>>(S, dv);
+		CK(cudaGetLastError());
 		CK(cudaStreamSynchronize(stream_));
 		return true;
 	}
 	if (!stage(n_)) return false;
-	CK(cudaMemcpyAsync(io_host_, S.io, bytes, cudaMemcpyDeviceToHost, stream_));
+	AgentRecord* sv = static_cast<AgentRecord*>(host_device_view(io_host_));
+	if (sv) {
+		k_pack<<<nb, PACK_BLOCK, 0, stream_>>>(S, sv);
+	} else {
+		k_pack<<<nb, PACK_BLOCK, 0, stream_>>>(S, S.io);
+		CK(cudaMemcpyAsync(io_host_, S.io, bytes, cudaMemcpyDeviceToHost, stream_));
+	}
+	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(stream_));
 	std::memcpy(out, io_host_, bytes);
 	return true;
@@ -3464,19 +3508,28 @@ bool Engine::set_agent_data(const void* in, int m)
 	DevState& S = *d_;
 	if (!sync()) return false;
 	if (m <= 0) return true;
-	if (m > cap_ && !dalloc(S.io, (size_t)m, err_)) return false;
 	const size_t bytes = sizeof(AgentRecord) * m;
-	if (is_pinned(in)) {
-		CK(cudaMemcpyAsync(S.io, in, bytes, cudaMemcpyHostToDevice, stream_));
-	} else {
-		if (!stage(m)) return false;
-		std::memcpy(io_host_, in, bytes);
-		CK(cudaMemcpyAsync(S.io, io_host_, bytes, cudaMemcpyHostToDevice, stream_));
+	const int nb = (m + PACK_BLOCK - 1) / PACK_BLOCK;
+	// page-locked input: the kernel reads it directly
+	if (const AgentRecord* dv = static_cast<const AgentRecord*>(host_device_view(in))) {
+		k_unpack<<<nb, PACK_BLOCK, 0, stream_>>>(S, dv, m);
+		CK(cudaGetLastError());
+		CK(cudaStreamSynchronize(stream_));
+		return true;
 	}
-	k_unpack<<<(m + 255) / 256, 256, 0, stream_>>>(S, m);
+	if (!stage(m)) return false;
+	std::memcpy(io_host_, in, bytes);
+	const AgentRecord* sv = static_cast<const AgentRecord*>(host_device_view(io_host_));
+	if (sv) {
+		k_unpack<<<nb, PACK_BLOCK, 0, stream_>>>(S, sv, m);
+	} else {
+		if (m > cap_ && !dalloc(S.io, (size_t)m, err_)) return false;
+		CK(cudaMemcpyAsync(S.io, io_host_, bytes, cudaMemcpyHostToDevice, stream_));
+		k_unpack<<<nb, PACK_BLOCK, 0, stream_>>>(S, S.io, m);
+	}
 	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(stream_));
-	if (m > cap_ && !dalloc(S.io, (size_t)std::max(cap_, 1), err_)) return false;
+	if (!sv && m > cap_ && !dalloc(S.io, (size_t)std::max(cap_, 1), err_)) return false;
 	return true;
 }
 
