@@ -55,6 +55,7 @@ struct DevState {
 	int *sSlot, *sId;
 	int *cell, *cnt, *start, *blocksum;   // cnt: per-cell histogram, zero between steps
 	unsigned* ticket;       // blocks of k_count_scan done (zero between launches)
+	unsigned* gbar;         // k_grid_coop's barrier: arrivals, generation
 	GridParams* grid;       // [nscen]
 	unsigned* bbox;         // [4 * nscen]
 	// profiling only (else null): Karamouzas samples inside the window, pairs
@@ -411,6 +412,39 @@ __global__ void __launch_bounds__(1024) k_count_scan(DevState S, int cap)
 	block_scan_cells(S, nc, sm);
 }
 
+// Barrier of all blocks of a cooperative launch (every block resident): an
+// arrival count and a generation word.  The last block to arrive resets the
+// count and advances the generation.  The wait is bounded: after GBAR_SPINS
+// polls the block records ST_GRID_BARRIER and goes on (the host then reports
+// an error).  That cannot happen while every block is resident, which the
+// cooperative launch guarantees.
+constexpr int GBAR_SPINS = 1 << 22;
+__device__ __forceinline__ void grid_barrier(const DevState& S)
+{
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		volatile unsigned* gen = S.gbar + 1;
+		const unsigned g = *gen;
+		__threadfence();
+		if (atomicAdd(S.gbar, 1u) == gridDim.x - 1) {
+			S.gbar[0] = 0u;
+			__threadfence();
+			atomicAdd(S.gbar + 1, 1u);
+		} else {
+			int spins = 0;
+			while (*gen == g) {
+				if (++spins > GBAR_SPINS) {
+					atomicOr(S.status, ST_GRID_BARRIER);
+					break;
+				}
+				__nanosleep(32);
+			}
+		}
+		__threadfence();
+	}
+	__syncthreads();
+}
+
 // The same exclusive scan in one block, for grids of at most
 // SCAN_SINGLE_MAX_CELLS cells (one launch instead of three): each warp scans
 // a contiguous range of cells in coalesced chunks of 32, after a first pass
@@ -470,7 +504,7 @@ __device__ __forceinline__ void scatter_one(const DevState& S, int i)
 	int top = 0;
 	if (lane == leader) top = atomicSub(&S.cnt[c], __popc(peers));
 	top = __shfl_sync(peers, top, leader);
-	const int t = S.start[c] + top - __popc(peers) + __popc(peers & ((1u << lane) - 1u));
+	const int t = __ldcg(S.start + c) + top - __popc(peers) + __popc(peers & ((1u << lane) - 1u));
 	const float2 p = S.pos[i];
 	const float2 g = S.goal[i];
 	const float4 prm = S.prm[i];
@@ -496,6 +530,92 @@ __global__ void k_scatter(DevState S)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < S.n) scatter_one(S, i);
+}
+
+// The whole grid build of a static grid in one cooperative launch: the
+// histogram (blocks striding over the agents), a barrier, each block's sum of
+// its stretch of cells, a barrier, each block's exclusive scan of its stretch
+// (after the sums of the stretches before it), a barrier, the scatter.  No
+// one-block scan and no launch in between.
+__global__ void __launch_bounds__(1024) k_grid_coop(DevState S)
+{
+	const int n = S.n, nt = blockDim.x, tid = threadIdx.x;
+	const int stride = gridDim.x * nt;
+	for (int i = blockIdx.x * nt + tid; i < n; i += stride) {
+		// the scatter's inputs, fetched into L2 while the count and scan run
+		asm volatile("prefetch.global.L2 [%0];" ::"l"(S.vel + i));
+		asm volatile("prefetch.global.L2 [%0];" ::"l"(S.goal + i));
+		asm volatile("prefetch.global.L2 [%0];" ::"l"(S.prm + i));
+		asm volatile("prefetch.global.L2 [%0];" ::"l"(S.id + i));
+		const int sc = S.agent_scen[i];
+		count_one(S, i, S.grid[sc], S.cell_base[sc]);
+	}
+	grid_barrier(S);
+	const int nc = S.cell_base[S.nscen];
+	const int seg = (nc + gridDim.x - 1) / gridDim.x;
+	const int c0 = min(nc, (int)blockIdx.x * seg), c1 = min(nc, c0 + seg);
+	__shared__ int red[32];
+	const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+	// block sum of the stretch
+	int s = 0;
+	for (int c = c0 + tid; c < c1; c += nt) s += __ldcg(S.cnt + c);
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if (lane == 0) red[warp] = s;
+	__syncthreads();
+	if (tid == 0) {
+		int t = 0;
+		for (int w = 0; w < nw; ++w) t += red[w];
+		S.blocksum[blockIdx.x] = t;
+	}
+	grid_barrier(S);
+	// the sums of the stretches before this one
+	int before = 0;
+	for (int b = tid; b < (int)blockIdx.x; b += nt) before += __ldcg(S.blocksum + b);
+	for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+	__syncthreads();
+	if (lane == 0) red[warp] = before;
+	__syncthreads();
+	if (warp == 0) {
+		int v = lane < nw ? red[lane] : 0;
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+		if (lane == 0) red[0] = v;
+	}
+	__syncthreads();
+	int run = red[0];
+	__syncthreads();
+	// exclusive scan of the stretch, 1024 cells per round
+	for (int base = c0; base < c1; base += nt) {
+		const int c = base + tid;
+		const int v = c < c1 ? __ldcg(S.cnt + c) : 0;
+		int incl = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, incl, o);
+			if (lane >= o) incl += u;
+		}
+		if (lane == 31) red[warp] = incl;
+		__syncthreads();
+		if (warp == 0) {
+			const int wv = lane < nw ? red[lane] : 0;
+			int w = wv;
+			for (int o = 1; o < 32; o <<= 1) {
+				const int u = __shfl_up_sync(0xffffffffu, w, o);
+				if (lane >= o) w += u;
+			}
+			if (lane < nw) red[lane] = w - wv;
+		}
+		__syncthreads();
+		if (c < c1) S.start[c] = run + red[warp] + incl - v;
+		const int tot = __shfl_sync(0xffffffffu, incl, 31);
+		__syncthreads();
+		// the round's total: the last warp's offset plus its own total
+		if (warp == nw - 1 && lane == 31) red[0] = red[nw - 1] + tot;
+		__syncthreads();
+		run += red[0];
+		__syncthreads();
+	}
+	if (blockIdx.x == 0 && tid == 0) S.start[nc] = n;
+	grid_barrier(S);
+	for (int i = blockIdx.x * nt + tid; i < n; i += stride) scatter_one(S, i);
 }
 
 // The whole grid build of a small single-scenario world in one block (the
@@ -3380,10 +3500,11 @@ bool Engine::alloc(int cap)
 	    !dalloc(S.sB, cap, err_) || !dalloc(S.sE, cap, err_) || !dalloc(S.sSlot, cap, err_) || !dalloc(S.sId, cap, err_) ||
 	    !dalloc(S.cell, cap, err_) || !dalloc(S.agent_scen, cap, err_) || !dalloc(S.cnt, mc + 1, err_) ||
 	    !dalloc(S.start, mc + 1, err_) ||
-	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 3, err_))
+	    !dalloc(S.blocksum, mc / SCAN_PER_BLOCK + 5, err_))
 		return false;
 	S.ticket = reinterpret_cast<unsigned*>(S.blocksum + mc / SCAN_PER_BLOCK + 2);
-	CK(cudaMemset(S.ticket, 0, sizeof(unsigned)));
+	S.gbar = reinterpret_cast<unsigned*>(S.blocksum + mc / SCAN_PER_BLOCK + 3);
+	CK(cudaMemset(S.ticket, 0, 3 * sizeof(unsigned)));
 	if (!S.grid && !dalloc(S.grid, ns, err_)) return false;
 	if (!S.bbox && !dalloc(S.bbox, 4 * ns, err_)) return false;
 	if (!S.cell_base && !dalloc(S.cell_base, ns + 1, err_)) return false;
@@ -3769,6 +3890,10 @@ void Engine::enqueue_grid(const DevState& S)
 		k_grid<<<1, 1024, 0, stream_>>>(S);
 	}
 	const int cells_bound = grid_fixed ? static_cells_ : S.max_cells;
+	if (grid_fixed && coop_state_ > 0) {
+		launch_grid_coop(S);   // a launch error is caught after the step is enqueued
+		return;
+	}
 	if (grid_fixed && cells_bound <= SCAN_SMEM_MAX_CELLS) {
 		k_count_scan<<<std::max(1, (n_ + 1023) / 1024), 1024, scan_smem_bytes(cells_bound), stream_>>>(S, cells_bound);
 		k_scatter<<<nb, threads, 0, stream_>>>(S);
@@ -3788,11 +3913,58 @@ void Engine::enqueue_grid(const DevState& S)
 	k_scatter<<<nb, threads, 0, stream_>>>(S);
 }
 
+// The one-launch grid build (k_grid_coop): one block per SM (the agents
+// spread over all of them, one per thread), blocks of up to 1024 threads,
+// more blocks only when the agents need them (at most as many as are
+// resident at once).
+cudaError_t Engine::launch_grid_coop(const DevState& S)
+{
+	const int threads = std::min(1024, std::max(32, (n_ + num_sms_ - 1) / num_sms_ + 31) / 32 * 32);
+	const int want = std::max(1, (n_ + threads - 1) / threads);
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3((unsigned)std::min(want, coop_blocks_max_));
+	cfg.blockDim = dim3(threads);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = stream_;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeCooperative;
+	attr[0].val.cooperative = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, k_grid_coop, S);
+}
+
+// Once, outside any capture: whether the cooperative launch can be captured
+// into a graph (a throwaway capture, never launched).  If not, the static
+// grid is built in two launches.
+void Engine::probe_grid_coop()
+{
+	if (coop_state_ != 0) return;
+	coop_state_ = -1;
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_coop, 1024, 0) != cudaSuccess || per_sm < 1) {
+		cudaGetLastError();
+		return;
+	}
+	coop_blocks_max_ = per_sm * num_sms_;
+	if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaGetLastError();
+		return;
+	}
+	const cudaError_t e = launch_grid_coop(*d_);
+	cudaGraph_t g = nullptr;
+	const cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+	if (g) cudaGraphDestroy(g);
+	cudaGetLastError();
+	if (e == cudaSuccess && e2 == cudaSuccess) coop_state_ = 1;
+}
+
 // Toric worlds only: the grid parameters and cell ranges, which do not
 // change between steps, computed once outside any graph capture.
 bool Engine::ensure_static_grid()
 {
 	if (!toric_only_ || static_grid_ready_ || small_world()) return true;
+	probe_grid_coop();
 	DevState& S = *d_;
 	S.n = n_;
 	k_grid<<<1, 1024, 0, stream_>>>(S);
@@ -3830,6 +4002,7 @@ int Engine::kernels_per_step() const
 	if (small_world()) return 1 + (int)groups_.size();
 	const bool grid_fixed = toric_only_ && static_grid_ready_;
 	const int cells_bound = grid_fixed ? static_cells_ : d_->max_cells;
+	if (grid_fixed && coop_state_ > 0) return 1 + (int)groups_.size();
 	if (grid_fixed && cells_bound <= SCAN_SMEM_MAX_CELLS) return 2 + (int)groups_.size();
 	const bool single = cells_bound <= SCAN_SINGLE_MAX_CELLS;
 	return (grid_fixed ? 0 : 2) + 1 + (single ? 1 : 3) + 1 + (int)groups_.size();
@@ -4289,6 +4462,7 @@ bool Engine::sync()
 			return false;
 		}
 		if (st & ST_GRID_OVERFLOW) { err_ = "non-finite agent positions"; return false; }
+		if (st & ST_GRID_BARRIER) { err_ = "grid build: a block gave up waiting at a grid barrier"; return false; }
 		err_ = "device status " + std::to_string(st);
 		return false;
 	}

@@ -149,6 +149,10 @@ private:
 	void enqueue_step();
 	void enqueue_grid(const DevState& S);
 	bool ensure_static_grid();
+	cudaError_t launch_grid_coop(const DevState& S);
+	void probe_grid_coop();
+	int coop_state_ = 0;        // one-launch grid build: 0 untried, 1 usable, -1 not capturable
+	int coop_blocks_max_ = 1;
 	bool toric_only_ = false;          // every scenario's world is toric: the grid is fixed
 	bool static_grid_ready_ = false;   // its parameters are on the device
 	int static_cells_ = 0;             // its cell count

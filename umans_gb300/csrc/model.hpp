@@ -116,6 +116,7 @@ enum StatusBits : int {
 	ST_NEIGHBOUR_OVERFLOW = 1,
 	ST_ORCA_OVERFLOW = 2,
 	ST_GRID_OVERFLOW = 4,
+	ST_GRID_BARRIER = 8,   // a grid barrier of the one-launch grid build gave up waiting
 };
 
 }  // namespace umans
