@@ -2517,8 +2517,10 @@ __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 	if (__any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
 }
 
+// MODE 2: every policy is the global method with one ORCA cost (the ORCA
+// solve only: 64 registers, 8 blocks per SM, against 128 and 4 for MODE 0).
 template <int MODE, bool TAPE = false, bool OBST = true, bool SAMP = false>
-__global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, int dump)
+__global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_agent(DevState S, int dump)
 {
 	extern __shared__ unsigned char smem[];
 	const int lane = threadIdx.x & 31;
@@ -2626,7 +2628,13 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : 4) k_agent(DevState S, in
 		float2 nv = V(0, 0);
 		uint32_t rng_next = 0;
 		bool rng_used = false;
-		if (!viszero(A.pref)) {
+		if (MODE == 2 && !viszero(A.pref)) {
+			// global method, one ORCA cost: its solution (ORCA::GetGlobalMinimum)
+			int nl = 0;
+			const float2 best = orca_solve(A, N, pol.cost[0], lines, proj, &nl, lane);
+			const float2 acc = vclamp(vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt)), A.maxacc);
+			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
+		} else if (MODE == 0 && !viszero(A.pref)) {
 			CostPrep P;
 			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
 			for (int ci = 0; ci < pol.ncost; ++ci) {
@@ -3285,11 +3293,13 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	// ORCA cost, the others (k_agent<0>); cell space orders scenarios by group
 	{
 		std::vector<int> cls(scen_.size(), 0);
+		std::vector<char> pure_orca(scen_.size(), 1);   // every policy: global method, one ORCA cost
 		for (size_t k = 0; k < scen_.size(); ++k) {
 			bool force_only = true, orca = false;
 			for (size_t pi = 0; pi < pols_.size(); ++pi) {
 				if (pol_scen_[pi] != (int)k) continue;
 				const PolicyDesc& P = pols_[pi];
+				if (!(P.method == M_GLOBAL && P.ncost == 1 && P.cost[0].kind == K_ORCA)) pure_orca[k] = 0;
 				// any method: the force-only kernels pick the velocity from the
 				// cost targets (gradient step, global minimum or sample argmin)
 				for (int c = 0; c < P.ncost; ++c) {
@@ -3308,6 +3318,11 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 				if (cls[k] == c) scen_order_.push_back((int)k);
 			if ((int)scen_order_.size() > j0) {
 				KGroup g{ c == 0 ? 1 : 0, j0, (int)scen_order_.size(), 0, 0, 0 };
+				if (c == 1) {
+					bool all = true;
+					for (int j = j0; j < g.j1; ++j) all = all && pure_orca[scen_order_[j]];
+					if (all) g.mode = 2;   // k_agent<2>: the ORCA-only kernel
+				}
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
 				g.quad_ok = g.mode == 1 && !g.obst;
 				g.samp = false;
@@ -3736,7 +3751,9 @@ static int quad_blocks_for(int num_sms, int warps_per_block, size_t smem)
 static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int mode = 0, bool obst = true)
 {
 	int per_sm = 0;
-	if (mode == 1 && !obst)
+	if (mode == 2)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<2>, warps_per_block * 32, smem);
+	else if (mode == 1 && !obst)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1, false, false>, warps_per_block * 32, smem);
 	else if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1>, warps_per_block * 32, smem);
 	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<0>, warps_per_block * 32, smem);
@@ -3763,6 +3780,8 @@ bool Engine::configure()
 	if (smem0 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
 		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+		CK(cudaFuncSetAttribute(k_agent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+		CK(cudaFuncSetAttribute(k_agent<2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
 	}
 	if (smem1 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
@@ -3849,6 +3868,9 @@ void Engine::enqueue_step()
 				else k_force_quad<false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			} else if (wl) k_force_quad<false, false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			else k_force_quad<false><<<blocks, wpb * 32, smemq, st>>>(A);
+		} else if (g.mode == 2) {   // taped runs have no ORCA policy (diff_begin checks)
+			if (g.obst) k_agent<2><<<blocks, wpb * 32, smem0, st>>>(A, 0);
+			else k_agent<2, false, false><<<blocks, wpb * 32, smem0, st>>>(A, 0);
 		} else if (g.mode == 1 && g.samp && !S.tape_list) {
 			if (g.obst) k_agent<1, false, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
 			else k_agent<1, false, false, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
