@@ -1446,6 +1446,9 @@ __device__ __forceinline__ float rng_uniform(uint32_t x, float a, float b)
 #endif
 constexpr int KS = UMANS_KS;
 
+// KARA: every policy of the launch samples a regular schedule with one
+// Karamouzas cost (the general sampler is compiled out)
+template <bool KARA = false>
 __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView& N, const PolicyDesc& pol,
                              const CostPrep& P, uint32_t rng0, int lane, float4* pair4, float* pairv)
 {
@@ -1462,7 +1465,7 @@ __device__ float2 sample_min(const DevState& S, const AgentCtx& A, const NbView&
 	const int ncost = pol.single_cost ? 1 : pol.ncost;
 	float bestC = MAXF;
 	int bestI = 0x7fffffff;
-	if (ncost == 1 && pol.cost[0].kind == K_KARAMOUZAS && !pol.table_random) {
+	if (KARA || (ncost == 1 && pol.cost[0].kind == K_KARAMOUZAS && !pol.table_random)) {
 		// Karamouzas alone: most samples fall outside its window (cost MAXF);
 		// the lanes test the windows of 32 samples at a time, then the warp
 		// sweeps the neighbours for each sample inside, in sample order.
@@ -1818,6 +1821,37 @@ __device__ float2 force_and_contact(const AgentCtx& A, const NbView& N, const Co
 	const float2 sum = list_sum(fx, fy, N.K, lane);
 	__syncwarp();
 	return vadd(sum, obstacle_force(A, N, c, lane));
+}
+
+// Karamouzas's per-agent terms (Karamouzas.cpp: the time to collision at the
+// preferred velocity, its deviation window): the time is a min, so lanes
+// split the neighbours.
+__device__ __forceinline__ void karamouzas_prep(const AgentCtx& A, const NbView& N, const CostDesc& c, int ci,
+                                                int lane, CostPrep* P)
+{
+	float m = MAXF;
+	const float md2 = c.range * c.range;
+	for (int k = lane; k < N.K; k += 32) {
+		if (N.d2[k] > md2) continue;
+		const float tt = ttc_pair(A.pos, A.pref, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
+		if (tt == 0) continue;
+		if (tt < m) m = tt;
+	}
+	for (int k = lane; k < N.KO; k += 32) {
+		float2 a, b;
+		nb_seg(N, k, &a, &b);
+		if (dist2_to_segment(A.pos, a, b) > md2) continue;
+		const float tt = ttc_segment(A.pos, A.pref, A.radius, a, b);
+		if (tt == 0) continue;
+		if (tt < m) m = tt;
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		const float x = __shfl_xor_sync(0xffffffffu, m, o);
+		if (x < m) m = x;
+	}
+	P->ttcp[ci] = m;
+	P->maxdev[ci] = karamouzas_maxdev(m);
+	P->cosdev[ci] = cosf(P->maxdev[ci]);
 }
 
 // Candidate velocity i of a sampling policy (costFunction.cpp:99-158): the
@@ -2519,6 +2553,10 @@ __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 
 // MODE 2: every policy is the global method with one ORCA cost (the ORCA
 // solve only: 64 registers, 8 blocks per SM, against 128 and 4 for MODE 0).
+// MODE 3: every policy samples a regular schedule with one Karamouzas cost
+// (the general sampler compiled out: 21% faster than MODE 0 on a 100k-agent
+// corridor at the same 128 registers; at 96 registers it spilled and was
+// slower).
 template <int MODE, bool TAPE = false, bool OBST = true, bool SAMP = false>
 __global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_agent(DevState S, int dump)
 {
@@ -2634,38 +2672,22 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_ag
 			const float2 best = orca_solve(A, N, pol.cost[0], lines, proj, &nl, lane);
 			const float2 acc = vclamp(vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt)), A.maxacc);
 			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
+		} else if (MODE == 3 && !viszero(A.pref)) {
+			// sampling a regular schedule with one Karamouzas cost
+			CostPrep P;
+			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
+			karamouzas_prep(A, N, pol.cost[0], 0, lane, &P);
+			const float2 best = sample_min<true>(S, A, N, pol, P, S.rng[slot], lane, lines, reinterpret_cast<float*>(proj));
+			const float2 acc = vclamp(vdiv(vsub(best, A.vel), fmaxr(pol.relax_time, A.dt)), A.maxacc);
+			nv = vclamp(vadd(A.vel, vmul(acc, A.dt)), A.maxspeed);
 		} else if (MODE == 0 && !viszero(A.pref)) {
 			CostPrep P;
 			P.lines = lines; P.nlines = 0; P.orca_v = V(0, 0);
 			for (int ci = 0; ci < pol.ncost; ++ci) {
 				const CostDesc& c = pol.cost[ci];
 				if (is_force_based(c.kind)) P.target[ci] = target_velocity(A, N, c, lane, fx, fy);
-				else if (c.kind == K_KARAMOUZAS) {
-					// TTC at the preferred velocity: a min, so lanes split the neighbours
-					float m = MAXF;
-					const float md2 = c.range * c.range;
-					for (int k = lane; k < K; k += 32) {
-						if (N.d2[k] > md2) continue;
-						const float tt = ttc_pair(A.pos, A.pref, A.radius, nb_pos(N, k), nb_vel(N, k), nb_radius(N, k));
-						if (tt == 0) continue;
-						if (tt < m) m = tt;
-					}
-					for (int k = lane; k < N.KO; k += 32) {
-						float2 a, b;
-						nb_seg(N, k, &a, &b);
-						if (dist2_to_segment(A.pos, a, b) > md2) continue;
-						const float tt = ttc_segment(A.pos, A.pref, A.radius, a, b);
-						if (tt == 0) continue;
-						if (tt < m) m = tt;
-					}
-					for (int o = 16; o > 0; o >>= 1) {
-						const float x = __shfl_xor_sync(0xffffffffu, m, o);
-						if (x < m) m = x;
-					}
-					P.ttcp[ci] = m;
-					P.maxdev[ci] = karamouzas_maxdev(m);
-					P.cosdev[ci] = cosf(P.maxdev[ci]);
-				} else if (c.kind == K_ORCA) {
+				else if (c.kind == K_KARAMOUZAS) karamouzas_prep(A, N, c, ci, lane, &P);
+				else if (c.kind == K_ORCA) {
 					P.orca_v = orca_solve(A, N, c, lines, proj, &P.nlines, lane);
 				}
 			}
@@ -3294,12 +3316,15 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 	{
 		std::vector<int> cls(scen_.size(), 0);
 		std::vector<char> pure_orca(scen_.size(), 1);   // every policy: global method, one ORCA cost
+		std::vector<char> pure_kara(scen_.size(), 1);   // every policy: regular sampling, one Karamouzas cost
 		for (size_t k = 0; k < scen_.size(); ++k) {
 			bool force_only = true, orca = false;
 			for (size_t pi = 0; pi < pols_.size(); ++pi) {
 				if (pol_scen_[pi] != (int)k) continue;
 				const PolicyDesc& P = pols_[pi];
 				if (!(P.method == M_GLOBAL && P.ncost == 1 && P.cost[0].kind == K_ORCA)) pure_orca[k] = 0;
+				if (!(P.method == M_SAMPLING && P.ncost == 1 && P.cost[0].kind == K_KARAMOUZAS && P.s_type == 0))
+					pure_kara[k] = 0;
 				// any method: the force-only kernels pick the velocity from the
 				// cost targets (gradient step, global minimum or sample argmin)
 				for (int c = 0; c < P.ncost; ++c) {
@@ -3322,6 +3347,10 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 					bool all = true;
 					for (int j = j0; j < g.j1; ++j) all = all && pure_orca[scen_order_[j]];
 					if (all) g.mode = 2;   // k_agent<2>: the ORCA-only kernel
+				} else if (c == 2) {
+					bool all = true;
+					for (int j = j0; j < g.j1; ++j) all = all && pure_kara[scen_order_[j]];
+					if (all) g.mode = 3;   // k_agent<3>: the Karamouzas-sampling kernel
 				}
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
 				g.quad_ok = g.mode == 1 && !g.obst;
@@ -3753,6 +3782,8 @@ static int agent_blocks_for(int num_sms, int warps_per_block, size_t smem, int m
 	int per_sm = 0;
 	if (mode == 2)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<2>, warps_per_block * 32, smem);
+	else if (mode == 3)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<3>, warps_per_block * 32, smem);
 	else if (mode == 1 && !obst)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1, false, false>, warps_per_block * 32, smem);
 	else if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent<1>, warps_per_block * 32, smem);
@@ -3782,6 +3813,8 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_agent<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
 		CK(cudaFuncSetAttribute(k_agent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
 		CK(cudaFuncSetAttribute(k_agent<2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+		CK(cudaFuncSetAttribute(k_agent<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
+		CK(cudaFuncSetAttribute(k_agent<3, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
 	}
 	if (smem1 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
@@ -3871,6 +3904,9 @@ void Engine::enqueue_step()
 		} else if (g.mode == 2) {   // taped runs have no ORCA policy (diff_begin checks)
 			if (g.obst) k_agent<2><<<blocks, wpb * 32, smem0, st>>>(A, 0);
 			else k_agent<2, false, false><<<blocks, wpb * 32, smem0, st>>>(A, 0);
+		} else if (g.mode == 3) {   // nor a sampling one
+			if (g.obst) k_agent<3><<<blocks, wpb * 32, smem0, st>>>(A, 0);
+			else k_agent<3, false, false><<<blocks, wpb * 32, smem0, st>>>(A, 0);
 		} else if (g.mode == 1 && g.samp && !S.tape_list) {
 			if (g.obst) k_agent<1, false, true, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
 			else k_agent<1, false, false, true><<<blocks, wpb * 32, smem1, st>>>(A, 0);
