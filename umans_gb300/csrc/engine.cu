@@ -1440,9 +1440,11 @@ __device__ __forceinline__ float rng_uniform(uint32_t x, float a, float b)
 
 // CostFunction::ApproximateGlobalMinimumBySampling: costFunction.cpp:66-164.
 // Samples are spread over lanes; the argmin keeps the first strict minimum.
-// samples of the Karamouzas window swept together (independent chains)
+// Samples of the Karamouzas window swept together (independent chains).
+// Measured on a 100k-agent corridor (k_agent<3>, ms per step):
+// 2: 17.9, 3: 17.3, 4: 16.8, 5: 17.1, 6: 17.2, 8: 20.5, 10: 23.5.
 #ifndef UMANS_KS
-#define UMANS_KS 6
+#define UMANS_KS 4
 #endif
 constexpr int KS = UMANS_KS;
 
