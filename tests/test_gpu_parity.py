@@ -20,7 +20,7 @@ from test_oracle_golden import assert_same_list
 from umans_gb300 import Simulation, scenarios as S
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-4   # m over the first 100 steps (spec bound)
+TOL = 1e-4   # m over the first 100 steps (the parity bound)
 THREADS = os.cpu_count() or 4
 
 

@@ -2,7 +2,7 @@
 
 The fixtures were produced by the reference engine compiled from its own
 sources (tests/golden/make_golden.py).  The port must reproduce them: the
-spec bound is 1e-4 m over the first 100 steps; on these scenarios the
+bound is 1e-4 m over the first 100 steps; on these scenarios the
 port is in fact bit-identical on the machine that made the fixtures.
 """
 import numpy as np
