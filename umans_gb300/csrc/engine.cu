@@ -51,7 +51,7 @@ struct DevState {
 	uint32_t* rng;
 	float2 *sP, *sV;
 	float4* sB;
-	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces)
+	float4* sE;          // cell order: normalised preferred velocity, speed (SocialForces), radius
 	int *sSlot, *sId;
 	int *cell, *cnt, *start, *blocksum;   // cnt: per-cell histogram, zero between steps
 	unsigned* ticket;       // blocks of k_count_scan done (zero between launches)
@@ -522,7 +522,7 @@ __device__ __forceinline__ void scatter_one(const DevState& S, int i)
 	// same values
 	const float2 v = S.vel[i];
 	const float2 eb = vnorm(pv);
-	S.sE[t] = make_float4(eb.x, eb.y, vmag(v), 0.0f);
+	S.sE[t] = make_float4(eb.x, eb.y, vmag(v), prm.x);   // w: the radius, for the force pass's single load
 	S.sSlot[t] = i;
 	S.sId[t] = S.id[i];
 }
@@ -2403,10 +2403,11 @@ __device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists&
 			const uint32_t rr = L.ref[k];
 			const int j = (int)(rr & 0x0FFFFFFFu);
 			const float2 np = vadd(S.sP[j], group_offset(rr >> 28, W, H));
-			const float nr = S.sB[j].z;
+			const float4 E = S.sE[j];   // (normalised preferred velocity, speed, radius)
+			const float nr = E.w;
 			const float d2 = L.key[k];
 			float2 f = V(0, 0);
-			if (d2 <= rs) f = sf ? sf_force(A, SK, np, S.sE[j], nr) : pl_force(A, *c, np, S.sV[j], nr);
+			if (d2 <= rs) f = sf ? sf_force(A, SK, np, E, nr) : pl_force(A, *c, np, S.sV[j], nr);
 			L.key[k] = f.x;
 			L.ref[k] = __float_as_uint(f.y);
 			if (contact_scale > 0) {
