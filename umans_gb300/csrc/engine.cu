@@ -2386,11 +2386,13 @@ __device__ int q_gather(const DevState& S, const GridParams& G, int cb, int worl
 // velocity); contact_scale 0: no contact forces.  Returns the cost's force
 // (agents, then the (0, 0) of the absent obstacles), on all of the agent's
 // lanes.
+// SF: every neighbour cost of the launch is SocialForces (PowerLaw's code left out)
+template <bool SF = false>
 __device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists& L, int K, const CostDesc* c,
                           float contact_scale, float W, float H, const QLane& q, float2* contact)
 {
 	const float rs = c ? c->range * c->range : -1.0f;
-	const bool sf = c && c->kind == K_SOCIALFORCES;
+	const bool sf = SF || (c && c->kind == K_SOCIALFORCES);
 	SfConst SK = {};
 	if (c) SK = sf_const(A, *c);
 	float2 cacc = V(0, 0);
@@ -2407,7 +2409,10 @@ __device__ float2 q_force(const DevState& S, const AgentCtx& A, const WarpLists&
 			const float nr = E.w;
 			const float d2 = L.key[k];
 			float2 f = V(0, 0);
-			if (d2 <= rs) f = sf ? sf_force(A, SK, np, E, nr) : pl_force(A, *c, np, S.sV[j], nr);
+			if (d2 <= rs) {
+				if (SF || sf) f = sf_force(A, SK, np, E, nr);
+				else if constexpr (!SF) f = pl_force(A, *c, np, S.sV[j], nr);
+			}
 			L.key[k] = f.x;
 			L.ref[k] = __float_as_uint(f.y);
 			if (contact_scale > 0) {
@@ -2459,7 +2464,7 @@ __host__ __device__ constexpr size_t q_words(int maxnb) { return 2 * (size_t)max
 // One group of four agents (qi: its index in the launch's range) of
 // k_force_quad: the gather, the force pass, the agents' records; every 32
 // records, the per-agent remainder.
-template <bool TAPE, bool SAMP>
+template <bool TAPE, bool SAMP, bool SF>
 __device__ __forceinline__ void quad_step(const DevState& S, const QLane& q, const WarpLists& L, float* stash,
                                           int lane, int qi, int& nb, bool& overflow)
 {
@@ -2498,7 +2503,7 @@ __device__ __forceinline__ void quad_step(const DevState& S, const QLane& q, con
 		if (pol.cost[k].kind != K_GOALREACHING) ci = k;
 	const CostDesc* cd = (valid && ci >= 0 && !viszero(A.pref)) ? &pol.cost[ci] : nullptr;
 	float2 contact;
-	const float2 f = q_force(S, A, L, K, cd, valid ? pol.contact_scale : 0.0f, W, H, q, &contact);
+	const float2 f = q_force<SF>(S, A, L, K, cd, valid ? pol.contact_scale : 0.0f, W, H, q, &contact);
 	if (valid && q.sl == 0) {
 		float* rec = stash + (nb + q.sg) * STASH_STRIDE;
 		rec[0] = __int_as_float(t);
@@ -2516,8 +2521,9 @@ __device__ __forceinline__ void quad_step(const DevState& S, const QLane& q, con
 }
 
 // WL: compiled for the work-list schedule (schedule 2), which it then
-// requires; the other schedules use the variant without it.
-template <bool TAPE, bool SAMP = false, bool WL = false>
+// requires; the other schedules use the variant without it.  SF: every
+// neighbour cost of the group is SocialForces.
+template <bool TAPE, bool SAMP = false, bool WL = false, bool SF = false>
 __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 {
 	extern __shared__ unsigned char smem[];
@@ -2539,12 +2545,12 @@ __global__ void __launch_bounds__(128, 8) k_force_quad(DevState S)
 	if constexpr (WL) {
 		WorkIter w;
 		for (int qi = work_first<32 / QN>(S, w, nq, gw, lane); qi >= 0; qi = work_after<32 / QN>(S, w, qi, lane, nq))
-			quad_step<TAPE, SAMP>(S, q, L, stash, lane, qi, nb, overflow);
+			quad_step<TAPE, SAMP, SF>(S, q, L, stash, lane, qi, nb, overflow);
 	} else {
 		const int per = (nq + S.total_warps - 1) / S.total_warps;
 		const int q0 = S.sched ? gw * per : gw, qstride = S.sched ? 1 : S.total_warps;
 		const int qend = S.sched ? min(nq, q0 + per) : nq;
-		for (int qi = q0; qi < qend; qi += qstride) quad_step<TAPE, SAMP>(S, q, L, stash, lane, qi, nb, overflow);
+		for (int qi = q0; qi < qend; qi += qstride) quad_step<TAPE, SAMP, SF>(S, q, L, stash, lane, qi, nb, overflow);
 	}
 	if (nb > 0) {
 		__syncwarp();
@@ -3358,6 +3364,7 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 				for (int j = j0; j < g.j1; ++j) g.obst |= scen_[scen_order_[j]].nedges > 0;
 				g.quad_ok = g.mode == 1 && !g.obst;
 				g.samp = false;
+				g.sf_only = true;
 				for (size_t pi = 0; pi < pols_.size(); ++pi) {
 					bool in_group = false;
 					for (int j = j0; j < g.j1; ++j) in_group |= pol_scen_[pi] == scen_order_[j];
@@ -3365,6 +3372,10 @@ bool Engine::init(const std::vector<std::string>& xmls, const EngineOptions& opt
 					int nbc = 0;
 					for (int c2 = 0; c2 < pols_[pi].ncost; ++c2) nbc += pols_[pi].cost[c2].kind != K_GOALREACHING;
 					if (nbc > 1) g.quad_ok = false;
+					for (int c2 = 0; c2 < pols_[pi].ncost; ++c2) {
+						const int kd = pols_[pi].cost[c2].kind;
+						if (kd != K_GOALREACHING && kd != K_SOCIALFORCES) g.sf_only = false;
+					}
 					if (pols_[pi].method != M_GRADIENT) g.samp = true;
 				}
 				groups_.push_back(g);
@@ -3810,6 +3821,8 @@ bool Engine::configure()
 		CK(cudaFuncSetAttribute(k_force_quad<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 		CK(cudaFuncSetAttribute(k_force_quad<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 		CK(cudaFuncSetAttribute(k_force_quad<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
+		CK(cudaFuncSetAttribute(k_force_quad<false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemq));
 	}
 	if (smem0 > 48 * 1024) {
 		CK(cudaFuncSetAttribute(k_agent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0));
@@ -3902,6 +3915,9 @@ void Engine::enqueue_step()
 			} else if (g.samp) {
 				if (wl) k_force_quad<false, true, true><<<blocks, wpb * 32, smemq, st>>>(A);
 				else k_force_quad<false, true><<<blocks, wpb * 32, smemq, st>>>(A);
+			} else if (g.sf_only) {
+				if (wl) k_force_quad<false, false, true, true><<<blocks, wpb * 32, smemq, st>>>(A);
+				else k_force_quad<false, false, false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			} else if (wl) k_force_quad<false, false, true><<<blocks, wpb * 32, smemq, st>>>(A);
 			else k_force_quad<false><<<blocks, wpb * 32, smemq, st>>>(A);
 		} else if (g.mode == 2) {   // taped runs have no ORCA policy (diff_begin checks)

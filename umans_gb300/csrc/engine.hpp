@@ -226,6 +226,7 @@ private:
 		bool quad_ok = false;   // k_force_quad allowed: force-only, no obstacle edges, <= 1 neighbour cost per policy
 		bool quad = false;      // k_force_quad chosen (quad_ok and EngineOptions::agent_lanes == 8)
 		bool samp = false;   // a force-only group with a policy of the sampling or global method
+		bool sf_only = false;   // every neighbour cost of the group is SocialForces
 	};
 	std::vector<KGroup> groups_;
 	std::vector<int> scen_order_;
