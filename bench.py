@@ -338,11 +338,16 @@ def diff_leg(tmp: str, sets: int = 256, n: int = 512, steps: int = 100, every: i
 
 
 def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: int = 0,
-               cpu_seconds: float = 10.0) -> dict:
+               cpu_seconds: float = 10.0, whole_run: bool = False) -> dict:
     """Another configuration of the reference's benchmark list, timed like the
     headline (per-step CUDA events, L2 flushed before each step), with the
     reference CPU step beside it (on the full case, or on a smaller case at
-    the same density when the full one would take minutes per step)."""
+    the same density when the full one would take minutes per step).
+
+    whole_run: the configuration's whole run (`steps` steps from the initial
+    state) is also timed as one call, the way the reference's
+    RunSimulationSteps runs it; small worlds then step inside one launch.
+    That figure becomes the leg's value, the per-step one is kept beside it."""
     import torch
     from umans_gb300 import Simulation
     sub = os.path.join(tmp, name)
@@ -390,6 +395,31 @@ def config_leg(name: str, tmp: str, steps: int, warmup: int, flush, cpu_agents: 
                            l2="flushed (256 MiB write) before every timed step"),
                value=n * steps / (t_ms / 1e3), unit="agent-steps/s", steps=steps, warmup=warmup,
                ms_per_step=t_ms / steps)
+    if whole_run:
+        runs = []
+        for k in range(warmup + 1):   # the first runs warm up, the last is timed
+            sim = Simulation(path)
+            stream = torch.cuda.ExternalStream(sim.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+                e0.record(stream)
+            sim.step_async(steps)
+            e1.record(stream)
+            sim.synchronize()
+            torch.cuda.synchronize()
+            runs.append(e0.elapsed_time(e1))
+            launches = sim.profile_totals()["kernels_per_step"]
+            sim.close()
+        w_ms = runs[-1]
+        out["one_step_per_call"] = dict(value=out["value"], ms_per_step=out["ms_per_step"],
+                                        timed_steps=out["config"]["timed_steps"])
+        out["value"] = n * steps / (w_ms / 1e3)
+        out["ms_per_step"] = w_ms / steps
+        out["config"]["timed_steps"] = f"the whole run, steps 1..{steps}, as one call ({warmup} untimed runs before)"
+        out["config"]["l2"] = "flushed (256 MiB write) before the timed run"
+        out["whole_run"] = dict(ms=w_ms, launches_per_call=launches if launches == 1 else launches * steps)
     if work:
         out["fp32_roofline"] = work
     t_gpu = time.perf_counter() - t0 - t_write - t_load
@@ -684,7 +714,7 @@ def run_ours(args):
         extra = None
         if not args.no_extra and world == 1:
             extra = {"small_orca_circle": config_leg("circle_orca", tmp, 300, args.warmup, flush,
-                                                     cpu_agents=0 if not args.no_cpu else -1),
+                                                     cpu_agents=0 if not args.no_cpu else -1, whole_run=True),
                      "sampling_heavy_karamouzas": config_leg("karamouzas_corridor", tmp, 5, 3, flush,
                                                              cpu_agents=20_000 if not args.no_cpu else -1)}
         lap("other_configs")

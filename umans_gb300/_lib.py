@@ -41,6 +41,7 @@ _SIGS = {
     "umans_autotune": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_float),
                                  C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "umans_set_launch": (C.c_int, [P, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int]),
+    "umans_set_multi_step": (C.c_int, [P, C.c_int]),
     "umans_step": (C.c_int, [P, C.c_int]),
     "umans_step_async": (C.c_int, [P, C.c_int]),
     "umans_synchronize": (C.c_int, [P]),

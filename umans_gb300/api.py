@@ -123,6 +123,11 @@ class Simulation:
         self._check(self._lib.umans_set_launch(self._h, float(cells_per_range), int(warps_per_block),
                                                float(occupancy), int(schedule), int(agent_lanes)))
 
+    def set_multi_step(self, enable: bool = True):
+        """Small worlds: the steps of one call in one launch (the default), or
+        one graph launch per step; results do not depend on it."""
+        self._check(self._lib.umans_set_multi_step(self._h, int(bool(enable))))
+
     def profile(self, enable: bool = True):
         self._check(self._lib.umans_profile(self._h, int(bool(enable))))
 

@@ -25,8 +25,8 @@ namespace umans {
 // (the general sampler compiled out: 21% faster than MODE 0 on a 100k-agent
 // corridor at the same 128 registers; at 96 registers it spilled and was
 // slower).
-template <int MODE, bool TAPE = false, bool OBST = true, bool SAMP = false>
-__global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_agent(DevState S, int dump)
+template <int MODE, bool TAPE, bool OBST, bool SAMP>
+__device__ __forceinline__ void agent_pass(const DevState& S, int dump)
 {
 	extern __shared__ unsigned char smem[];
 	const int lane = threadIdx.x & 31;
@@ -239,6 +239,37 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_ag
 	}
 	work_end(S, lane);
 	if (overflow && lane == 0) atomicOr(S.status, ST_NEIGHBOUR_OVERFLOW);
+}
+
+template <int MODE, bool TAPE = false, bool OBST = true, bool SAMP = false>
+__global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_agent(DevState S, int dump)
+{
+	agent_pass<MODE, TAPE, OBST, SAMP>(S, dump);
+}
+
+// Small worlds (the range of build_small), several steps in one cooperative
+// launch, so that a step costs no launch: block 0 builds the step's grid
+// (build_small) while the other blocks wait at a grid barrier, then every
+// block updates its agents (one warp per agent where the launch has the
+// warps) and a second grid barrier ends the step.  S describes the launch as
+// the agent pass's only one (t_begin 0, t_end n, total_warps the launch's
+// warps, the interleaved schedule).  The fences of the grid barrier order the
+// build's writes before every block's reads, and each step's agent writes
+// before the next build.  After a step that set a status bit every block
+// leaves the loop (all read the status after the same barrier): the host
+// reports it, or re-runs the steps from its snapshot with a longer
+// neighbour capacity.
+constexpr int SMALL_STEPS_MAX_THREADS = 256;
+template <int MODE>
+__global__ void __launch_bounds__(SMALL_STEPS_MAX_THREADS, MODE == 2 ? 4 : 2) k_small_steps(DevState S, int nsteps)
+{
+	for (int s = 0; s < nsteps; ++s) {
+		if (blockIdx.x == 0) build_small(S);
+		grid_barrier(S);
+		agent_pass<MODE, false, true, false>(S, 0);
+		grid_barrier(S);
+		if (__ldcg(S.status) != 0) break;
+	}
 }
 
 }  // namespace umans

@@ -138,6 +138,13 @@ int umans_set_launch(umans_sim* s, float cells_per_range, int warps_per_block, f
 	return UMANS_OK;
 }
 
+int umans_set_multi_step(umans_sim* s, int enable)
+{
+	if (!s) return UMANS_ERR_ARGUMENT;
+	if (!s->eng->set_multi_step(enable != 0)) return fail(s, UMANS_ERR_CUDA, s->eng->error());
+	return UMANS_OK;
+}
+
 int umans_autotune(umans_sim* s, int trial_steps, float* cells_per_range, int* warps_per_block, float* occupancy,
                    int* schedule, int* agent_lanes)
 {

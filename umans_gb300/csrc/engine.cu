@@ -790,6 +790,7 @@ bool Engine::configure()
 	// work-list counters: a pair per kernel group, and one for the list dump
 	if (!dalloc(S.work, 2 * (groups_.size() + 1), err_)) return false;
 	CK(cudaMemset(S.work, 0, sizeof(unsigned) * 2 * (groups_.size() + 1)));
+	if (!small_steps_occupancy()) return false;
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
 	return true;
@@ -997,8 +998,102 @@ bool Engine::profile_counters(unsigned long long* out, int n)
 	return true;
 }
 
+static constexpr size_t SMALL_STEPS_SMEM = 200 * 1024;   // dynamic shared memory per block, at most
+
+// k_small_steps takes a small world whose one kernel group runs k_agent
+// (modes 0, 2, 3) and whose steps need no host work in between (no
+// trajectory output, profiling or tape).  Blocks of 4 warps (8 above 512
+// agents), as many as give every agent its own warp, at most as many as are
+// resident at once and as the line scratch covers; 0 blocks when the steps
+// of a call cannot run in one launch.
+void Engine::small_steps_shape(int* blocks, int* threads) const
+{
+	*blocks = 0;
+	*threads = 0;
+	if (!opt_.multi_step || profile_ || n_ < 1 || !small_world() || groups_.size() != 1 || d_->tape_list) return;
+	const KGroup& g = groups_[0];
+	if (g.quad || g.mode == 1) return;
+	const int m = g.mode == 2 ? 2 : (g.mode == 3 ? 3 : 0);
+	const int wpb = n_ <= 512 ? 4 : 8;
+	const size_t smem = agent_smem(wpb, maxnb_, g.mode);
+	if (smem > SMALL_STEPS_SMEM) return;
+	const int resident = small_steps_resident_[m][wpb == 4 ? 0 : 1];
+	if (resident < 1) return;
+	int nb = (n_ + wpb - 1) / wpb;
+	nb = std::min(nb, resident * num_sms_);
+	nb = (int)std::min<long long>(nb, (long long)g.blocks * opt_.warps_per_block / wpb);   // line scratch
+	if (nb < 1) return;
+	*blocks = nb;
+	*threads = wpb * 32;
+}
+
+bool Engine::launch_small_steps(int nsteps, int blocks, int threads)
+{
+	const KGroup& g = groups_[0];
+	DevState S = *d_;
+	S.n = n_;
+	S.maxnb = maxnb_;
+	S.counters = nullptr;
+	S.t_begin = 0;
+	S.t_end = n_;
+	S.total_warps = blocks * threads / 32;
+	S.sched = 0;
+	S.scratch = d_->scratch + g.scratch_off;
+	S.obs_list = d_->obs_list + g.obs_off;
+	const size_t smem = agent_smem(threads / 32, maxnb_, g.mode);
+	const int m = g.mode == 2 ? 2 : (g.mode == 3 ? 3 : 0);
+	void (*fn)(DevState, int) = m == 2 ? k_small_steps<2> : (m == 3 ? k_small_steps<3> : k_small_steps<0>);
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3((unsigned)blocks);
+	cfg.blockDim = dim3((unsigned)threads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream_;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeCooperative;
+	attr[0].val.cooperative = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	CK(cudaLaunchKernelEx(&cfg, fn, S, nsteps));
+	return true;
+}
+
+// Blocks of k_small_steps resident per SM for the current neighbour
+// capacity (by mode, 4 and 8 warps per block); configure() refreshes them.
+bool Engine::small_steps_occupancy()
+{
+	const int modes[3] = {0, 2, 3};
+	for (int m : modes) {
+		void (*fn)(DevState, int) = m == 2 ? k_small_steps<2> : (m == 3 ? k_small_steps<3> : k_small_steps<0>);
+		// the kernel's static shared memory (build_small's scan) counts
+		// against the 48 KB default too: allow the whole budget
+		CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMALL_STEPS_SMEM));
+		for (int k = 0; k < 2; ++k) {
+			const int wpb = k == 0 ? 4 : 8;
+			int per_sm = 0;
+			const size_t smem = agent_smem(wpb, maxnb_, m);
+			if (smem > SMALL_STEPS_SMEM ||
+			    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess) {
+				cudaGetLastError();
+				per_sm = 0;
+			}
+			small_steps_resident_[m][k] = per_sm;
+		}
+	}
+	return true;
+}
+
+bool Engine::set_multi_step(bool on)
+{
+	if (!sync()) return false;
+	opt_.multi_step = on;
+	return true;
+}
+
 int Engine::kernels_per_step() const
 {
+	int sblocks = 0, sthreads = 0;
+	small_steps_shape(&sblocks, &sthreads);
+	if (sblocks > 0) return 1;
 	if (small_world()) return 1 + (int)groups_.size();
 	const bool grid_fixed = toric_only_ && static_grid_ready_;
 	const int cells_bound = grid_fixed ? static_cells_ : d_->max_cells;
@@ -1172,6 +1267,16 @@ bool Engine::run_steps(int nsteps, bool record)
 	if (!ensure_static_grid()) return false;
 	steps_pending_ = true;
 	record = record && !recs_.empty();
+	int sblocks = 0, sthreads = 0;
+	if (!record) small_steps_shape(&sblocks, &sthreads);
+	if (sblocks > 0) {
+		if (!launch_small_steps(nsteps, sblocks, sthreads)) return false;
+		for (int s = 0; s < nsteps; ++s) {
+			time_ += sc_.dt;
+			for (size_t k = 0; k < times_.size(); ++k) times_[k] += scen_[k].dt;
+		}
+		return true;
+	}
 	if (record && n_ > rec_cap_n_) {
 		// the population grew since the ring was sized (it was flushed then)
 		CK(cudaStreamSynchronize(stream_));

@@ -36,6 +36,7 @@ struct EngineOptions {
 	int schedule = 0;         // agents to warps: 0 interleaved, 1 contiguous blocks, 2 work list of agent tiles
 	int agent_lanes = 8;      // lanes per agent in the force-only groups that allow 8 (else 32)
 	bool use_graph = true;
+	bool multi_step = true;   // small worlds: the steps of one call in one launch (k_small_steps)
 };
 
 class Engine {
@@ -83,6 +84,9 @@ public:
 	bool autotune(int trial_steps, EngineOptions* chosen);
 	// applies a launch shape (the fields autotune chooses); results do not depend on it
 	bool set_launch(const EngineOptions& o);
+	// small worlds: every step of a call in one launch (on by default), or
+	// one graph launch per step; results do not depend on it
+	bool set_multi_step(bool on);
 	const EngineOptions& options() const { return opt_; }
 
 	// device pointers of the raw state for callers that keep data on the GPU
@@ -103,6 +107,9 @@ public:
 	{ *agent_ms = prof_agent_ms_; *step_ms = prof_step_ms_; *steps = prof_steps_; *grid_ms = prof_grid_ms_; }
 	int kernels_per_step() const;
 	bool small_world() const;   // one-block grid build (k_build_small)
+	// launch shape of k_small_steps for the current state (0 blocks when the
+	// steps of a call cannot run in one launch)
+	void small_steps_shape(int* blocks, int* threads) const;
 
 	// ---- differentiable form ------------------------------------------
 	// Episode: `steps` steps from the current state (recorded as the
@@ -151,6 +158,9 @@ private:
 	bool ensure_static_grid();
 	cudaError_t launch_grid_coop(const DevState& S);
 	void probe_grid_coop();
+	bool launch_small_steps(int nsteps, int blocks, int threads);
+	bool small_steps_occupancy();
+	int small_steps_resident_[4][2] = {};   // per mode: blocks per SM at 4 and 8 warps per block
 	int coop_state_ = 0;        // one-launch grid build: 0 untried, 1 usable, -1 not capturable
 	int coop_blocks_max_ = 1;
 	bool toric_only_ = false;          // every scenario's world is toric: the grid is fixed

@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(1024) k_grid_coop(DevState S)
 // one launch instead of seven, for worlds whose steps are launch-bound.
 // Values written by atomics in one phase are read through L2 (__ldcg).
 constexpr int SMALL_MAX_AGENTS = 4096, SMALL_MAX_CELLS = 32768;
-__global__ void __launch_bounds__(1024) k_build_small(DevState S)
+__device__ __forceinline__ void build_small(const DevState& S)
 {
 	const int n = S.n, tid = threadIdx.x, nt = blockDim.x;
 	for (int i = tid; i < n; i += nt) bbox_one(S, i);
@@ -573,6 +573,10 @@ __global__ void __launch_bounds__(1024) k_build_small(DevState S)
 	if (tid == 0) S.start[nc] = n;
 	__syncthreads();
 	for (int i = tid; i < n; i += nt) scatter_one(S, i);
+}
+__global__ void __launch_bounds__(1024) k_build_small(DevState S)
+{
+	build_small(S);
 }
 
 }  // namespace umans
