@@ -25,7 +25,10 @@ namespace umans {
 // (the general sampler compiled out: 21% faster than MODE 0 on a 100k-agent
 // corridor at the same 128 registers; at 96 registers it spilled and was
 // slower).
-template <int MODE, bool TAPE, bool OBST, bool SAMP>
+// SMEM_LINES: the ORCA lines and their projections (the Karamouzas
+// sampler's scratch) in shared memory after the lists, 16-byte aligned,
+// instead of the global line scratch
+template <int MODE, bool TAPE, bool OBST, bool SAMP, bool SMEM_LINES = false>
 __device__ __forceinline__ void agent_pass(const DevState& S, int dump)
 {
 	extern __shared__ unsigned char smem[];
@@ -45,7 +48,13 @@ __device__ __forceinline__ void agent_pass(const DevState& S, int dump)
 	}
 	float* fx = reinterpret_cast<float*>(L.nid);   // per-neighbour terms
 	float* fy = L.aux;
-	float4* lines = S.scratch + (size_t)gw * 2 * maxnb;
+	float4* lines;
+	if constexpr (SMEM_LINES) {
+		const uintptr_t l0 = reinterpret_cast<uintptr_t>(smem + (size_t)(blockDim.x >> 5) * 16 * maxnb);
+		lines = reinterpret_cast<float4*>((l0 + 15) & ~(uintptr_t)15) + (size_t)wib * 2 * maxnb;
+	} else {
+		lines = S.scratch + (size_t)gw * 2 * maxnb;
+	}
 	float4* proj = lines + maxnb;
 
 	WorkIter w;
@@ -249,9 +258,10 @@ __global__ void __launch_bounds__(128, MODE == 1 ? 8 : (MODE == 2 ? 8 : 4)) k_ag
 
 // Small worlds (the range of build_small), several steps in one cooperative
 // launch, so that a step costs no launch: block 0 builds the step's grid
-// (build_small) while the other blocks wait at a grid barrier, then every
+// (build_small_smem) while the other blocks wait at a grid barrier, then every
 // block updates its agents (one warp per agent where the launch has the
-// warps) and a second grid barrier ends the step.  S describes the launch as
+// warps, the ORCA lines in shared memory) and a second grid barrier ends
+// the step.  S describes the launch as
 // the agent pass's only one (t_begin 0, t_end n, total_warps the launch's
 // warps, the interleaved schedule).  The fences of the grid barrier order the
 // build's writes before every block's reads, and each step's agent writes
@@ -263,10 +273,11 @@ constexpr int SMALL_STEPS_MAX_THREADS = 256;
 template <int MODE>
 __global__ void __launch_bounds__(SMALL_STEPS_MAX_THREADS, MODE == 2 ? 4 : 2) k_small_steps(DevState S, int nsteps)
 {
+	__shared__ SmallGrid B;
 	for (int s = 0; s < nsteps; ++s) {
-		if (blockIdx.x == 0) build_small(S);
+		if (blockIdx.x == 0) build_small_smem(S, B);
 		grid_barrier(S);
-		agent_pass<MODE, false, true, false>(S, 0);
+		agent_pass<MODE, false, true, false, true>(S, 0);
 		grid_barrier(S);
 		if (__ldcg(S.status) != 0) break;
 	}

@@ -998,7 +998,13 @@ bool Engine::profile_counters(unsigned long long* out, int n)
 	return true;
 }
 
-static constexpr size_t SMALL_STEPS_SMEM = 200 * 1024;   // dynamic shared memory per block, at most
+// k_small_steps: the lists, then (16-byte aligned) 2 * maxnb float4 of
+// lines per warp
+static size_t small_steps_smem(int warps_per_block, int maxnb, int mode)
+{
+	return agent_smem(warps_per_block, maxnb, mode) + (size_t)warps_per_block * 2 * maxnb * sizeof(float4) + 16;
+}
+static constexpr size_t SMALL_STEPS_SMEM = 160 * 1024;   // dynamic shared memory per block, at most (with the static 33 KB, below the 227 KB limit)
 
 // k_small_steps takes a small world whose one kernel group runs k_agent
 // (modes 0, 2, 3) and whose steps need no host work in between (no
@@ -1015,7 +1021,7 @@ void Engine::small_steps_shape(int* blocks, int* threads) const
 	if (g.quad || g.mode == 1) return;
 	const int m = g.mode == 2 ? 2 : (g.mode == 3 ? 3 : 0);
 	const int wpb = n_ <= 512 ? 4 : 8;
-	const size_t smem = agent_smem(wpb, maxnb_, g.mode);
+	const size_t smem = small_steps_smem(wpb, maxnb_, g.mode);
 	if (smem > SMALL_STEPS_SMEM) return;
 	const int resident = small_steps_resident_[m][wpb == 4 ? 0 : 1];
 	if (resident < 1) return;
@@ -1040,7 +1046,7 @@ bool Engine::launch_small_steps(int nsteps, int blocks, int threads)
 	S.sched = 0;
 	S.scratch = d_->scratch + g.scratch_off;
 	S.obs_list = d_->obs_list + g.obs_off;
-	const size_t smem = agent_smem(threads / 32, maxnb_, g.mode);
+	const size_t smem = small_steps_smem(threads / 32, maxnb_, g.mode);
 	const int m = g.mode == 2 ? 2 : (g.mode == 3 ? 3 : 0);
 	void (*fn)(DevState, int) = m == 2 ? k_small_steps<2> : (m == 3 ? k_small_steps<3> : k_small_steps<0>);
 	cudaLaunchConfig_t cfg = {};
@@ -1070,7 +1076,7 @@ bool Engine::small_steps_occupancy()
 		for (int k = 0; k < 2; ++k) {
 			const int wpb = k == 0 ? 4 : 8;
 			int per_sm = 0;
-			const size_t smem = agent_smem(wpb, maxnb_, m);
+			const size_t smem = small_steps_smem(wpb, maxnb_, m);
 			if (smem > SMALL_STEPS_SMEM ||
 			    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess) {
 				cudaGetLastError();

@@ -41,6 +41,26 @@ __global__ void k_bbox(DevState S)
 	if (i < S.n) bbox_one(S, i);
 }
 
+// grid over the box (x0, y0) + (ex, ey): the cell size range /
+// cells_per_range, doubled until the grid has at most max_cells cells
+__device__ __forceinline__ GridParams grid_of_box(const DevState& S, const ScenDesc& sd, float x0, float y0, float ex,
+                                                  float ey, int max_cells)
+{
+	if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
+		atomicOr(S.status, ST_GRID_OVERFLOW);
+		x0 = y0 = 0; ex = ey = 1;
+	}
+	float cs = sd.max_range / S.cells_per_range;
+	if (!(cs >= 1e-3f)) cs = 1e-3f;
+	// +2 per axis: nx, ny below come from float divisions that may round up
+	while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)max_cells) cs *= 2.0f;
+	GridParams g;
+	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
+	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
+	g.ncells = g.nx * g.ny; g.pad = 0;
+	return g;
+}
+
 // grid of scenario s (origin, cell size, counts) from its bounding box, which
 // is reset for the next step; returns the scenario's cell count
 __device__ int grid_params(const DevState& S, int s)
@@ -57,18 +77,7 @@ __device__ int grid_params(const DevState& S, int s)
 	}
 	B[0] = B[1] = f2o(FLT_MAX);
 	B[2] = B[3] = f2o(-FLT_MAX);
-	if (!isfinite(x0) || !isfinite(y0) || !isfinite(ex) || !isfinite(ey)) {
-		atomicOr(S.status, ST_GRID_OVERFLOW);
-		x0 = y0 = 0; ex = ey = 1;
-	}
-	float cs = sd.max_range / S.cells_per_range;
-	if (!(cs >= 1e-3f)) cs = 1e-3f;
-	// +2 per axis: nx, ny below come from float divisions that may round up
-	while (((double)ex / cs + 2.0) * ((double)ey / cs + 2.0) > (double)sd.max_cells) cs *= 2.0f;
-	GridParams g;
-	g.x0 = x0; g.y0 = y0; g.cs = cs; g.inv_cs = 1.0f / cs;
-	g.nx = (int)(ex / cs) + 1; g.ny = (int)(ey / cs) + 1;
-	g.ncells = g.nx * g.ny; g.pad = 0;
+	const GridParams g = grid_of_box(S, sd, x0, y0, ex, ey, sd.max_cells);
 	S.grid[s] = g;
 	return g.ncells;
 }
@@ -400,20 +409,10 @@ __global__ void __launch_bounds__(1024) k_scan_single(DevState S)
 	if (threadIdx.x == 0) S.start[nc] = S.n;
 }
 
-__device__ __forceinline__ void scatter_one(const DevState& S, int i)
+// the cell-sorted copies of agent i (position p) at index t, with its
+// preferred velocity
+__device__ __forceinline__ void scatter_to(const DevState& S, int i, int t, float2 p)
 {
-	const int c = S.cell[i];
-	const unsigned act = __activemask();
-	const unsigned peers = __match_any_sync(act, c);
-	const int lane = threadIdx.x & 31;
-	const int leader = __ffs(peers) - 1;
-	// the cell is filled from its top down: the histogram count is taken back
-	// by each agent placed, so it is all-zero again for the next step
-	int top = 0;
-	if (lane == leader) top = atomicSub(&S.cnt[c], __popc(peers));
-	top = __shfl_sync(peers, top, leader);
-	const int t = __ldcg(S.start + c) + top - __popc(peers) + __popc(peers & ((1u << lane) - 1u));
-	const float2 p = S.pos[i];
 	const float2 g = S.goal[i];
 	const float4 prm = S.prm[i];
 	// Agent::ComputePreferredVelocity / hasReachedGoal: agent.cpp:52-59, 99-102
@@ -433,6 +432,22 @@ __device__ __forceinline__ void scatter_one(const DevState& S, int i)
 	S.sE[t] = make_float4(eb.x, eb.y, vmag(v), prm.x);   // w: the radius, for the force pass's single load
 	S.sSlot[t] = i;
 	S.sId[t] = S.id[i];
+}
+
+__device__ __forceinline__ void scatter_one(const DevState& S, int i)
+{
+	const int c = S.cell[i];
+	const unsigned act = __activemask();
+	const unsigned peers = __match_any_sync(act, c);
+	const int lane = threadIdx.x & 31;
+	const int leader = __ffs(peers) - 1;
+	// the cell is filled from its top down: the histogram count is taken back
+	// by each agent placed, so it is all-zero again for the next step
+	int top = 0;
+	if (lane == leader) top = atomicSub(&S.cnt[c], __popc(peers));
+	top = __shfl_sync(peers, top, leader);
+	const int t = __ldcg(S.start + c) + top - __popc(peers) + __popc(peers & ((1u << lane) - 1u));
+	scatter_to(S, i, t, S.pos[i]);
 }
 __global__ void k_scatter(DevState S)
 {
@@ -577,6 +592,106 @@ __device__ __forceinline__ void build_small(const DevState& S)
 __global__ void __launch_bounds__(1024) k_build_small(DevState S)
 {
 	build_small(S);
+}
+
+// build_small for k_small_steps, with the bounding box, the histogram and
+// the scan in shared memory: global memory only gives the agents' state and
+// takes the cell-sorted copies, the cell starts and the grid parameters.
+// The grid has at most SMALL_SMEM_CELLS cells (the cell size is doubled
+// until it fits, as for any cell cap; no neighbour list depends on it).
+constexpr int SMALL_SMEM_CELLS = 4096;
+struct SmallGrid {
+	int cnt[SMALL_SMEM_CELLS];
+	int start[SMALL_SMEM_CELLS + 1];
+	unsigned box[4];
+	int tot[32];
+	GridParams g;
+};
+__device__ __forceinline__ void build_small_smem(const DevState& S, SmallGrid& B)
+{
+	const int n = S.n, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+	const ScenDesc& sd = S.scen[0];
+	const int world = sd.world;
+	if (world != W_TORIC) {
+		unsigned a = f2o(FLT_MAX), b = a, c = f2o(-FLT_MAX), d = c;
+		for (int i = tid; i < n; i += nt) {
+			const float2 p = S.pos[i];
+			a = min(a, f2o(p.x)); b = min(b, f2o(p.y));
+			c = max(c, f2o(p.x)); d = max(d, f2o(p.y));
+		}
+		a = __reduce_min_sync(0xffffffffu, a); b = __reduce_min_sync(0xffffffffu, b);
+		c = __reduce_max_sync(0xffffffffu, c); d = __reduce_max_sync(0xffffffffu, d);
+		if (tid < 4) B.box[tid] = tid < 2 ? f2o(FLT_MAX) : f2o(-FLT_MAX);
+		__syncthreads();
+		if (lane == 0) {
+			atomicMin(&B.box[0], a); atomicMin(&B.box[1], b);
+			atomicMax(&B.box[2], c); atomicMax(&B.box[3], d);
+		}
+		__syncthreads();
+	}
+	if (tid == 0) {
+		// the box as grid_params takes it
+		float x0, y0, ex, ey;
+		if (world == W_TORIC) {
+			x0 = -0.5f * sd.width; y0 = -0.5f * sd.height; ex = sd.width; ey = sd.height;
+		} else {
+			x0 = o2f(B.box[0]); y0 = o2f(B.box[1]);
+			ex = o2f(B.box[2]) - x0; ey = o2f(B.box[3]) - y0;
+			if (sd.n == 0) { x0 = y0 = 0; ex = ey = 1; }
+		}
+		const GridParams g = grid_of_box(S, sd, x0, y0, ex, ey, min(sd.max_cells, SMALL_SMEM_CELLS));
+		S.grid[0] = g;
+		S.cell_base[0] = 0;
+		S.cell_base[1] = g.ncells;
+		B.g = g;
+	}
+	__syncthreads();
+	const GridParams g = B.g;
+	const int nc = g.ncells;
+	for (int c = tid; c < nc; c += nt) B.cnt[c] = 0;
+	__syncthreads();
+	for (int i = tid; i < n; i += nt) {
+		const float2 p = S.pos[i];
+		atomicAdd(&B.cnt[cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx)], 1);
+	}
+	__syncthreads();
+	// exclusive scan: a run of cells per thread, then the threads' sums
+	const int per = (nc + nt - 1) / nt;
+	const int c0 = min(nc, tid * per), c1 = min(nc, c0 + per);
+	int local = 0;
+	for (int c = c0; c < c1; ++c) local += B.cnt[c];
+	int incl = local;
+	for (int o = 1; o < 32; o <<= 1) {
+		const int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if (lane >= o) incl += v;
+	}
+	if (lane == 31) B.tot[wid] = incl;
+	__syncthreads();
+	if (wid == 0) {
+		const int v = lane < nw ? B.tot[lane] : 0;
+		int w = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(0xffffffffu, w, o);
+			if (lane >= o) w += u;
+		}
+		B.tot[lane] = w - v;
+	}
+	__syncthreads();
+	int run = B.tot[wid] + incl - local;
+	for (int c = c0; c < c1; ++c) {
+		B.start[c] = run;
+		S.start[c] = run;
+		run += B.cnt[c];
+	}
+	if (tid == 0) S.start[nc] = n;
+	__syncthreads();
+	// the scatter fills each cell from its top down
+	for (int i = tid; i < n; i += nt) {
+		const float2 p = S.pos[i];
+		const int c = cell_coord(p.y, g.y0, g.inv_cs, g.ny) * g.nx + cell_coord(p.x, g.x0, g.inv_cs, g.nx);
+		const int t = B.start[c] + atomicSub(&B.cnt[c], 1) - 1;
+		scatter_to(S, i, t, p);
+	}
 }
 
 }  // namespace umans
