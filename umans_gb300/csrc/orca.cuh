@@ -13,6 +13,18 @@ __device__ __forceinline__ float det2(float2 a, float2 b) { return a.x * b.y - a
 __device__ __forceinline__ float2 lp_point(float4 l) { return V(l.x, l.y); }
 __device__ __forceinline__ float2 lp_dir(float4 l) { return V(l.z, l.w); }
 
+// order-preserving unsigned keys of finite floats (for warp min / max by
+// redux.sync)
+__device__ __forceinline__ unsigned lp_key(float f)
+{
+	const unsigned u = __float_as_uint(f);
+	return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float lp_val(unsigned k)
+{
+	return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
 // linearProgram1 (ORCASolver.cpp:173-226), the warp splitting the earlier
 // lines.  tl only grows and tr only shrinks along the reference's loop, so
 // its early exits (a parallel line excluding the whole line, or tl > tr at
@@ -40,14 +52,11 @@ static __device__ bool lp1(const float4* L, int lineNo, float radius, float2 opt
 		if (den >= 0.0f) tr = fminr(tr, t);
 		else tl = fmaxr(tl, t);
 	}
-	for (int o = 16; o > 0; o >>= 1) {
-		tr = fminr(tr, __shfl_xor_sync(0xffffffffu, tr, o));
-		tl = fmaxr(tl, __shfl_xor_sync(0xffffffffu, tl, o));
-	}
-	// one representative for every lane (equal values may differ in the sign
-	// of zero between lanes)
-	tr = __shfl_sync(0xffffffffu, tr, 0);
-	tl = __shfl_sync(0xffffffffu, tl, 0);
+	// one warp reduction each, the same value on every lane (of equal values
+	// of different zero sign the minimum takes -0, the maximum +0; either is
+	// exact for the uses below)
+	tr = lp_val(__reduce_min_sync(0xffffffffu, lp_key(tr)));
+	tl = lp_val(__reduce_max_sync(0xffffffffu, lp_key(tl)));
 	if (__any_sync(0xffffffffu, bad) || tl > tr) return false;
 	if (dirOpt) {
 		if (vdot(opt, D) > 0.0f) *res = vadd(P, vmul(D, tr));
