@@ -123,11 +123,14 @@ int umans_autotune(umans_sim* sim, int trial_steps, float* cells_per_range, int*
  * 32).  Results do not depend on it.  UMANS_ERR_ARGUMENT when out of range. */
 int umans_set_launch(umans_sim* sim, float cells_per_range, int warps_per_block, float occupancy, int schedule,
                      int agent_lanes);
-/* Small worlds (one scenario, at most 4096 agents) whose policies run the
- * general, ORCA or Karamouzas-sampling kernel: with enable != 0 (the
- * default) the steps of one umans_step / umans_step_async call run in one
- * launch, a block that builds the grid and updates the agents step after
- * step; with 0, one graph launch per step.  Results do not depend on it. */
+/* Small worlds (one scenario, at most 4096 agents, neighbour lists that fit
+ * in shared memory) whose policies run the general, ORCA or
+ * Karamouzas-sampling kernel: with enable != 0 (the default) the steps of
+ * one umans_step / umans_step_async call run in one cooperative launch (one
+ * block builds each step's grid, then every block updates its agents); with
+ * 0, one graph launch per step.  Steps that need host work in between
+ * (trajectory output, agents joining or leaving) take one launch each
+ * either way.  Results do not depend on it. */
 int umans_set_multi_step(umans_sim* sim, int enable);
 /* CrowdSimulator::RunSimulationSteps (crowdSimulator.cpp:77-95): n steps,
  * waits for them, reports device-side errors */
