@@ -790,7 +790,7 @@ bool Engine::configure()
 	// work-list counters: a pair per kernel group, and one for the list dump
 	if (!dalloc(S.work, 2 * (groups_.size() + 1), err_)) return false;
 	CK(cudaMemset(S.work, 0, sizeof(unsigned) * 2 * (groups_.size() + 1)));
-	if (!small_steps_occupancy()) return false;
+	small_steps_occupancy();
 	configured_maxnb_ = maxnb_;
 	invalidate_graph();
 	return true;
@@ -1064,20 +1064,23 @@ bool Engine::launch_small_steps(int nsteps, int blocks, int threads)
 }
 
 // Blocks of k_small_steps resident per SM for the current neighbour
-// capacity (by mode, 4 and 8 warps per block); configure() refreshes them.
-bool Engine::small_steps_occupancy()
+// capacity (by mode, 4 and 8 warps per block; 0 leaves the mode on the
+// graph path); configure() refreshes them.
+void Engine::small_steps_occupancy()
 {
 	const int modes[3] = {0, 2, 3};
 	for (int m : modes) {
 		void (*fn)(DevState, int) = m == 2 ? k_small_steps<2> : (m == 3 ? k_small_steps<3> : k_small_steps<0>);
-		// the kernel's static shared memory (build_small's scan) counts
+		// the kernel's static shared memory (build_small_smem's grid) counts
 		// against the 48 KB default too: allow the whole budget
-		CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMALL_STEPS_SMEM));
+		const bool allowed =
+		    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMALL_STEPS_SMEM) == cudaSuccess;
+		if (!allowed) cudaGetLastError();
 		for (int k = 0; k < 2; ++k) {
 			const int wpb = k == 0 ? 4 : 8;
 			int per_sm = 0;
 			const size_t smem = small_steps_smem(wpb, maxnb_, m);
-			if (smem > SMALL_STEPS_SMEM ||
+			if (!allowed || smem > SMALL_STEPS_SMEM ||
 			    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess) {
 				cudaGetLastError();
 				per_sm = 0;
@@ -1085,7 +1088,6 @@ bool Engine::small_steps_occupancy()
 			small_steps_resident_[m][k] = per_sm;
 		}
 	}
-	return true;
 }
 
 bool Engine::set_multi_step(bool on)

@@ -159,7 +159,7 @@ private:
 	cudaError_t launch_grid_coop(const DevState& S);
 	void probe_grid_coop();
 	bool launch_small_steps(int nsteps, int blocks, int threads);
-	bool small_steps_occupancy();
+	void small_steps_occupancy();
 	int small_steps_resident_[4][2] = {};   // per mode: blocks per SM at 4 and 8 warps per block
 	int coop_state_ = 0;        // one-launch grid build: 0 untried, 1 usable, -1 not capturable
 	int coop_blocks_max_ = 1;
